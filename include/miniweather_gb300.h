@@ -1,0 +1,181 @@
+/*
+ * miniweather_gb300.h -- C ABI of the GB300 (sm_103a) PyMiniWeather time step.
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream
+ * (cudaStream_t passed as void*, NULL = legacy default stream), launches its
+ * kernels on that stream and returns without synchronising.  Nothing here
+ * allocates device memory: temporaries are caller-provided workspaces.
+ *
+ * Layout (the reference's Fields, pyminiweather/data/fields.py:58-123):
+ *   state arrays   : (4, nz+4, nx+4) C order, variables DENS=0 UMOM=1 WMOM=2
+ *                    RHOT=3 (pyminiweather/__init__.py:14-18), 2-cell halo;
+ *   hy_dens_cell, hy_dens_theta_cell             : (nz+4) FP64;
+ *   hy_dens_int, hy_dens_theta_int, hy_pressure_int : (nz+1) FP64.
+ * Backgrounds stay FP64 for every storage type.
+ *
+ * Return value: MW_OK (0) or one of the MW_ERR_* codes below; the message of
+ * the last failure on the calling thread is given by mw_last_error().
+ * Requirements checked before any launch: nx >= 2 (the periodic halo is two
+ * cells wide), nz >= 1, 4*(nx+4)*(nz+4) < 2^40, non-NULL pointers, naturally
+ * aligned FP64 / FP32 arrays, finite positive dx, dz and time steps.
+ */
+#ifndef MINIWEATHER_GB300_H
+#define MINIWEATHER_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MW_ABI_VERSION 1
+
+enum mw_status {
+  MW_OK = 0,
+  MW_ERR_INVALID_ARG = 1, /* NULL pointer, non-finite or non-positive scalar, bad enum */
+  MW_ERR_SHAPE = 2,       /* grid sizes outside the supported range */
+  MW_ERR_ALIGN = 3,       /* misaligned pointer */
+  MW_ERR_ALIAS = 4,       /* output overlaps an input it must not overlap */
+  MW_ERR_CUDA = 5,        /* a CUDA call or kernel launch failed */
+  MW_ERR_WORKSPACE = 6,   /* workspace too small */
+  MW_ERR_NONFINITE = 7    /* a device-side check found NaN or Inf */
+};
+
+enum mw_direction { MW_DIR_X = 0, MW_DIR_Z = 1 }; /* ics/directions.py:4-6 */
+
+/* Arithmetic of the FP64-storage direction-stage kernels. */
+enum mw_f64_mode {
+  MW_F64_NATIVE = 0, /* every operation on the FP64 pipe, the reference's formulas */
+  MW_F64_SPLIT = 1   /* GB300 form: FP64 loads/stores and update, interior
+                        arithmetic in pairs of FP32 (about 2^-46 relative) */
+};
+
+/* Flags of the direction-stage and step entry points. */
+#define MW_FLAG_WRITE_HALO 1u /* write the halo cells into the forcing array
+                                 as set_bc_x / set_bc_z do (ics/bcs.py:8-148) */
+
+/* Background profile of the initial condition. */
+enum mw_background {
+  MW_BG_CONST_THETA = 0, /* hydro_const_theta, ics/initial_conditions.py:26-52 */
+  MW_BG_BVFREQ = 1       /* hydro_const_bvfreq with N = 0.02, initial_conditions.py:54-81 */
+};
+
+#define MW_MAX_BUBBLES 8
+
+const char* mw_last_error(void);
+const char* mw_status_string(int status);
+int mw_abi_version(void);
+
+/* ---------------------------------------------------------------------------
+ * One direction-stage: replaces discrete_step (pyminiweather/solve/step.py:21-82)
+ * with set_bc_x/z (ics/bcs.py:8-148), interpolate_x/z, compute_flux_x/z,
+ * compute_tend_x/z (solve/interpolate.py:10-250) and add_source_terms
+ * (solve/source.py:53-75) fused into one kernel:
+ *   out[interior] = init[interior] + dt_stage * tend(forcing)
+ * The halo is synthesised from the periodic (x) / wall (z) rule; halo cells
+ * of the arrays are never read.  dt_full is params["dt"] (the hyperviscosity
+ * time scale, interpolate.py:99-101,147-149).  src_w (nz, nx) is the optional
+ * forcing added to the w tendency (the gravity-wave source), NULL for none.
+ * `out` may equal `init`; it must not overlap `forcing` (MW_ERR_ALIAS).
+ * ------------------------------------------------------------------------- */
+int mw_dirstage_f64(int nx, int nz, double dx, double dz, double dt_full, const double* hy_dens_cell,
+                    const double* hy_dens_theta_cell, const double* hy_dens_int, const double* hy_dens_theta_int,
+                    const double* hy_pressure_int, const double* src_w, const double* init, double* forcing,
+                    double* out, double dt_stage, int direction, int f64_mode, unsigned flags, void* stream);
+
+/* FP32 perturbation fields (precision form); backgrounds FP64, converted per row. */
+int mw_dirstage_f32(int nx, int nz, double dx, double dz, double dt_full, const double* hy_dens_cell,
+                    const double* hy_dens_theta_cell, const double* hy_dens_int, const double* hy_dens_theta_int,
+                    const double* hy_pressure_int, const double* src_w, const float* init, float* forcing,
+                    float* out, double dt_stage, int direction, unsigned flags, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * nsteps full time steps: replaces evolve (pyminiweather/solve/step.py:85-143).
+ * Per step the direction order is [Z, X] when *reverse == 0 and [X, Z] when 1
+ * (the reference's module-global reverse_direction), toggled after each step;
+ * *reverse is a host int updated in place.  Per direction the three RK stages
+ * run with dt/3, dt/2, dt:
+ *   scratch = S + dt/3 L(S);  state_tmp = S + dt/2 L(scratch);  S = S + dt L(state_tmp)
+ * so state_tmp ends holding what the reference's state_tmp holds.  scratch is
+ * a third state-sized array (the fused kernel cannot update in place).  dt is
+ * evolve's time step; dt_full is params["dt"], the hyperviscosity time scale
+ * (the reference uses both, step.py:85 and interpolate.py:99-101).
+ * ------------------------------------------------------------------------- */
+int mw_step_f64(int nx, int nz, double dx, double dz, double dt_full, double dt, const double* hy_dens_cell,
+                const double* hy_dens_theta_cell, const double* hy_dens_int, const double* hy_dens_theta_int,
+                const double* hy_pressure_int, const double* src_w, double* state, double* state_tmp,
+                double* scratch, int nsteps, int* reverse, int f64_mode, unsigned flags, void* stream);
+
+int mw_step_f32(int nx, int nz, double dx, double dz, double dt_full, double dt, const double* hy_dens_cell,
+                const double* hy_dens_theta_cell, const double* hy_dens_int, const double* hy_dens_theta_int,
+                const double* hy_pressure_int, const double* src_w, float* state, float* state_tmp, float* scratch,
+                int nsteps, int* reverse, unsigned flags, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Initial condition: replaces init (pyminiweather/ics/initial.py:11-105):
+ * 3x3 Gauss-Legendre cell averages over all (nz+4)(nx+4) cells of the bubbles
+ * (sample_ellipse_cosine, utils/utils.py:5-51), plus the hydrostatic
+ * backgrounds at cell centres and interfaces, all in FP64.  bubbles is a HOST
+ * array of nbubble x (amplitude, x0, z0, xrad, zrad); u0 is the constant
+ * initial wind (15 m/s for the gravity-wave case, 0 otherwise).
+ * The _f32 form computes in FP64 and rounds the state once at the end.
+ * ------------------------------------------------------------------------- */
+int mw_init_f64(int nx, int nz, double xlen, double zlen, int background, double u0, int nbubble,
+                const double* bubbles, double* state, double* hy_dens_cell, double* hy_dens_theta_cell,
+                double* hy_dens_int, double* hy_dens_theta_int, double* hy_pressure_int, void* stream);
+int mw_init_f32(int nx, int nz, double xlen, double zlen, int background, double u0, int nbubble,
+                const double* bubbles, float* state, double* hy_dens_cell, double* hy_dens_theta_cell,
+                double* hy_dens_int, double* hy_dens_theta_int, double* hy_pressure_int, void* stream);
+
+/* GravityBCSourceTerm (pyminiweather/solve/source.py:20-50): src_w (nz, nx) =
+ * sample_ellipse_cosine(cell centres, 0.01, xlen/8, 1000, 500, 500) * hy_dens_cell. */
+int mw_gravity_source_f64(int nx, int nz, double xlen, double zlen, const double* hy_dens_cell, double* src_w,
+                          void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Domain totals: replaces compute_stats (pyminiweather/post/stats.py:8-35).
+ * out2 (device, 2 doubles) receives (total mass, total energy), summed in FP64
+ * in a fixed order (deterministic).  workspace must hold
+ * mw_stats_workspace_bytes(nx, nz) bytes.
+ * ------------------------------------------------------------------------- */
+size_t mw_stats_workspace_bytes(int nx, int nz);
+int mw_stats_f64(int nx, int nz, double dx, double dz, const double* hy_dens_cell, const double* hy_dens_theta_cell,
+                 const double* state, void* workspace, size_t workspace_bytes, double* out2, void* stream);
+int mw_stats_f32(int nx, int nz, double dx, double dz, const double* hy_dens_cell, const double* hy_dens_theta_cell,
+                 const float* state, void* workspace, size_t workspace_bytes, double* out2, void* stream);
+
+/* compute_solution_variables (pyminiweather/post/stats.py:38-69): out (4, nz, nx)
+ * = (rho', u, w, theta'). */
+int mw_solution_variables_f64(int nx, int nz, const double* hy_dens_cell, const double* hy_dens_theta_cell,
+                              const double* state, double* out, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Unfused pieces of one direction-stage, for callers that use the reference's
+ * fine-grained functions.  Intermediate shapes follow data/fields.py:67-78.
+ * ------------------------------------------------------------------------- */
+/* set_bc_x / set_bc_z (ics/bcs.py:8-39, 67-148), in place on `state`. */
+int mw_set_bc_f64(int nx, int nz, const double* hy_dens_cell, double* state, int direction, void* stream);
+/* interpolate_x (vals, d3: (4, nz, nx+1)) / interpolate_z ((4, nz+1, nx)),
+ * solve/interpolate.py:10-79; reads the halo cells of `state` as stored. */
+int mw_interpolate_f64(int nx, int nz, const double* state, double* vals, double* d3, int direction, void* stream);
+/* compute_flux_x / compute_flux_z (solve/interpolate.py:82-186): flux (4, nz+1, nx+1);
+ * the z form zeroes d3[DENS] at interfaces 0 and nz in place, as the reference does. */
+int mw_flux_f64(int nx, int nz, double dx, double dz, double dt_full, const double* hy_dens_cell,
+                const double* hy_dens_theta_cell, const double* hy_dens_int, const double* hy_dens_theta_int,
+                const double* hy_pressure_int, const double* vals, double* d3, double* flux, int direction,
+                void* stream);
+/* compute_tend_x / compute_tend_z (solve/interpolate.py:189-250) plus the
+ * optional src_w forcing: tend (4, nz, nx). */
+int mw_tend_f64(int nx, int nz, double dx, double dz, const double* flux, const double* state_forcing,
+                const double* src_w, double* tend, int direction, void* stream);
+/* add_source_terms (pyminiweather/solve/source.py:53-75) for the gravity-wave
+ * case: tend[WMOM] += src_w. */
+int mw_add_source_f64(int nx, int nz, const double* src_w, double* tend, void* stream);
+/* The stage update of discrete_step (solve/step.py:80-82). */
+int mw_update_f64(int nx, int nz, const double* init, const double* tend, double* out, double dt_stage, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MINIWEATHER_GB300_H */

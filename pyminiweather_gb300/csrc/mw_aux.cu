@@ -1,0 +1,611 @@
+// mw_aux.cu -- initial condition, diagnostics and the unfused pieces of one
+// direction-stage.  Everything here is FP64 (the precision form keeps the
+// initial condition, backgrounds and reductions in FP64 too).
+//
+// The unfused kernels follow the reference's NumPy expressions operation by
+// operation with explicitly rounded intrinsics (__dadd_rn, __dmul_rn, ...),
+// so that no multiply-add is contracted and results round exactly as NumPy's
+// do, pow and cos aside.
+#include "mw_common.cuh"
+#include "mw_split.cuh"
+
+namespace mw {
+
+namespace {
+
+__device__ __forceinline__ double add_(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub_(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double mul_(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double div_(double a, double b) { return __ddiv_rn(a, b); }
+
+// numpy.linspace(start, stop, num, endpoint=False)[k]
+__device__ __forceinline__ double linspace_at(double start, double stop, int num, int k) {
+  const double step = div_(sub_(stop, start), (double)num);
+  return add_(mul_((double)k, step), start);
+}
+
+// pyminiweather/data/quadrature.py:15-30
+__constant__ double c_qp[3] = {0.112701665379258311482073460022, 0.500000000000000000000000000000,
+                               0.887298334620741688517926539980};
+__constant__ double c_qw[3] = {0.277777777777777777777777777779, 0.444444444444444444444444444444,
+                               0.277777777777777777777777777779};
+
+// hydro_const_theta / hydro_const_bvfreq, ics/initial_conditions.py:26-81
+__device__ void hydro(int bg, double z, double* hr, double* ht) {
+  if (bg == MW_BG_BVFREQ) {
+    const double bv0 = 0.02;
+    const double t = mul_(kTheta0, exp(mul_(div_(mul_(bv0, bv0), kGrav), z)));
+    const double exner =
+        sub_(kExner0, div_(mul_(div_(mul_(kGrav, kGrav), mul_(mul_(kCp, bv0), bv0)), sub_(t, kTheta0)),
+                           mul_(t, kTheta0)));
+    const double p = mul_(kP0, pow(exner, kCp / kRd));
+    *ht = t;
+    *hr = div_(pow(div_(p, kC0), 1.0 / kGamma), t);
+  } else {
+    const double exner = sub_(kExner0, div_(mul_(kGrav, z), mul_(kCp, kTheta0)));
+    const double p = mul_(kP0, pow(exner, kCp / kRd));
+    *ht = kTheta0;
+    *hr = div_(pow(div_(p, kC0), 1.0 / kGamma), kTheta0);
+  }
+}
+
+struct Bubbles {
+  int n;
+  double b[MW_MAX_BUBBLES][5];  // amplitude, x0, z0, xrad, zrad
+};
+
+// sample_ellipse_cosine, utils/utils.py:5-51
+__device__ __forceinline__ double ellipse_cos2(double x, double z, const double* B) {
+  const double a = div_(sub_(x, B[1]), B[3]);
+  const double b = div_(sub_(z, B[2]), B[4]);
+  const double dist = div_(mul_(sqrt(add_(mul_(a, a), mul_(b, b))), kPi), 2.0);
+  if (dist <= kPi / 2.0) {
+    const double c = cos(dist);
+    return mul_(B[0], mul_(c, c));
+  }
+  return 0.0;
+}
+
+// init(), ics/initial.py:57-77: one CTA per halo-indexed row.
+template <typename T>
+__global__ void k_init_state(int nx, int nz, double dx, double dz, int bg, double u0, Bubbles bub, T* state) {
+  __shared__ double s_hr[3], s_ht[3], s_z[3];
+  const int NX = nx + 2 * kHs, NZ = nz + 2 * kHs;
+  const long long plane = (long long)NX * NZ;
+  const int k = blockIdx.x;
+  const double zm = linspace_at(-kHs * dz, (nz + kHs) * dz, NZ, k);
+  if (threadIdx.x < 3) {
+    const double z = add_(zm, mul_(c_qp[threadIdx.x], dz));
+    s_z[threadIdx.x] = z;
+    hydro(bg, z, &s_hr[threadIdx.x], &s_ht[threadIdx.x]);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < NX; i += blockDim.x) {
+    const double xm = linspace_at(-kHs * dx, (nx + kHs) * dx, NX, i);
+    double acc[4][3];
+#pragma unroll
+    for (int qa = 0; qa < 3; ++qa) {
+      const double z = s_z[qa], hr = s_hr[qa], ht = s_ht[qa];
+#pragma unroll
+      for (int qb = 0; qb < 3; ++qb) {
+        const double x = add_(xm, mul_(c_qp[qb], dx));
+        double t = 0.0;
+        for (int n = 0; n < bub.n; ++n) t = add_(t, ellipse_cos2(x, z, bub.b[n]));
+        const double W = mul_(c_qw[qa], c_qw[qb]);
+        const double r = 0.0;
+        const double v0 = mul_(r, W);
+        const double v1 = mul_(mul_(add_(r, hr), u0), W);
+        const double v2 = mul_(mul_(add_(r, hr), 0.0), W);
+        const double v3 = mul_(sub_(mul_(add_(r, hr), add_(t, ht)), mul_(hr, ht)), W);
+        if (qb == 0) {
+          acc[0][qa] = v0; acc[1][qa] = v1; acc[2][qa] = v2; acc[3][qa] = v3;
+        } else {
+          acc[0][qa] = add_(acc[0][qa], v0); acc[1][qa] = add_(acc[1][qa], v1);
+          acc[2][qa] = add_(acc[2][qa], v2); acc[3][qa] = add_(acc[3][qa], v3);
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      state[q * plane + (long long)k * NX + i] = (T)add_(add_(acc[q][0], acc[q][1]), acc[q][2]);
+  }
+}
+
+// Backgrounds, ics/initial.py:84-105.
+__global__ void k_init_background(int nz, double dz, int bg, double* hyc, double* hytc, double* hyi, double* hyti,
+                                  double* hypi) {
+  const int NZ = nz + 2 * kHs;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < NZ; k += gridDim.x * blockDim.x) {
+    const double z = linspace_at((-kHs + 0.5) * dz, (nz + kHs + 0.5) * dz, NZ, k);
+    double hr, ht;
+    hydro(bg, z, &hr, &ht);
+    const double sumw = add_(add_(c_qw[0], c_qw[1]), c_qw[2]);
+    hyc[k] = mul_(hr, sumw);
+    const double a = mul_(ht, hr);
+    hytc[k] = add_(add_(mul_(a, c_qw[0]), mul_(a, c_qw[1])), mul_(a, c_qw[2]));
+    if (k <= nz) {
+      const double ze = linspace_at(0.0, (nz + 1) * dz, nz + 1, k);
+      hydro(bg, ze, &hr, &ht);
+      hyi[k] = hr;
+      hyti[k] = mul_(hr, ht);
+      hypi[k] = mul_(kC0, pow(mul_(hr, ht), kGamma));
+    }
+  }
+}
+
+// GravityBCSourceTerm, solve/source.py:20-50
+__global__ void k_gravity_source(int nx, int nz, double xlen, double zlen, const double* hyc, double* src) {
+  const double dx = xlen / nx, dz = zlen / nz;
+  double B[5] = {0.01, xlen / 8, 1000.0, 500.0, 500.0};
+  const long long n = (long long)nx * nz;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(idx / nx), i = (int)(idx % nx);
+    const double z = linspace_at(dz / 2.0, zlen + dz / 2.0, nz, k);
+    const double x = linspace_at(dx / 2.0, xlen + dx / 2.0, nx, i);
+    src[idx] = mul_(ellipse_cos2(x, z, B), hyc[k + kHs]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// compute_stats, post/stats.py:8-35.  Level 1: block b reduces rows
+// [b*rpb, (b+1)*rpb) into workspace[2b .. 2b+1]; level 2 reduces the block
+// partials.  Both levels use fixed trees, so the result does not depend on
+// scheduling.
+constexpr int kStatThreads = 256;
+constexpr int kStatMaxBlocks = 1024;
+
+__device__ __forceinline__ double load_state(const double* p) { return *p; }
+__device__ __forceinline__ double load_state(const float* p) { return split::f2d(*p); }
+
+template <typename T>
+__global__ void __launch_bounds__(kStatThreads) k_stats_partial(int nx, int nz, int rpb, double dx, double dz,
+                                                                const double* hyc, const double* hytc, const T* state,
+                                                                double* part) {
+  __shared__ double sm[kStatThreads], se[kStatThreads];
+  const int NX = nx + 2 * kHs;
+  const long long plane = (long long)NX * (nz + 2 * kHs);
+  double m = 0.0, e = 0.0;
+  const int k0 = blockIdx.x * rpb, k1 = min(k0 + rpb, nz);
+  for (int k = k0; k < k1; ++k) {
+    const int kk = k + kHs;
+    const double hr = hyc[kk], hrt = hytc[kk];
+    for (int i = threadIdx.x; i < nx; i += kStatThreads) {
+      const long long o = (long long)kk * NX + i + kHs;
+      const double rho = add_(load_state(state + o), hr);
+      const double u = div_(load_state(state + plane + o), rho);
+      const double w = div_(load_state(state + 2 * plane + o), rho);
+      const double th = div_(add_(load_state(state + 3 * plane + o), hrt), rho);
+      const double p = mul_(kC0, pow(mul_(rho, th), kGamma));
+      const double t = div_(th, pow(div_(kP0, p), kRd / kCp));
+      const double ke = mul_(rho, add_(mul_(u, u), mul_(w, w)));
+      const double ie = mul_(mul_(rho, kCv), t);
+      m = add_(m, rho);
+      e = add_(e, add_(ke, ie));
+    }
+  }
+  sm[threadIdx.x] = m;
+  se[threadIdx.x] = e;
+  __syncthreads();
+  for (int s = kStatThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      sm[threadIdx.x] = add_(sm[threadIdx.x], sm[threadIdx.x + s]);
+      se[threadIdx.x] = add_(se[threadIdx.x], se[threadIdx.x + s]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = sm[0];
+    part[2 * blockIdx.x + 1] = se[0];
+  }
+}
+
+__global__ void __launch_bounds__(kStatMaxBlocks) k_stats_final(int nblocks, double dx, double dz, const double* part,
+                                                                double* out2) {
+  __shared__ double sm[kStatMaxBlocks], se[kStatMaxBlocks];
+  const int t = threadIdx.x;
+  sm[t] = t < nblocks ? part[2 * t] : 0.0;
+  se[t] = t < nblocks ? part[2 * t + 1] : 0.0;
+  __syncthreads();
+  for (int s = kStatMaxBlocks / 2; s > 0; s >>= 1) {
+    if (t < s) {
+      sm[t] = add_(sm[t], sm[t + s]);
+      se[t] = add_(se[t], se[t + s]);
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+    out2[0] = mul_(mul_(sm[0], dx), dz);
+    out2[1] = mul_(mul_(se[0], dx), dz);
+  }
+}
+
+int stats_blocks(int nz, int* rpb) {
+  const int nb = nz < kStatMaxBlocks ? nz : kStatMaxBlocks;
+  *rpb = (nz + nb - 1) / nb;
+  return (nz + *rpb - 1) / *rpb;
+}
+
+template <typename T>
+int run_stats(int nx, int nz, double dx, double dz, const double* hyc, const double* hytc, const T* state,
+              void* workspace, size_t workspace_bytes, double* out2, cudaStream_t stream) {
+  int st = check_grid(nx, nz);
+  if (st) return st;
+  MW_REQUIRE(hyc && hytc && state && workspace && out2, MW_ERR_INVALID_ARG, "NULL pointer argument");
+  MW_REQUIRE(finite_pos(dx) && finite_pos(dz), MW_ERR_INVALID_ARG, "dx, dz must be finite and positive");
+  MW_REQUIRE(aligned(state) && aligned(hyc) && aligned(hytc) && aligned(out2) && ((uintptr_t)workspace % 8) == 0,
+             MW_ERR_ALIGN, "misaligned pointer");
+  const size_t need = mw_stats_workspace_bytes(nx, nz);
+  MW_REQUIRE(workspace_bytes >= need, MW_ERR_WORKSPACE, "stats workspace needs %zu bytes, got %zu", need,
+             workspace_bytes);
+  int rpb;
+  const int nb = stats_blocks(nz, &rpb);
+  k_stats_partial<T><<<nb, kStatThreads, 0, stream>>>(nx, nz, rpb, dx, dz, hyc, hytc, state, (double*)workspace);
+  st = check_launch("stats partial launch");
+  if (st) return st;
+  k_stats_final<<<1, kStatMaxBlocks, 0, stream>>>(nb, dx, dz, (const double*)workspace, out2);
+  return check_launch("stats final launch");
+}
+
+// compute_solution_variables, post/stats.py:38-69
+__global__ void k_solution_vars(int nx, int nz, const double* hyc, const double* hytc, const double* state,
+                                double* out) {
+  const int NX = nx + 2 * kHs;
+  const long long plane = (long long)NX * (nz + 2 * kHs);
+  const long long n = (long long)nx * nz;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(idx / nx), i = (int)(idx % nx);
+    const long long o = (long long)(k + kHs) * NX + i + kHs;
+    const double hr = hyc[k + kHs], hrt = hytc[k + kHs];
+    const double d = state[o];
+    out[idx] = d;
+    out[n + idx] = div_(state[plane + o], add_(hr, d));
+    out[2 * n + idx] = div_(state[2 * plane + o], add_(hr, d));
+    out[3 * n + idx] = sub_(div_(add_(state[3 * plane + o], hrt), add_(hr, d)), div_(hrt, hr));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Unfused pieces.
+__global__ void k_set_bc(int nx, int nz, const double* hyc, double* f, int dir) {
+  const int NX = nx + 2 * kHs;
+  const long long plane = (long long)NX * (nz + 2 * kHs);
+  if (dir == MW_DIR_X) {  // ics/bcs.py:35-39, interior rows
+    const long long n = 4LL * nz;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+         idx += (long long)gridDim.x * blockDim.x) {
+      const int q = (int)(idx / nz), k = (int)(idx % nz);
+      double* row = f + q * plane + (long long)(k + kHs) * NX;
+      row[0] = row[nx];
+      row[1] = row[nx + 1];
+      row[nx + kHs] = row[kHs];
+      row[nx + kHs + 1] = row[kHs + 1];
+    }
+  } else {  // ics/bcs.py:92-148, all nx+4 columns
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < NX; c += gridDim.x * blockDim.x) {
+      auto at = [&](int q, int r) -> double& { return f[q * plane + (long long)r * NX + c]; };
+      at(WMOM, 0) = 0.0;
+      at(WMOM, 1) = 0.0;
+      at(WMOM, nz + kHs) = 0.0;
+      at(WMOM, nz + kHs + 1) = 0.0;
+      at(UMOM, 0) = mul_(div_(at(UMOM, kHs), hyc[kHs]), hyc[0]);
+      at(UMOM, 1) = mul_(div_(at(UMOM, kHs), hyc[kHs]), hyc[1]);
+      at(UMOM, nz + kHs) = mul_(div_(at(UMOM, nz + kHs - 1), hyc[nz + kHs - 1]), hyc[nz + kHs]);
+      at(UMOM, nz + kHs + 1) = mul_(div_(at(UMOM, nz + kHs - 1), hyc[nz + kHs - 1]), hyc[nz + kHs + 1]);
+      for (int q = 0; q < 4; q += 3) {  // DENS and RHOT
+        at(q, 0) = at(q, kHs);
+        at(q, 1) = at(q, kHs);
+        at(q, nz + kHs) = at(q, nz + kHs - 1);
+        at(q, nz + kHs + 1) = at(q, nz + kHs - 1);
+      }
+    }
+  }
+}
+
+// scipy.signal.convolve(mode="same")[..., 2:-1] accumulation order
+__device__ __forceinline__ double interp4_rn(double s0, double s1, double s2, double s3) {
+  const double k0 = -1.0 / 12, k1 = 7.0 / 12;
+  return add_(add_(add_(mul_(s0, k0), mul_(s1, k1)), mul_(s2, k1)), mul_(s3, k0));
+}
+__device__ __forceinline__ double diff3_rn(double s0, double s1, double s2, double s3) {
+  return add_(add_(add_(mul_(s0, -1.0), mul_(s1, 3.0)), mul_(s2, -3.0)), mul_(s3, 1.0));
+}
+
+__global__ void k_interpolate(int nx, int nz, const double* s, double* vals, double* d3, int dir) {
+  const int NX = nx + 2 * kHs;
+  const long long plane = (long long)NX * (nz + 2 * kHs);
+  const int ni = dir == MW_DIR_X ? nx + 1 : nx;  // columns of the output
+  const int nk = dir == MW_DIR_X ? nz : nz + 1;  // rows of the output
+  const long long n = 4LL * nk * ni;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+    const int q = (int)(idx / ((long long)nk * ni));
+    const int r = (int)((idx / ni) % nk), i = (int)(idx % ni);
+    double t[4];
+    if (dir == MW_DIR_X) {
+      const double* row = s + q * plane + (long long)(r + kHs) * NX + i;
+      t[0] = row[0]; t[1] = row[1]; t[2] = row[2]; t[3] = row[3];
+    } else {
+      const double* col = s + q * plane + (long long)r * NX + i + kHs;
+      t[0] = col[0]; t[1] = col[NX]; t[2] = col[2 * NX]; t[3] = col[3 * NX];
+    }
+    vals[idx] = interp4_rn(t[0], t[1], t[2], t[3]);
+    d3[idx] = diff3_rn(t[0], t[1], t[2], t[3]);
+  }
+}
+
+struct FluxArgs {
+  int nx, nz;
+  double hv;
+  const double *hyc, *hytc, *hyi, *hyti, *hypi;
+  const double* vals;
+  double* d3;
+  double* flux;
+  int dir;
+};
+
+__global__ void k_flux(FluxArgs a) {
+  const int ni = a.dir == MW_DIR_X ? a.nx + 1 : a.nx;
+  const int nk = a.dir == MW_DIR_X ? a.nz : a.nz + 1;
+  const long long vplane = (long long)nk * ni;               // vals/d3 plane
+  const long long fplane = (long long)(a.nz + 1) * (a.nx + 1);  // flux plane
+  const long long n = vplane;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(idx / ni), i = (int)(idx % ni);
+    double v[4], d[4];
+    for (int q = 0; q < 4; ++q) {
+      v[q] = a.vals[q * vplane + idx];
+      d[q] = a.d3[q * vplane + idx];
+    }
+    const long long fo = (long long)r * (a.nx + 1) + i;
+    if (a.dir == MW_DIR_X) {  // interpolate.py:105-129
+      const double rho = add_(v[DENS], a.hyc[r + kHs]);
+      const double u = div_(v[UMOM], rho);
+      const double w = div_(v[WMOM], rho);
+      const double t = div_(add_(v[RHOT], a.hytc[r + kHs]), rho);
+      const double p = mul_(kC0, pow(mul_(rho, t), kGamma));
+      a.flux[0 * fplane + fo] = sub_(mul_(rho, u), mul_(a.hv, d[DENS]));
+      a.flux[1 * fplane + fo] = sub_(add_(mul_(rho, mul_(u, u)), p), mul_(a.hv, d[UMOM]));
+      a.flux[2 * fplane + fo] = sub_(mul_(mul_(rho, u), w), mul_(a.hv, d[WMOM]));
+      a.flux[3 * fplane + fo] = sub_(mul_(mul_(rho, u), t), mul_(a.hv, d[RHOT]));
+    } else {  // interpolate.py:153-186
+      const double rho = add_(v[DENS], a.hyi[r]);
+      const double u = div_(v[UMOM], rho);
+      double w = div_(v[WMOM], rho);
+      const double t = div_(add_(v[RHOT], a.hyti[r]), rho);
+      const double p = sub_(mul_(kC0, pow(mul_(rho, t), kGamma)), a.hypi[r]);
+      if (r == 0 || r == a.nz) {
+        w = 0.0;
+        d[DENS] = 0.0;
+        a.d3[DENS * vplane + idx] = 0.0;
+      }
+      a.flux[0 * fplane + fo] = sub_(mul_(rho, w), mul_(a.hv, d[DENS]));
+      a.flux[1 * fplane + fo] = sub_(mul_(mul_(rho, w), u), mul_(a.hv, d[UMOM]));
+      a.flux[2 * fplane + fo] = sub_(add_(mul_(rho, mul_(w, w)), p), mul_(a.hv, d[WMOM]));
+      a.flux[3 * fplane + fo] = sub_(mul_(mul_(rho, w), t), mul_(a.hv, d[RHOT]));
+    }
+  }
+}
+
+__global__ void k_tend(int nx, int nz, double d, const double* flux, const double* forcing, const double* srcw,
+                       double* tend, int dir) {
+  const int NX = nx + 2 * kHs;
+  const long long splane = (long long)NX * (nz + 2 * kHs);
+  const long long fplane = (long long)(nz + 1) * (nx + 1);
+  const long long tplane = (long long)nz * nx;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < tplane;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(idx / nx), i = (int)(idx % nx);
+    const long long f0 = (long long)k * (nx + 1) + i;
+    const long long f1 = dir == MW_DIR_X ? f0 + 1 : f0 + (nx + 1);
+    for (int q = 0; q < 4; ++q) {
+      double t = div_(-sub_(flux[q * fplane + f1], flux[q * fplane + f0]), d);
+      if (q == WMOM && dir == MW_DIR_Z)
+        t = sub_(t, mul_(forcing[DENS * splane + (long long)(k + kHs) * NX + i + kHs], kGrav));
+      if (q == WMOM && srcw) t = add_(t, srcw[idx]);
+      tend[q * tplane + idx] = t;
+    }
+  }
+}
+
+__global__ void k_update(int nx, int nz, const double* init, const double* tend, double* out, double dt) {
+  const int NX = nx + 2 * kHs;
+  const long long splane = (long long)NX * (nz + 2 * kHs);
+  const long long tplane = (long long)nz * nx;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < 4 * tplane;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int q = (int)(idx / tplane);
+    const long long r = idx % tplane;
+    const int k = (int)(r / nx), i = (int)(r % nx);
+    const long long o = q * splane + (long long)(k + kHs) * NX + i + kHs;
+    out[o] = add_(init[o], mul_(dt, tend[idx]));
+  }
+}
+
+__global__ void k_add_source(int nx, int nz, const double* srcw, double* tend) {
+  const long long tplane = (long long)nz * nx;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < tplane;
+       idx += (long long)gridDim.x * blockDim.x)
+    tend[WMOM * tplane + idx] = add_(tend[WMOM * tplane + idx], srcw[idx]);
+}
+
+inline unsigned grid_for(long long n, int threads) {
+  long long b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  if (b > 65535LL * 16) b = 65535LL * 16;
+  return (unsigned)b;
+}
+
+int check_bubbles(int nbubble, const double* bubbles, Bubbles* out) {
+  MW_REQUIRE(nbubble >= 0 && nbubble <= MW_MAX_BUBBLES, MW_ERR_INVALID_ARG, "nbubble must be in [0, %d]",
+             MW_MAX_BUBBLES);
+  MW_REQUIRE(nbubble == 0 || bubbles, MW_ERR_INVALID_ARG, "bubbles must not be NULL when nbubble > 0");
+  out->n = nbubble;
+  for (int n = 0; n < MW_MAX_BUBBLES; ++n)
+    for (int j = 0; j < 5; ++j) out->b[n][j] = n < nbubble ? bubbles[5 * n + j] : 0.0;
+  for (int n = 0; n < nbubble; ++n) {
+    MW_REQUIRE(std::isfinite(out->b[n][0]) && std::isfinite(out->b[n][1]) && std::isfinite(out->b[n][2]),
+               MW_ERR_INVALID_ARG, "bubble %d: non-finite amplitude or centre", n);
+    MW_REQUIRE(finite_pos(out->b[n][3]) && finite_pos(out->b[n][4]), MW_ERR_INVALID_ARG,
+               "bubble %d: radii must be finite and positive", n);
+  }
+  return MW_OK;
+}
+
+template <typename T>
+int run_init(int nx, int nz, double xlen, double zlen, int background, double u0, int nbubble, const double* bubbles,
+             T* state, double* hyc, double* hytc, double* hyi, double* hyti, double* hypi, cudaStream_t stream) {
+  int st = check_grid(nx, nz);
+  if (st) return st;
+  MW_REQUIRE(finite_pos(xlen) && finite_pos(zlen), MW_ERR_INVALID_ARG, "xlen, zlen must be finite and positive");
+  MW_REQUIRE(std::isfinite(u0), MW_ERR_INVALID_ARG, "u0 must be finite");
+  MW_REQUIRE(background == MW_BG_CONST_THETA || background == MW_BG_BVFREQ, MW_ERR_INVALID_ARG,
+             "unknown background %d", background);
+  MW_REQUIRE(state && hyc && hytc && hyi && hyti && hypi, MW_ERR_INVALID_ARG, "NULL pointer argument");
+  MW_REQUIRE(aligned(state) && aligned(hyc) && aligned(hytc) && aligned(hyi) && aligned(hyti) && aligned(hypi),
+             MW_ERR_ALIGN, "misaligned pointer");
+  Bubbles b;
+  st = check_bubbles(nbubble, bubbles, &b);
+  if (st) return st;
+  const double dx = xlen / nx, dz = zlen / nz;
+  k_init_state<T><<<nz + 2 * kHs, 256, 0, stream>>>(nx, nz, dx, dz, background, u0, b, state);
+  st = check_launch("initial condition launch");
+  if (st) return st;
+  k_init_background<<<grid_for(nz + 2 * kHs, 128), 128, 0, stream>>>(nz, dz, background, hyc, hytc, hyi, hyti, hypi);
+  return check_launch("background launch");
+}
+
+}  // namespace
+}  // namespace mw
+
+using namespace mw;
+
+extern "C" int mw_init_f64(int nx, int nz, double xlen, double zlen, int background, double u0, int nbubble,
+                           const double* bubbles, double* state, double* hyc, double* hytc, double* hyi, double* hyti,
+                           double* hypi, void* stream) {
+  return run_init<double>(nx, nz, xlen, zlen, background, u0, nbubble, bubbles, state, hyc, hytc, hyi, hyti, hypi,
+                          (cudaStream_t)stream);
+}
+
+extern "C" int mw_init_f32(int nx, int nz, double xlen, double zlen, int background, double u0, int nbubble,
+                           const double* bubbles, float* state, double* hyc, double* hytc, double* hyi, double* hyti,
+                           double* hypi, void* stream) {
+  return run_init<float>(nx, nz, xlen, zlen, background, u0, nbubble, bubbles, state, hyc, hytc, hyi, hyti, hypi,
+                         (cudaStream_t)stream);
+}
+
+extern "C" int mw_gravity_source_f64(int nx, int nz, double xlen, double zlen, const double* hyc, double* src_w,
+                                     void* stream) {
+  int st = check_grid(nx, nz);
+  if (st) return st;
+  MW_REQUIRE(finite_pos(xlen) && finite_pos(zlen), MW_ERR_INVALID_ARG, "xlen, zlen must be finite and positive");
+  MW_REQUIRE(hyc && src_w, MW_ERR_INVALID_ARG, "NULL pointer argument");
+  MW_REQUIRE(aligned(hyc) && aligned(src_w), MW_ERR_ALIGN, "misaligned pointer");
+  k_gravity_source<<<grid_for((long long)nx * nz, 256), 256, 0, (cudaStream_t)stream>>>(nx, nz, xlen, zlen, hyc, src_w);
+  return check_launch("gravity source launch");
+}
+
+extern "C" size_t mw_stats_workspace_bytes(int nx, int nz) {
+  (void)nx;
+  if (nz < 1) return 0;
+  int rpb;
+  return sizeof(double) * 2 * (size_t)stats_blocks(nz, &rpb);
+}
+
+extern "C" int mw_stats_f64(int nx, int nz, double dx, double dz, const double* hyc, const double* hytc,
+                            const double* state, void* workspace, size_t workspace_bytes, double* out2, void* stream) {
+  return run_stats<double>(nx, nz, dx, dz, hyc, hytc, state, workspace, workspace_bytes, out2, (cudaStream_t)stream);
+}
+
+extern "C" int mw_stats_f32(int nx, int nz, double dx, double dz, const double* hyc, const double* hytc,
+                            const float* state, void* workspace, size_t workspace_bytes, double* out2, void* stream) {
+  return run_stats<float>(nx, nz, dx, dz, hyc, hytc, state, workspace, workspace_bytes, out2, (cudaStream_t)stream);
+}
+
+extern "C" int mw_solution_variables_f64(int nx, int nz, const double* hyc, const double* hytc, const double* state,
+                                         double* out, void* stream) {
+  int st = check_grid(nx, nz);
+  if (st) return st;
+  MW_REQUIRE(hyc && hytc && state && out, MW_ERR_INVALID_ARG, "NULL pointer argument");
+  MW_REQUIRE(aligned(hyc) && aligned(hytc) && aligned(state) && aligned(out), MW_ERR_ALIGN, "misaligned pointer");
+  k_solution_vars<<<grid_for((long long)nx * nz, 256), 256, 0, (cudaStream_t)stream>>>(nx, nz, hyc, hytc, state, out);
+  return check_launch("solution variables launch");
+}
+
+extern "C" int mw_set_bc_f64(int nx, int nz, const double* hyc, double* state, int direction, void* stream) {
+  int st = check_grid(nx, nz);
+  if (st) return st;
+  MW_REQUIRE(hyc && state, MW_ERR_INVALID_ARG, "NULL pointer argument");
+  MW_REQUIRE(aligned(hyc) && aligned(state), MW_ERR_ALIGN, "misaligned pointer");
+  MW_REQUIRE(direction == MW_DIR_X || direction == MW_DIR_Z, MW_ERR_INVALID_ARG, "direction must be 0 or 1");
+  const long long n = direction == MW_DIR_X ? 4LL * nz : nx + 2 * kHs;
+  k_set_bc<<<grid_for(n, 128), 128, 0, (cudaStream_t)stream>>>(nx, nz, hyc, state, direction);
+  return check_launch("set_bc launch");
+}
+
+extern "C" int mw_interpolate_f64(int nx, int nz, const double* state, double* vals, double* d3, int direction,
+                                  void* stream) {
+  int st = check_grid(nx, nz);
+  if (st) return st;
+  MW_REQUIRE(state && vals && d3, MW_ERR_INVALID_ARG, "NULL pointer argument");
+  MW_REQUIRE(aligned(state) && aligned(vals) && aligned(d3), MW_ERR_ALIGN, "misaligned pointer");
+  MW_REQUIRE(direction == MW_DIR_X || direction == MW_DIR_Z, MW_ERR_INVALID_ARG, "direction must be 0 or 1");
+  const long long n = direction == MW_DIR_X ? 4LL * nz * (nx + 1) : 4LL * (nz + 1) * nx;
+  k_interpolate<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(nx, nz, state, vals, d3, direction);
+  return check_launch("interpolate launch");
+}
+
+extern "C" int mw_flux_f64(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
+                           const double* hyi, const double* hyti, const double* hypi, const double* vals, double* d3,
+                           double* flux, int direction, void* stream) {
+  int st = check_grid(nx, nz);
+  if (st) return st;
+  MW_REQUIRE(finite_pos(dx) && finite_pos(dz) && finite_pos(dt_full), MW_ERR_INVALID_ARG,
+             "dx, dz, dt_full must be finite and positive");
+  MW_REQUIRE(hyc && hytc && hyi && hyti && hypi && vals && d3 && flux, MW_ERR_INVALID_ARG, "NULL pointer argument");
+  MW_REQUIRE(direction == MW_DIR_X || direction == MW_DIR_Z, MW_ERR_INVALID_ARG, "direction must be 0 or 1");
+  FluxArgs a;
+  a.nx = nx;
+  a.nz = nz;
+  a.hv = -kHvBeta * (direction == MW_DIR_X ? dx : dz) / (16 * dt_full);
+  a.hyc = hyc;
+  a.hytc = hytc;
+  a.hyi = hyi;
+  a.hyti = hyti;
+  a.hypi = hypi;
+  a.vals = vals;
+  a.d3 = d3;
+  a.flux = flux;
+  a.dir = direction;
+  const long long n = direction == MW_DIR_X ? (long long)nz * (nx + 1) : (long long)(nz + 1) * nx;
+  k_flux<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(a);
+  return check_launch("flux launch");
+}
+
+extern "C" int mw_tend_f64(int nx, int nz, double dx, double dz, const double* flux, const double* state_forcing,
+                           const double* src_w, double* tend, int direction, void* stream) {
+  int st = check_grid(nx, nz);
+  if (st) return st;
+  MW_REQUIRE(finite_pos(dx) && finite_pos(dz), MW_ERR_INVALID_ARG, "dx, dz must be finite and positive");
+  MW_REQUIRE(flux && state_forcing && tend, MW_ERR_INVALID_ARG, "NULL pointer argument");
+  MW_REQUIRE(direction == MW_DIR_X || direction == MW_DIR_Z, MW_ERR_INVALID_ARG, "direction must be 0 or 1");
+  k_tend<<<grid_for((long long)nx * nz, 256), 256, 0, (cudaStream_t)stream>>>(
+      nx, nz, direction == MW_DIR_X ? dx : dz, flux, state_forcing, src_w, tend, direction);
+  return check_launch("tend launch");
+}
+
+extern "C" int mw_update_f64(int nx, int nz, const double* init, const double* tend, double* out, double dt_stage,
+                             void* stream) {
+  int st = check_grid(nx, nz);
+  if (st) return st;
+  MW_REQUIRE(init && tend && out, MW_ERR_INVALID_ARG, "NULL pointer argument");
+  MW_REQUIRE(std::isfinite(dt_stage), MW_ERR_INVALID_ARG, "dt_stage must be finite");
+  k_update<<<grid_for(4LL * nx * nz, 256), 256, 0, (cudaStream_t)stream>>>(nx, nz, init, tend, out, dt_stage);
+  return check_launch("update launch");
+}
+
+extern "C" int mw_add_source_f64(int nx, int nz, const double* src_w, double* tend, void* stream) {
+  int st = check_grid(nx, nz);
+  if (st) return st;
+  MW_REQUIRE(src_w && tend, MW_ERR_INVALID_ARG, "NULL pointer argument");
+  k_add_source<<<grid_for((long long)nx * nz, 256), 256, 0, (cudaStream_t)stream>>>(nx, nz, src_w, tend);
+  return check_launch("add_source launch");
+}

@@ -1,0 +1,489 @@
+// mw_dirstage.cu -- fused direction-stage kernels and the RK3 step driver.
+//
+// One kernel launch performs one discrete_step of the reference
+// (pyminiweather/solve/step.py:21-82): halo rule, 4-point interpolation,
+// flux with hyperviscosity, flux divergence, gravity term, forcing, stage
+// update.  Halo cells are never read: the periodic (x) and wall (z) rules of
+// ics/bcs.py are applied to the indices / values as they are loaded.
+//
+// x pass: one CTA row-segment per (row, 255 cells).  Thread t evaluates the
+// flux at interface x0+t into shared memory; after one barrier thread t
+// updates cell x0+t from interfaces t and t+1.  Interface loads are
+// coalesced rows; the four taps hit L1.
+// z pass: one thread per column marching down a tile of kZTile rows with a
+// rolling 4-row register window, so every forcing value is loaded once per
+// tile and every interface flux is evaluated once; rows are coalesced across
+// the warp.
+#include "mw_common.cuh"
+#include "mw_split.cuh"
+
+namespace mw {
+
+constexpr int kXThreads = 256;          // interfaces per x CTA
+constexpr int kXCells = kXThreads - 1;  // cells updated per x CTA
+constexpr int kZThreads = 128;          // columns per z CTA
+constexpr int kZTile = 32;              // rows marched per z thread
+
+enum Mode { MODE_NATIVE64 = 0, MODE_SPLIT64 = 1, MODE_F32 = 2 };
+
+template <typename T>
+struct StageArgs {
+  int nx, nz, pitch;
+  long long plane;
+  double dx, dz;
+  double hv;        // -hv_beta * d / (16 dt_full), d = dx or dz (interpolate.py:101,149)
+  double dt_stage;
+  const double* hyc;
+  const double* hytc;
+  const double* hyi;
+  const double* hyti;
+  const double* hypi;
+  const double* srcw;
+  const T* init;
+  T* forcing;
+  T* out;
+  unsigned flags;
+};
+
+// ---- interpolation in the accumulation order of scipy.signal.convolve ----
+template <typename T>
+__device__ __forceinline__ T interp4(T s0, T s1, T s2, T s3) {
+  const T k0 = T(-1.0 / 12), k1 = T(7.0 / 12);
+  return ((s0 * k0 + s1 * k1) + s2 * k1) + s3 * k0;
+}
+template <typename T>
+__device__ __forceinline__ T diff3(T s0, T s1, T s2, T s3) {
+  return ((s0 * T(-1) + s1 * T(3)) + s2 * T(-3)) + s3;
+}
+
+// ---- fluxes: the reference's formulas on the FP64 pipe ----
+__device__ __forceinline__ void flux_x_native(const double s[4][4], double hyc, double hytc, double hv, double F[4]) {
+  double v[4], d3[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    v[q] = interp4(s[q][0], s[q][1], s[q][2], s[q][3]);
+    d3[q] = diff3(s[q][0], s[q][1], s[q][2], s[q][3]);
+  }
+  double rho = v[DENS] + hyc;
+  double u = v[UMOM] / rho;
+  double w = v[WMOM] / rho;
+  double t = (v[RHOT] + hytc) / rho;
+  double p = kC0 * pow(rho * t, kGamma);
+  F[0] = rho * u - hv * d3[DENS];
+  F[1] = rho * (u * u) + p - hv * d3[UMOM];
+  F[2] = rho * u * w - hv * d3[WMOM];
+  F[3] = rho * u * t - hv * d3[RHOT];
+}
+
+__device__ __forceinline__ void flux_z_native(const double s[4][4], double hyi, double hyti, double hypi, double hv,
+                                              bool wall, double F[4]) {
+  double v[4], d3[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    v[q] = interp4(s[q][0], s[q][1], s[q][2], s[q][3]);
+    d3[q] = diff3(s[q][0], s[q][1], s[q][2], s[q][3]);
+  }
+  double rho = v[DENS] + hyi;
+  double u = v[UMOM] / rho;
+  double w = v[WMOM] / rho;
+  double t = (v[RHOT] + hyti) / rho;
+  double p = kC0 * pow(rho * t, kGamma) - hypi;
+  if (wall) {
+    w = 0.0;
+    d3[DENS] = 0.0;
+  }
+  F[0] = rho * w - hv * d3[DENS];
+  F[1] = rho * w * u - hv * d3[UMOM];
+  F[2] = rho * (w * w) + p - hv * d3[WMOM];
+  F[3] = rho * w * t - hv * d3[RHOT];
+}
+
+// ---- FP32 fluxes (precision form) ----
+// Pressure enters as the perturbation P_row * ((1 + delta)^gamma - 1),
+// delta = (rho theta)' / (rho theta)_background.  In z this is exactly the
+// reference's p - hy_pressure_int; in x the row constant C0 (rho theta)_bg^gamma
+// cancels in the flux difference, so the tendency is unchanged while FP32 no
+// longer differences two values near 1e5.  rho*u is formed as (rho u)' itself.
+__device__ __forceinline__ float pgm1f(float d) {
+  return expm1f(float(kGamma) * log1pf(d));
+}
+
+struct RowF {
+  float hy_r, hy_rt, inv_hy_rt, P;
+};
+
+__device__ __forceinline__ void flux_x_f32(const float s[4][4], const RowF& r, float hv, float F[4]) {
+  float v[4], d3[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    v[q] = interp4(s[q][0], s[q][1], s[q][2], s[q][3]);
+    d3[q] = diff3(s[q][0], s[q][1], s[q][2], s[q][3]);
+  }
+  float rho = v[DENS] + r.hy_r;
+  float ri = 1.0f / rho;
+  float u = v[UMOM] * ri;
+  float w = v[WMOM] * ri;
+  float th = (v[RHOT] + r.hy_rt) * ri;
+  float pp = r.P * pgm1f(v[RHOT] * r.inv_hy_rt);
+  F[0] = v[UMOM] - hv * d3[DENS];
+  F[1] = v[UMOM] * u + pp - hv * d3[UMOM];
+  F[2] = v[UMOM] * w - hv * d3[WMOM];
+  F[3] = v[UMOM] * th - hv * d3[RHOT];
+}
+
+__device__ __forceinline__ void flux_z_f32(const float s[4][4], const RowF& r, float hv, bool wall, float F[4]) {
+  float v[4], d3[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    v[q] = interp4(s[q][0], s[q][1], s[q][2], s[q][3]);
+    d3[q] = diff3(s[q][0], s[q][1], s[q][2], s[q][3]);
+  }
+  float rho = v[DENS] + r.hy_r;
+  float ri = 1.0f / rho;
+  float u = v[UMOM] * ri;
+  float w = v[WMOM] * ri;
+  float th = (v[RHOT] + r.hy_rt) * ri;
+  float pp = r.P * pgm1f(v[RHOT] * r.inv_hy_rt);
+  float rw = v[WMOM];
+  if (wall) {
+    w = 0.0f;
+    rw = 0.0f;
+    d3[DENS] = 0.0f;
+  }
+  F[0] = rw - hv * d3[DENS];
+  F[1] = rw * u - hv * d3[UMOM];
+  F[2] = rw * w + pp - hv * d3[WMOM];
+  F[3] = rw * th - hv * d3[RHOT];
+}
+
+// ---- halo rules -----------------------------------------------------------
+// Periodic x (ics/bcs.py:35-39): interior column j in [-2, nx+1] maps to j mod nx.
+__device__ __forceinline__ int wrap_x(int j, int nx) { return j < 0 ? j + nx : (j >= nx ? j - nx : j); }
+
+// Wall z (ics/bcs.py:92-148): value of variable q at interior row k in
+// [-2, nz+1] of the halo-indexed column col.
+template <typename T>
+__device__ __forceinline__ T zval(const StageArgs<T>& a, int q, int k, int col) {
+  if (k >= 0 && k < a.nz) return a.forcing[q * a.plane + (long long)(k + kHs) * a.pitch + col];
+  if (q == WMOM) return T(0);
+  const int src = k < 0 ? kHs : a.nz + kHs - 1;  // halo-indexed source row
+  T s = a.forcing[q * a.plane + (long long)src * a.pitch + col];
+  if (q == UMOM) return T((double)s / a.hyc[src] * a.hyc[k + kHs]);
+  return s;
+}
+
+template <typename T>
+__device__ __forceinline__ void write_z_halo_column(const StageArgs<T>& a, int col) {
+  const int rows[4] = {-2, -1, a.nz, a.nz + 1};
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    T vals[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) vals[r] = zval(a, q, rows[r], col);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) a.forcing[q * a.plane + (long long)(rows[r] + kHs) * a.pitch + col] = vals[r];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// x direction-stage
+template <typename T, int MODE>
+__global__ void __launch_bounds__(kXThreads) k_stage_x(StageArgs<T> a) {
+  __shared__ T sF[4][kXThreads];
+  const int t = threadIdx.x;
+  const int x0 = blockIdx.x * kXCells;
+  const int i = x0 + t;  // interface index 0..nx (between cells i-1 and i)
+  for (int k = blockIdx.y; k < a.nz; k += gridDim.y) {
+    const long long row = (long long)(k + kHs) * a.pitch;
+    if ((a.flags & MW_FLAG_WRITE_HALO) && blockIdx.x == 0 && t < 4) {
+      const int dst[4] = {0, 1, a.nx + kHs, a.nx + kHs + 1};
+      const int src[4] = {a.nx, a.nx + 1, kHs, kHs + 1};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) a.forcing[q * a.plane + row + dst[t]] = a.forcing[q * a.plane + row + src[t]];
+    }
+    if (i <= a.nx) {
+      T s[4][4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const long long col = wrap_x(i - 2 + j, a.nx) + kHs;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) s[q][j] = __ldg(a.forcing + q * a.plane + row + col);
+      }
+      T F[4];
+      if constexpr (MODE == MODE_NATIVE64) {
+        flux_x_native(s, a.hyc[k + kHs], a.hytc[k + kHs], a.hv, F);
+      } else {
+        const double hr = a.hyc[k + kHs], hrt = a.hytc[k + kHs];
+        RowF r;
+        r.hy_r = split::d2f(hr);
+        r.hy_rt = split::d2f(hrt);
+        r.inv_hy_rt = 1.0f / r.hy_rt;
+        r.P = float(kC0) * powf(r.hy_rt, float(kGamma));
+        flux_x_f32(s, r, float(a.hv), F);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) sF[q][t] = F[q];
+    }
+    __syncthreads();
+    if (t < kXCells && i < a.nx) {
+      const long long o = row + i + kHs;
+      if constexpr (MODE == MODE_NATIVE64) {
+        double tend[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) tend[q] = -(sF[q][t + 1] - sF[q][t]) / a.dx;
+        if (a.srcw) tend[WMOM] = tend[WMOM] + a.srcw[(long long)k * a.nx + i];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = a.init[q * a.plane + o] + a.dt_stage * tend[q];
+      } else {
+        const float c = float(a.dt_stage / a.dx), dt = float(a.dt_stage);
+        float inc[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) inc[q] = (sF[q][t] - sF[q][t + 1]) * c;
+        if (a.srcw) inc[WMOM] += dt * split::d2f(a.srcw[(long long)k * a.nx + i]);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = a.init[q * a.plane + o] + inc[q];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// z direction-stage
+template <typename T, int MODE>
+__global__ void __launch_bounds__(kZThreads) k_stage_z(StageArgs<T> a) {
+  const int c = blockIdx.x * kZThreads + threadIdx.x;  // interior column
+  if ((a.flags & MW_FLAG_WRITE_HALO) && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x < 4) {
+    const int hcol[4] = {0, 1, a.nx + kHs, a.nx + kHs + 1};
+    write_z_halo_column(a, hcol[threadIdx.x]);
+  }
+  if (c >= a.nx) return;
+  const int col = c + kHs;
+  if ((a.flags & MW_FLAG_WRITE_HALO) && blockIdx.y == 0) write_z_halo_column(a, col);
+  const int z0 = blockIdx.y * kZTile;
+  const int z1 = min(z0 + kZTile, a.nz);
+  T w[4][4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) w[q][j] = zval(a, q, z0 - 2 + j, col);
+
+  auto flux_at = [&](int k, T F[4]) {
+    const bool wall = (k == 0) || (k == a.nz);
+    if constexpr (MODE == MODE_NATIVE64) {
+      flux_z_native(w, a.hyi[k], a.hyti[k], a.hypi[k], a.hv, wall, F);
+    } else {
+      RowF r;
+      r.hy_r = split::d2f(a.hyi[k]);
+      r.hy_rt = split::d2f(a.hyti[k]);
+      r.inv_hy_rt = 1.0f / r.hy_rt;
+      r.P = split::d2f(a.hypi[k]);
+      flux_z_f32(w, r, float(a.hv), wall, F);
+    }
+  };
+  T Fp[4];
+  flux_at(z0, Fp);
+  for (int k = z0; k < z1; ++k) {
+    const T rho_k = w[DENS][2];  // forcing rho' at cell k (interpolate.py:248-250)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      w[q][0] = w[q][1];
+      w[q][1] = w[q][2];
+      w[q][2] = w[q][3];
+      w[q][3] = zval(a, q, k + 2, col);
+    }
+    T Fn[4];
+    flux_at(k + 1, Fn);
+    const long long o = (long long)(k + kHs) * a.pitch + col;
+    if constexpr (MODE == MODE_NATIVE64) {
+      double tend[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) tend[q] = -(Fn[q] - Fp[q]) / a.dz;
+      tend[WMOM] = tend[WMOM] - rho_k * kGrav;
+      if (a.srcw) tend[WMOM] = tend[WMOM] + a.srcw[(long long)k * a.nx + c];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = a.init[q * a.plane + o] + a.dt_stage * tend[q];
+    } else {
+      const float cz = float(a.dt_stage / a.dz), dt = float(a.dt_stage);
+      float inc[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) inc[q] = (Fp[q] - Fn[q]) * cz;
+      inc[WMOM] -= dt * (rho_k * float(kGrav));
+      if (a.srcw) inc[WMOM] += dt * split::d2f(a.srcw[(long long)k * a.nx + c]);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = a.init[q * a.plane + o] + inc[q];
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) Fp[q] = Fn[q];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+template <typename T>
+static int validate_stage(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
+                          const double* hyi, const double* hyti, const double* hypi, const T* init, const T* forcing,
+                          const T* out, int direction) {
+  int st = check_grid(nx, nz);
+  if (st) return st;
+  MW_REQUIRE(finite_pos(dx) && finite_pos(dz) && finite_pos(dt_full), MW_ERR_INVALID_ARG,
+             "dx, dz and dt_full must be finite and positive (got %g, %g, %g)", dx, dz, dt_full);
+  MW_REQUIRE(direction == MW_DIR_X || direction == MW_DIR_Z, MW_ERR_INVALID_ARG, "direction must be 0 (x) or 1 (z)");
+  MW_REQUIRE(hyc && hytc && hyi && hyti && hypi, MW_ERR_INVALID_ARG, "background arrays must not be NULL");
+  MW_REQUIRE(init && forcing && out, MW_ERR_INVALID_ARG, "state arrays must not be NULL");
+  MW_REQUIRE(aligned(hyc) && aligned(hytc) && aligned(hyi) && aligned(hyti) && aligned(hypi), MW_ERR_ALIGN,
+             "background arrays must be 8-byte aligned");
+  MW_REQUIRE(aligned(init) && aligned(forcing) && aligned(out), MW_ERR_ALIGN, "state arrays misaligned");
+  const size_t bytes = sizeof(T) * 4 * (size_t)make_geom(nx, nz).plane;
+  MW_REQUIRE(!ranges_overlap(out, bytes, forcing, bytes), MW_ERR_ALIAS,
+             "out must not overlap forcing (the fused kernel reads forcing neighbours while writing out)");
+  MW_REQUIRE(out == init || !ranges_overlap(out, bytes, init, bytes), MW_ERR_ALIAS,
+             "out must either equal init or not overlap it");
+  return MW_OK;
+}
+
+template <typename T, int MODE>
+static int launch_stage(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
+                        const double* hyi, const double* hyti, const double* hypi, const double* srcw, const T* init,
+                        T* forcing, T* out, double dt_stage, int direction, unsigned flags, cudaStream_t stream) {
+  const Geom g = make_geom(nx, nz);
+  StageArgs<T> a;
+  a.nx = nx;
+  a.nz = nz;
+  a.pitch = g.pitch;
+  a.plane = g.plane;
+  a.dx = dx;
+  a.dz = dz;
+  a.hv = -kHvBeta * (direction == MW_DIR_X ? dx : dz) / (16 * dt_full);
+  a.dt_stage = dt_stage;
+  a.hyc = hyc;
+  a.hytc = hytc;
+  a.hyi = hyi;
+  a.hyti = hyti;
+  a.hypi = hypi;
+  a.srcw = srcw;
+  a.init = init;
+  a.forcing = forcing;
+  a.out = out;
+  a.flags = flags;
+  if (direction == MW_DIR_X) {
+    dim3 grid((nx + kXCells - 1) / kXCells, (unsigned)min(nz, 65535));
+    k_stage_x<T, MODE><<<grid, kXThreads, 0, stream>>>(a);
+  } else {
+    dim3 grid((nx + kZThreads - 1) / kZThreads, (nz + kZTile - 1) / kZTile);
+    k_stage_z<T, MODE><<<grid, kZThreads, 0, stream>>>(a);
+  }
+  return check_launch(direction == MW_DIR_X ? "x direction-stage launch" : "z direction-stage launch");
+}
+
+// Split-arithmetic launches live in mw_split_stage.cu.
+int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
+                       const double* hyi, const double* hyti, const double* hypi, const double* srcw,
+                       const double* init, double* forcing, double* out, double dt_stage, int direction,
+                       unsigned flags, cudaStream_t stream);
+
+static int stage_f64(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
+                     const double* hyi, const double* hyti, const double* hypi, const double* srcw,
+                     const double* init, double* forcing, double* out, double dt_stage, int direction, int mode,
+                     unsigned flags, cudaStream_t stream) {
+  if (mode == MW_F64_SPLIT)
+    return launch_stage_split(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, srcw, init, forcing, out,
+                              dt_stage, direction, flags, stream);
+  return launch_stage<double, MODE_NATIVE64>(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, srcw, init, forcing,
+                                             out, dt_stage, direction, flags, stream);
+}
+
+template <typename T, typename StageFn>
+static int run_steps(double dt, T* S, T* Tmp, T* A, int nsteps, int* reverse, StageFn stage) {
+  for (int n = 0; n < nsteps; ++n) {
+    const int dirs[2] = {*reverse ? MW_DIR_X : MW_DIR_Z, *reverse ? MW_DIR_Z : MW_DIR_X};
+    for (int d = 0; d < 2; ++d) {
+      int st;
+      if ((st = stage(S, S, A, dt / 3, dirs[d]))) return st;
+      if ((st = stage(S, A, Tmp, dt / 2, dirs[d]))) return st;
+      if ((st = stage(S, Tmp, S, dt / 1, dirs[d]))) return st;
+    }
+    *reverse = *reverse ? 0 : 1;
+  }
+  return MW_OK;
+}
+
+template <typename T>
+static int validate_step(int nx, int nz, double dx, double dz, double dt, const double* hyc, const double* hytc,
+                         const double* hyi, const double* hyti, const double* hypi, const T* S, const T* Tmp,
+                         const T* A, int nsteps, const int* reverse) {
+  int st = validate_stage<T>(nx, nz, dx, dz, dt, hyc, hytc, hyi, hyti, hypi, S, A, Tmp, MW_DIR_X);
+  if (st) return st;
+  MW_REQUIRE(reverse != nullptr, MW_ERR_INVALID_ARG, "reverse flag pointer must not be NULL");
+  MW_REQUIRE(nsteps >= 0, MW_ERR_INVALID_ARG, "nsteps must be >= 0");
+  const size_t bytes = sizeof(T) * 4 * (size_t)make_geom(nx, nz).plane;
+  MW_REQUIRE(!ranges_overlap(S, bytes, Tmp, bytes) && !ranges_overlap(S, bytes, A, bytes) &&
+                 !ranges_overlap(Tmp, bytes, A, bytes),
+             MW_ERR_ALIAS, "state, state_tmp and scratch must be three separate arrays");
+  return MW_OK;
+}
+
+}  // namespace mw
+
+using namespace mw;
+
+extern "C" int mw_dirstage_f64(int nx, int nz, double dx, double dz, double dt_full, const double* hyc,
+                               const double* hytc, const double* hyi, const double* hyti, const double* hypi,
+                               const double* src_w, const double* init, double* forcing, double* out,
+                               double dt_stage, int direction, int f64_mode, unsigned flags, void* stream) {
+  int st = validate_stage<double>(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, init, forcing, out, direction);
+  if (st) return st;
+  MW_REQUIRE(f64_mode == MW_F64_NATIVE || f64_mode == MW_F64_SPLIT, MW_ERR_INVALID_ARG, "unknown f64_mode %d",
+             f64_mode);
+  MW_REQUIRE(std::isfinite(dt_stage), MW_ERR_INVALID_ARG, "dt_stage must be finite");
+  return stage_f64(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, src_w, init, forcing, out, dt_stage,
+                   direction, f64_mode, flags, (cudaStream_t)stream);
+}
+
+extern "C" int mw_dirstage_f32(int nx, int nz, double dx, double dz, double dt_full, const double* hyc,
+                               const double* hytc, const double* hyi, const double* hyti, const double* hypi,
+                               const double* src_w, const float* init, float* forcing, float* out, double dt_stage,
+                               int direction, unsigned flags, void* stream) {
+  int st = validate_stage<float>(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, init, forcing, out, direction);
+  if (st) return st;
+  MW_REQUIRE(std::isfinite(dt_stage), MW_ERR_INVALID_ARG, "dt_stage must be finite");
+  return launch_stage<float, MODE_F32>(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, src_w, init, forcing, out,
+                                       dt_stage, direction, flags, (cudaStream_t)stream);
+}
+
+extern "C" int mw_step_f64(int nx, int nz, double dx, double dz, double dt_full, double dt, const double* hyc,
+                           const double* hytc,
+                           const double* hyi, const double* hyti, const double* hypi, const double* src_w,
+                           double* state, double* state_tmp, double* scratch, int nsteps, int* reverse, int f64_mode,
+                           unsigned flags, void* stream) {
+  int st = validate_step<double>(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, state, state_tmp, scratch,
+                                 nsteps, reverse);
+  if (st) return st;
+  MW_REQUIRE(finite_pos(dt), MW_ERR_INVALID_ARG, "dt must be finite and positive");
+  if (st) return st;
+  MW_REQUIRE(f64_mode == MW_F64_NATIVE || f64_mode == MW_F64_SPLIT, MW_ERR_INVALID_ARG, "unknown f64_mode %d",
+             f64_mode);
+  cudaStream_t s = (cudaStream_t)stream;
+  return run_steps<double>(dt, state, state_tmp, scratch, nsteps, reverse,
+                           [&](const double* init, double* forcing, double* out, double dts, int dir) {
+                             return stage_f64(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, src_w, init, forcing,
+                                              out, dts, dir, f64_mode, flags, s);
+                           });
+}
+
+extern "C" int mw_step_f32(int nx, int nz, double dx, double dz, double dt_full, double dt, const double* hyc,
+                           const double* hytc,
+                           const double* hyi, const double* hyti, const double* hypi, const double* src_w, float* state,
+                           float* state_tmp, float* scratch, int nsteps, int* reverse, unsigned flags, void* stream) {
+  int st = validate_step<float>(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, state, state_tmp, scratch,
+                                nsteps, reverse);
+  if (st) return st;
+  MW_REQUIRE(finite_pos(dt), MW_ERR_INVALID_ARG, "dt must be finite and positive");
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  return run_steps<float>(dt, state, state_tmp, scratch, nsteps, reverse,
+                          [&](const float* init, float* forcing, float* out, double dts, int dir) {
+                            return launch_stage<float, MODE_F32>(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi,
+                                                                 src_w, init, forcing, out, dts, dir, flags, s);
+                          });
+}

@@ -1,0 +1,316 @@
+// mw_split_stage.cu -- FP64-storage direction-stage kernels with the interior
+// arithmetic in double-FP32 (see mw_split.cuh): the GB300 form of
+// discrete_step (pyminiweather/solve/step.py:21-82).
+//
+// Loads and stores are FP64; each loaded value is split once into (h, l);
+// interpolation, fluxes, pressure and flux divergence run on the FP32 pipe;
+// the stage update out = init + increment is one FP64 add per value.
+//
+// Quantities are carried scaled by 12 so that the 4-point interpolation
+// (-s0 + 7 s1 + 7 s2 - s3)/12 needs no division: A = 12 vals, and the
+// background terms, pressure and hyperviscosity coefficient are scaled to
+// match; the flux divergence is multiplied by dt / (12 d).
+//
+// Pressure: P_row ((1 + delta)^gamma - 1), delta = (rho theta)' / (rho theta)_bg,
+// with P_row = C0 (rho theta)_bg^gamma.  In z this is the reference's
+// p - hy_pressure_int (interpolate.py:163-165); in x the row constant cancels
+// in the flux difference.  (1 + delta)^gamma - 1 is the binomial series
+// sum_{n=1..16} C(gamma, n) delta^n, whose terms beyond n = 16 are below
+// 2^-56 relative for |delta| <= 1/8; terms 7..16 are summed in FP32, 1..6 in
+// double-FP32.  |delta| > 1/8 falls back to expm1(gamma log1p(delta)) in FP64.
+#include "mw_common.cuh"
+#include "mw_split.cuh"
+
+namespace mw {
+using namespace split;
+
+namespace {
+
+constexpr double binom_gamma(int n) {
+  double c = kGamma;
+  for (int k = 1; k < n; ++k) c = c * (kGamma - k) / (k + 1);
+  return c;
+}
+constexpr float hi_of(double v) { return (float)v; }
+constexpr float lo_of(double v) { return (float)(v - (double)(float)v); }
+
+__constant__ float c_pow_h[7] = {0.f,
+                                 hi_of(binom_gamma(1)), hi_of(binom_gamma(2)), hi_of(binom_gamma(3)),
+                                 hi_of(binom_gamma(4)), hi_of(binom_gamma(5)), hi_of(binom_gamma(6))};
+__constant__ float c_pow_l[7] = {0.f,
+                                 lo_of(binom_gamma(1)), lo_of(binom_gamma(2)), lo_of(binom_gamma(3)),
+                                 lo_of(binom_gamma(4)), lo_of(binom_gamma(5)), lo_of(binom_gamma(6))};
+__constant__ float c_pow_tail[17] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f,
+                                     (float)binom_gamma(7), (float)binom_gamma(8), (float)binom_gamma(9),
+                                     (float)binom_gamma(10), (float)binom_gamma(11), (float)binom_gamma(12),
+                                     (float)binom_gamma(13), (float)binom_gamma(14), (float)binom_gamma(15),
+                                     (float)binom_gamma(16)};
+
+constexpr int kXThreads = 256;
+constexpr int kXCells = kXThreads - 1;
+constexpr int kXTile = kXThreads + 3;  // cells x0-2 .. x0+256
+constexpr int kZThreads = 128;
+constexpr int kZTile = 32;
+
+struct RowS {
+  dw R;    // 12 * background rho
+  dw RT;   // 12 * background rho*theta
+  dw IRT;  // 1 / (12 * background rho*theta)
+  dw P12;  // 12 * background pressure
+};
+
+struct SplitArgs {
+  int nx, nz, pitch;
+  long long plane;
+  const double* hyc;
+  const double* hytc;
+  const double* hyi;
+  const double* hyti;
+  const double* hypi;
+  const double* srcw;
+  const double* init;
+  double* forcing;
+  double* out;
+  unsigned flags;
+  dwc hv12;  // 12 * hv
+  dwc c12;   // dt_stage / (12 d)
+  dwc dt;    // dt_stage
+  dwc dtg;   // dt_stage * grav
+};
+
+// (1 + d)^gamma - 1
+__device__ __forceinline__ dw pgm1(dw d) {
+  if (fabsf(d.h) <= 0.125f) {
+    const float df = d.h;
+    float t = c_pow_tail[16];
+#pragma unroll
+    for (int n = 15; n >= 7; --n) t = fmaf(t, df, c_pow_tail[n]);
+    dw y = add(mulf(d, t), dw{c_pow_h[6], c_pow_l[6]});
+#pragma unroll
+    for (int n = 5; n >= 1; --n) y = add(mul(y, d), dw{c_pow_h[n], c_pow_l[n]});
+    return mul(y, d);
+  }
+  const double dd = to_f64(d);
+  return from_f64(expm1(kGamma * log1p(dd)));
+}
+
+// 12 * (4-point interpolation) and the third difference, in the arrangement
+// 7 (s1 + s2) - (s0 + s3) and (s3 - s0) + 3 (s1 - s2).
+__device__ __forceinline__ void interp_split(dw s0, dw s1, dw s2, dw s3, dw& A, dw& D) {
+  A = sub(mulf(add(s1, s2), 7.0f), add(s0, s3));
+  D = add(sub(s3, s0), mulf(sub(s1, s2), 3.0f));
+}
+
+__device__ __forceinline__ void flux_x_split(const dw s[4][4], const RowS& r, dw hv12, dw F[4]) {
+  dw A[4], D[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) interp_split(s[q][0], s[q][1], s[q][2], s[q][3], A[q], D[q]);
+  const dw rho = add(A[DENS], r.R);
+  const dw ri = rcp(rho);
+  const dw u = mul(A[UMOM], ri);
+  const dw w = mul(A[WMOM], ri);
+  const dw th = mul(add(A[RHOT], r.RT), ri);
+  const dw pp = mul(r.P12, pgm1(mul(A[RHOT], r.IRT)));
+  F[0] = sub(A[UMOM], mul(hv12, D[DENS]));
+  F[1] = sub(add(mul(A[UMOM], u), pp), mul(hv12, D[UMOM]));
+  F[2] = sub(mul(A[UMOM], w), mul(hv12, D[WMOM]));
+  F[3] = sub(mul(A[UMOM], th), mul(hv12, D[RHOT]));
+}
+
+__device__ __forceinline__ void flux_z_split(const dw s[4][4], const RowS& r, dw hv12, bool wall, dw F[4]) {
+  dw A[4], D[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) interp_split(s[q][0], s[q][1], s[q][2], s[q][3], A[q], D[q]);
+  const dw rho = add(A[DENS], r.R);
+  const dw ri = rcp(rho);
+  const dw u = mul(A[UMOM], ri);
+  const dw th = mul(add(A[RHOT], r.RT), ri);
+  const dw pp = mul(r.P12, pgm1(mul(A[RHOT], r.IRT)));
+  dw rw = A[WMOM];
+  dw dd = D[DENS];
+  if (wall) {  // interpolate.py:167-173: w and d3[DENS] vanish at the walls
+    rw = dw{0.f, 0.f};
+    dd = dw{0.f, 0.f};
+  }
+  const dw w = mul(rw, ri);
+  F[0] = sub(rw, mul(hv12, dd));
+  F[1] = sub(mul(rw, u), mul(hv12, D[UMOM]));
+  F[2] = sub(add(mul(rw, w), pp), mul(hv12, D[WMOM]));
+  F[3] = sub(mul(rw, th), mul(hv12, D[RHOT]));
+}
+
+__device__ __forceinline__ RowS row_consts(double hy_r, double hy_rt, double P) {
+  RowS r;
+  r.R = from_f64(12.0 * hy_r);
+  r.RT = from_f64(12.0 * hy_rt);
+  r.IRT = from_f64(1.0 / (12.0 * hy_rt));
+  r.P12 = from_f64(12.0 * P);
+  return r;
+}
+
+__device__ __forceinline__ int wrap_x(int j, int nx) { return j < 0 ? j + nx : (j >= nx ? j - nx : j); }
+
+__device__ __forceinline__ double zval64(const SplitArgs& a, int q, int k, int col) {
+  if (k >= 0 && k < a.nz) return a.forcing[q * a.plane + (long long)(k + kHs) * a.pitch + col];
+  if (q == WMOM) return 0.0;
+  const int src = k < 0 ? kHs : a.nz + kHs - 1;
+  const double s = a.forcing[q * a.plane + (long long)src * a.pitch + col];
+  if (q == UMOM) return s / a.hyc[src] * a.hyc[k + kHs];
+  return s;
+}
+
+__device__ __forceinline__ void write_z_halo_column(const SplitArgs& a, int col) {
+  const int rows[4] = {-2, -1, a.nz, a.nz + 1};
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    double v[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) v[r] = zval64(a, q, rows[r], col);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) a.forcing[q * a.plane + (long long)(rows[r] + kHs) * a.pitch + col] = v[r];
+  }
+}
+
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kXThreads) k_stage_x_split(SplitArgs a) {
+  __shared__ dw sS[4][kXTile];
+  __shared__ dw sF[4][kXThreads];
+  __shared__ RowS sRow;
+  const int t = threadIdx.x;
+  const int x0 = blockIdx.x * kXCells;
+  const int i = x0 + t;
+  const dw hv12 = ld(a.hv12), c12 = ld(a.c12), dts = ld(a.dt);
+  for (int k = blockIdx.y; k < a.nz; k += gridDim.y) {
+    const long long row = (long long)(k + kHs) * a.pitch;
+    if ((a.flags & MW_FLAG_WRITE_HALO) && blockIdx.x == 0 && t < 4) {
+      const int dst[4] = {0, 1, a.nx + kHs, a.nx + kHs + 1};
+      const int src[4] = {a.nx, a.nx + 1, kHs, kHs + 1};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) a.forcing[q * a.plane + row + dst[t]] = a.forcing[q * a.plane + row + src[t]];
+    }
+    for (int j = t; j < kXTile; j += kXThreads) {
+      const int ci = x0 - 2 + j;
+      if (ci <= a.nx + 1) {
+        const long long col = wrap_x(ci, a.nx) + kHs;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) sS[q][j] = from_f64(__ldg(a.forcing + q * a.plane + row + col));
+      }
+    }
+    if (t == 0) {
+      const double hrt = a.hytc[k + kHs];
+      sRow = row_consts(a.hyc[k + kHs], hrt, kC0 * pow(hrt, kGamma));
+    }
+    __syncthreads();
+    if (i <= a.nx) {
+      dw s[4][4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) s[q][j] = sS[q][t + j];
+      dw F[4];
+      flux_x_split(s, sRow, hv12, F);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) sF[q][t] = F[q];
+    }
+    __syncthreads();
+    if (t < kXCells && i < a.nx) {
+      const long long o = row + i + kHs;
+      dw inc[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) inc[q] = mul(sub(sF[q][t], sF[q][t + 1]), c12);
+      if (a.srcw) inc[WMOM] = add(inc[WMOM], mul(from_f64(a.srcw[(long long)k * a.nx + i]), dts));
+#pragma unroll
+      for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = a.init[q * a.plane + o] + to_f64(inc[q]);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kZThreads) k_stage_z_split(SplitArgs a) {
+  __shared__ RowS sRow[kZTile + 1];
+  const int z0 = blockIdx.y * kZTile;
+  const int z1 = min(z0 + kZTile, a.nz);
+  if (threadIdx.x <= z1 - z0) {
+    const int k = z0 + threadIdx.x;
+    sRow[threadIdx.x] = row_consts(a.hyi[k], a.hyti[k], a.hypi[k]);
+  }
+  __syncthreads();
+  const int c = blockIdx.x * kZThreads + threadIdx.x;
+  if ((a.flags & MW_FLAG_WRITE_HALO) && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x < 4) {
+    const int hcol[4] = {0, 1, a.nx + kHs, a.nx + kHs + 1};
+    write_z_halo_column(a, hcol[threadIdx.x]);
+  }
+  if (c >= a.nx) return;
+  const int col = c + kHs;
+  if ((a.flags & MW_FLAG_WRITE_HALO) && blockIdx.y == 0) write_z_halo_column(a, col);
+  const dw hv12 = ld(a.hv12), c12 = ld(a.c12), dts = ld(a.dt), dtg = ld(a.dtg);
+  dw w[4][4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) w[q][j] = from_f64(zval64(a, q, z0 - 2 + j, col));
+  dw Fp[4];
+  flux_z_split(w, sRow[0], hv12, z0 == 0, Fp);
+  for (int k = z0; k < z1; ++k) {
+    const dw rho_k = w[DENS][2];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      w[q][0] = w[q][1];
+      w[q][1] = w[q][2];
+      w[q][2] = w[q][3];
+      w[q][3] = from_f64(zval64(a, q, k + 2, col));
+    }
+    dw Fn[4];
+    flux_z_split(w, sRow[k + 1 - z0], hv12, k + 1 == a.nz, Fn);
+    const long long o = (long long)(k + kHs) * a.pitch + col;
+    dw inc[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) inc[q] = mul(sub(Fp[q], Fn[q]), c12);
+    inc[WMOM] = sub(inc[WMOM], mul(rho_k, dtg));
+    if (a.srcw) inc[WMOM] = add(inc[WMOM], mul(from_f64(a.srcw[(long long)k * a.nx + c]), dts));
+#pragma unroll
+    for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = a.init[q * a.plane + o] + to_f64(inc[q]);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) Fp[q] = Fn[q];
+  }
+}
+
+}  // namespace
+
+int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
+                       const double* hyi, const double* hyti, const double* hypi, const double* srcw,
+                       const double* init, double* forcing, double* out, double dt_stage, int direction,
+                       unsigned flags, cudaStream_t stream) {
+  const Geom g = make_geom(nx, nz);
+  SplitArgs a;
+  a.nx = nx;
+  a.nz = nz;
+  a.pitch = g.pitch;
+  a.plane = g.plane;
+  a.hyc = hyc;
+  a.hytc = hytc;
+  a.hyi = hyi;
+  a.hyti = hyti;
+  a.hypi = hypi;
+  a.srcw = srcw;
+  a.init = init;
+  a.forcing = forcing;
+  a.out = out;
+  a.flags = flags;
+  const double d = direction == MW_DIR_X ? dx : dz;
+  const double hv = -kHvBeta * d / (16 * dt_full);
+  a.hv12 = split_host(12.0 * hv);
+  a.c12 = split_host(dt_stage / (12.0 * d));
+  a.dt = split_host(dt_stage);
+  a.dtg = split_host(dt_stage * kGrav);
+  if (direction == MW_DIR_X) {
+    dim3 grid((nx + kXCells - 1) / kXCells, (unsigned)min(nz, 65535));
+    k_stage_x_split<<<grid, kXThreads, 0, stream>>>(a);
+  } else {
+    dim3 grid((nx + kZThreads - 1) / kZThreads, (nz + kZTile - 1) / kZTile);
+    k_stage_z_split<<<grid, kZThreads, 0, stream>>>(a);
+  }
+  return check_launch(direction == MW_DIR_X ? "x split direction-stage launch" : "z split direction-stage launch");
+}
+
+}  // namespace mw

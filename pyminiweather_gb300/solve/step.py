@@ -1,0 +1,106 @@
+"""Time stepping: the GPU counterpart of pyminiweather/solve/step.py:18-143.
+
+evolve() advances the state by whole time steps through mw_step_* (six fused
+direction-stage launches per step).  discrete_step() runs one direction-stage
+through mw_dirstage_*.  Both write the halo cells of each forcing array as
+set_bc_x / set_bc_z do, so `fields.state` and `fields.state_tmp` hold, halo
+included, what the reference leaves in them.
+
+The direction order alternates from step to step through the module-global
+flag `reverse_direction`, as in the reference (step.py:18,103-109,143): the
+first step after import runs z then x.  reset_direction() restores that.
+
+FP64 arithmetic mode (params["f64_mode"], default DEFAULT_F64_MODE):
+  "split"  - GB300 form: FP64 loads, stores and stage update, interior
+             arithmetic in pairs of FP32 (GB300 retires FP64 at 1/64 of the
+             FP32 rate);
+  "native" - every operation on the FP64 pipe with the reference's formulas.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Dict
+
+import torch
+
+from .. import _native
+from ..ics.directions import Directions
+
+reverse_direction: bool = False
+DEFAULT_F64_MODE = "split"
+
+
+def reset_direction(value: bool = False) -> None:
+    """Set the direction flag (False: the next step runs z then x)."""
+    global reverse_direction
+    reverse_direction = bool(value)
+
+
+def f64_mode(params: Dict) -> int:
+    mode = params.get("f64_mode", DEFAULT_F64_MODE)
+    if mode not in _native.F64_MODES:
+        raise ValueError("f64_mode must be one of %s" % sorted(_native.F64_MODES))
+    return _native.F64_MODES[mode]
+
+
+def _check_state(fields, t, name):
+    return _native.require_cuda(t, name, dtype=fields.dtype, shape=fields.shape)
+
+
+def _dirstage(params, fields, init, forcing, out, dt, direction: int, flags: int):
+    hb = [_native.ptr(a) for a in fields.backgrounds()]
+    args = (fields.nx, fields.nz, float(params["dx"]), float(params["dz"]), float(params["dt"]), *hb,
+            _native.ptr(fields.src_w), _native.ptr(init), _native.ptr(forcing), _native.ptr(out), float(dt), direction)
+    if fields.dtype == torch.float64:
+        _native.call("mw_dirstage_f64", *args, f64_mode(params), flags, _native.stream_handle(fields.device))
+    else:
+        _native.call("mw_dirstage_f32", *args, flags, _native.stream_handle(fields.device))
+
+
+def discrete_step(params: Dict, fields, mesh, state_init, state_forcing, state_out, dt: float,
+                  direction: Directions) -> None:
+    """One direction-stage: state_out = state_init + dt * tend(state_forcing).
+
+    Like the reference it writes the halo of state_forcing; state_out may be
+    the same array as state_forcing (stage 2 of the reference's RK3) -- the
+    kernel then writes fields.scratch and the interior is copied over.
+    """
+    for t, n in ((state_init, "state_init"), (state_forcing, "state_forcing"), (state_out, "state_out")):
+        _check_state(fields, t, n)
+    d = _native.MW_DIR_X if direction == Directions.X else _native.MW_DIR_Z
+    if params.get("ic_type") == "injection":
+        raise NotImplementedError("the injection case is flagged unsupported by the reference")
+    flags = _native.MW_FLAG_WRITE_HALO
+    if state_out.data_ptr() == state_forcing.data_ptr():
+        tmp = fields.scratch
+        if tmp.data_ptr() in (state_init.data_ptr(), state_forcing.data_ptr()):
+            tmp = torch.empty_like(tmp)
+        _dirstage(params, fields, state_init, state_forcing, tmp, dt, d, flags)
+        h = fields.hs
+        state_out[:, h:-h, h:-h].copy_(tmp[:, h:-h, h:-h])
+    else:
+        _dirstage(params, fields, state_init, state_forcing, state_out, dt, d, flags)
+
+
+def evolve(params: Dict, fields, mesh=None, dt: float = 1e-4, nsteps: int = 1) -> None:
+    """Advance fields.state by nsteps time steps of size dt (step.py:85-143).
+
+    Hyperviscosity uses params["dt"], as in the reference.
+    """
+    global reverse_direction
+    _check_state(fields, fields.state, "fields.state")
+    _check_state(fields, fields.state_tmp, "fields.state_tmp")
+    _check_state(fields, fields.scratch, "fields.scratch")
+    if params.get("ic_type") == "injection":
+        raise NotImplementedError("the injection case is flagged unsupported by the reference")
+    rv = ctypes.c_int(1 if reverse_direction else 0)
+    hb = [_native.ptr(a) for a in fields.backgrounds()]
+    args = [fields.nx, fields.nz, float(params["dx"]), float(params["dz"]), float(params["dt"]), float(dt), *hb,
+            _native.ptr(fields.src_w), _native.ptr(fields.state), _native.ptr(fields.state_tmp),
+            _native.ptr(fields.scratch), int(nsteps), ctypes.byref(rv)]
+    flags = params.get("step_flags", _native.MW_FLAG_WRITE_HALO)
+    if fields.dtype == torch.float64:
+        _native.call("mw_step_f64", *args, f64_mode(params), flags, _native.stream_handle(fields.device))
+    else:
+        _native.call("mw_step_f32", *args, flags, _native.stream_handle(fields.device))
+    reverse_direction = bool(rv.value)

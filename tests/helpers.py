@@ -1,0 +1,55 @@
+"""Shared test helpers: golden fixtures, parameters, error metrics."""
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+# (fixture name, ic_type, nx, nz)
+CASES = [
+    ("thermal_100x50", "thermal", 100, 50),
+    ("collision_64x32", "collision", 64, 32),
+    ("collision_37x13", "collision", 37, 13),
+    ("gravity_48x24", "gravity", 48, 24),
+    ("density_current_40x20", "density-current", 40, 20),
+]
+
+BACKGROUNDS = ("hy_dens_cell", "hy_dens_theta_cell", "hy_dens_int", "hy_dens_theta_int", "hy_pressure_int")
+
+# The time-step tolerance the benchmark states: per-variable normwise error
+# max|a - b| / max|b| over the interior after the run.
+TOL_STEP = 1e-10
+
+
+def golden(name):
+    return np.load(os.path.join(GOLDEN, name + ".npz"))
+
+
+def make_params(nx, nz, ic_type, cfl=1.5, max_speed=450.0, xlen=2e4, zlen=1e4):
+    """The params dict of the reference CLI (pyminiweather/__main__.py:160-195)."""
+    p = dict(nx=nx, nz=nz, xlen=xlen, zlen=zlen, hs=2, s=4, ic_type=ic_type, cfl=cfl, max_speed=max_speed)
+    p["dx"] = p["xlen"] / p["nx"]
+    p["dz"] = p["zlen"] / p["nz"]
+    p["dt"] = min(p["dx"], p["dz"]) * cfl / max_speed
+    return p
+
+
+def normwise(a, b, hs=2, interior=True):
+    """Per-variable max|a-b| / max|b| (interior cells by default)."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    if interior:
+        a = a[:, hs:-hs, hs:-hs]
+        b = b[:, hs:-hs, hs:-hs]
+    out = []
+    for v in range(a.shape[0]):
+        den = np.abs(b[v]).max()
+        num = np.abs(a[v] - b[v]).max()
+        out.append(float(num / den) if den > 0 else float(num))
+    return out
+
+
+def rel_l2(a, b, hs=2):
+    a = np.asarray(a, dtype=np.float64)[:, hs:-hs, hs:-hs]
+    b = np.asarray(b, dtype=np.float64)[:, hs:-hs, hs:-hs]
+    return [float(np.linalg.norm(a[v] - b[v]) / max(np.linalg.norm(b[v]), 1e-300)) for v in range(a.shape[0])]

@@ -1,0 +1,255 @@
+"""Parity of the CUDA path with the reference (golden fixtures made by running
+it) and with the CPU oracle, through the package API and the C ABI.
+
+Tolerances (stated by the benchmark): the FP64 time step must stay within
+1e-10 per-variable normwise error (max|a-b| / max|b| over the interior) of
+the reference after 200 steps; the FP32 form within 1e-4 relative L2.
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from pyminiweather_gb300 import IDS, _native
+from pyminiweather_gb300.data import initialize_fields
+from pyminiweather_gb300.ics import Directions, init, set_bc_x, set_bc_z
+from pyminiweather_gb300.post import compute_solution_variables, compute_stats
+from pyminiweather_gb300.solve import (add_source_terms, compute_flux_x, compute_flux_z, compute_tend_x,
+                                       compute_tend_z, discrete_step, evolve, interpolate_x, interpolate_z,
+                                       reset_direction)
+from tests.helpers import BACKGROUNDS, CASES, TOL_STEP, golden, make_params, normwise, rel_l2
+
+pytestmark = pytest.mark.gpu
+MODES = ["split", "native"]
+
+
+def setup(ic, nx, nz, dtype=torch.float64, mode="split"):
+    p = make_params(nx, nz, ic)
+    p["f64_mode"] = mode
+    f = initialize_fields(p, dtype=dtype)
+    init(f, p)
+    reset_direction()
+    return p, f
+
+
+def host(t):
+    return t.detach().to(torch.float64).cpu().numpy()
+
+
+@pytest.mark.parametrize("name,ic,nx,nz", CASES)
+def test_initial_condition_vs_reference(name, ic, nx, nz):
+    g = golden(name)
+    p, f = setup(ic, nx, nz)
+    for k in BACKGROUNDS:
+        b = g[k]
+        assert np.abs(host(getattr(f, k)) - b).max() <= 1e-15 * np.abs(b).max(), k
+    st = host(f.state)
+    for v in range(4):  # every cell, halo included
+        b = g["state_0"][v]
+        assert np.abs(st[v] - b).max() <= 1e-13 * max(np.abs(b).max(), 1e-300), v
+    assert np.array_equal(host(f.state_tmp), st)
+    np.testing.assert_allclose(compute_stats(p, f), g["stats_0"], rtol=1e-13)
+
+
+def test_thermal_initial_fields():  # tests/unit/test_initial_conditions.py:13-41
+    p, f = setup("thermal", 200, 100)
+    st = host(f.state)
+    assert np.all(st[IDS.DENS] == 0) and np.all(st[IDS.UMOM] == 0) and np.all(st[IDS.WMOM] == 0)
+    assert np.count_nonzero(st[IDS.RHOT]) > 0
+    # constant-theta background: theta = 300 at every interface (initial_conditions.py:26-52)
+    th = host(f.hy_dens_theta_int) / host(f.hy_dens_int)
+    np.testing.assert_allclose(th, 300.0, rtol=1e-15)
+    assert np.all(np.diff(host(f.hy_dens_int)) < 0)
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("name,ic,nx,nz", CASES)
+def test_time_steps_vs_reference(mode, name, ic, nx, nz):
+    g = golden(name)
+    p, f = setup(ic, nx, nz, mode=mode)
+    done = 0
+    worst = 0.0
+    for c in g["checkpoints"]:
+        c = int(c)
+        evolve(p, f, None, dt=p["dt"], nsteps=c - done)
+        done = c
+        err = normwise(host(f.state), g["state_%d" % c])
+        errh = normwise(host(f.state), g["state_%d" % c], interior=False)
+        errt = normwise(host(f.state_tmp), g["state_tmp_%d" % c], interior=False)
+        worst = max(worst, max(err))
+        print("%s %s step %d normwise %s halo %.2e tmp %.2e" % (mode, name, c, ["%.2e" % e for e in err],
+                                                              max(errh), max(errt)))
+        assert max(err) <= TOL_STEP and max(errh) <= TOL_STEP and max(errt) <= TOL_STEP, (c, err, errh, errt)
+        np.testing.assert_allclose(compute_stats(p, f), g["stats_%d" % c], rtol=1e-12)
+    sv = host(compute_solution_variables(p, f))
+    gs = g["svars_%d" % done]
+    for v in range(4):
+        assert np.abs(sv[v] - gs[v]).max() <= TOL_STEP * max(np.abs(gs[v]).max(), 1e-300) * 10
+
+
+def _stage_fields(g, p, mode="split"):
+    f = initialize_fields(p)
+    for k in BACKGROUNDS:
+        getattr(f, k).copy_(torch.from_numpy(g[k]))
+    p["f64_mode"] = mode
+    return f
+
+
+def test_unfused_pieces_vs_reference():
+    """interpolate / flux / tend / set_bc / update kernels against the
+    reference's intermediate arrays of one discrete_step per direction."""
+    g = golden("stage_collision_24x12")
+    p = make_params(24, 12, "collision")
+    f = _stage_fields(g, p)
+    dev = f.device
+    for name in ("x", "z"):
+        st = torch.from_numpy(g["state_in"]).to(dev)
+        (set_bc_x if name == "x" else set_bc_z)(p, f, st, "collision")
+        assert np.array_equal(host(st), g["forcing_after_" + name])  # halo fill is exact
+        (interpolate_x if name == "x" else interpolate_z)(p, f, st)
+        vals = f.vals_x if name == "x" else f.vals_z
+        d3 = f.d3_vals_x if name == "x" else f.d3_vals_z
+        assert np.array_equal(host(vals), g["vals_" + name])  # convolve order reproduced
+        (compute_flux_x if name == "x" else compute_flux_z)(p, f)
+        gd3 = g["d3_vals_" + name]
+        assert np.array_equal(host(d3), gd3)
+        fl, gfl = host(f.flux), g["flux_" + name]
+        sl = (slice(None), slice(0, 12), slice(0, 25)) if name == "x" else (slice(None), slice(0, 13), slice(0, 24))
+        for v in range(4):
+            assert np.abs(fl[sl][v] - gfl[sl][v]).max() <= 1e-14 * np.abs(gfl[sl][v]).max(), v
+        (compute_tend_x if name == "x" else compute_tend_z)(p, f, st)
+        add_source_terms(p, None, f)
+        tn, gt = host(f.tend), g["tend_" + name]
+        for v in range(4):
+            assert np.abs(tn[v] - gt[v]).max() <= 1e-12 * np.abs(gt[v]).max(), v
+        out = torch.zeros_like(st)
+        _native.call("mw_update_f64", f.nx, f.nz, _native.ptr(st), _native.ptr(f.tend), _native.ptr(out),
+                     p["dt"] / 3, _native.stream_handle())
+        assert max(normwise(host(out), g["out_" + name])) <= 1e-13
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_fused_discrete_step_vs_reference(mode):
+    g = golden("stage_collision_24x12")
+    p = make_params(24, 12, "collision")
+    f = _stage_fields(g, p, mode)
+    dev = f.device
+    for name, d in (("x", Directions.X), ("z", Directions.Z)):
+        init_ = torch.from_numpy(g["state_in"]).to(dev)
+        forcing = init_.clone()
+        out = torch.zeros_like(init_)
+        discrete_step(p, f, None, init_, forcing, out, p["dt"] / 3, d)
+        # the fused kernel writes the halo of the forcing array as set_bc_* does
+        assert np.array_equal(host(forcing), g["forcing_after_" + name]), name
+        err = normwise(host(out), g["out_" + name])
+        print(mode, name, "stage normwise", ["%.2e" % e for e in err])
+        assert max(err) <= 1e-13, err
+        # aliasing out == forcing, as stage 2 of the reference's RK3 does
+        forcing2 = torch.from_numpy(g["state_in"]).to(dev)
+        discrete_step(p, f, None, init_, forcing2, forcing2, p["dt"] / 3, d)
+        assert max(normwise(host(forcing2), g["out_" + name])) <= 1e-13
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_vs_oracle_1024x512(mode):
+    p = make_params(1024, 512, "collision")
+    p["f64_mode"] = mode
+    f = initialize_fields(p)
+    init(f, p)
+    reset_direction()
+    o = O.OracleSim(O.make_params(1024, 512, "collision"))
+    assert max(normwise(host(f.state), o.state, interior=False)) <= 1e-13
+    for n in (1, 10):
+        evolve(p, f, None, dt=p["dt"], nsteps=n)
+        o.evolve(n)
+        err = normwise(host(f.state), o.state)
+        print(mode, "1024x512 collision after", n, "more steps:", ["%.2e" % e for e in err])
+        assert max(err) <= TOL_STEP
+
+
+def test_fp32_form_error_and_mass():
+    """Precision form: FP32 perturbation fields, FP64 background / IC / reductions."""
+    nx, nz = 512, 256
+    p = make_params(nx, nz, "collision")
+    f = initialize_fields(p, dtype=torch.float32)
+    init(f, p)
+    reset_direction()
+    o = O.OracleSim(O.make_params(nx, nz, "collision"))
+    m0 = compute_stats(p, f)[0]
+    done = 0
+    for c in (50, 100):
+        evolve(p, f, None, dt=p["dt"], nsteps=c - done)
+        o.evolve(c - done)
+        done = c
+        l2 = rel_l2(host(f.state), o.state)
+        mx = normwise(host(f.state), o.state)
+        print("fp32 step %d rel-L2 dens %.2e rhot %.2e max dens %.2e rhot %.2e" % (c, l2[0], l2[3], mx[0], mx[3]))
+        assert l2[IDS.DENS] <= 1e-4 and l2[IDS.RHOT] <= 1e-4
+    m1 = compute_stats(p, f)[0]
+    assert abs(m1 - m0) / m0 <= 1e-9
+
+
+def test_split_matches_native_full_size():
+    """8192 x 4096 collision, one step: the GB300 split form against the
+    native FP64 form, plus size-independent properties: mass conservation
+    and the mirror symmetry of the collision case about x = xlen/2."""
+    nx, nz = 8192, 4096
+    p = make_params(nx, nz, "collision")
+    f = initialize_fields(p)
+    init(f, p)
+    s0 = f.state.clone()
+    m0 = compute_stats(p, f)[0]
+    reset_direction()
+    p["f64_mode"] = "native"
+    evolve(p, f, None, dt=p["dt"], nsteps=1)
+    nat = f.state.clone()
+    f.state.copy_(s0)
+    reset_direction()
+    p["f64_mode"] = "split"
+    evolve(p, f, None, dt=p["dt"], nsteps=1)
+    dif = (f.state - nat)[:, 2:-2, 2:-2].abs().amax(dim=(1, 2))
+    scale = nat[:, 2:-2, 2:-2].abs().amax(dim=(1, 2))
+    err = (dif / scale).tolist()
+    print("8192x4096 split vs native after 1 step:", ["%.2e" % e for e in err])
+    assert max(err) <= 1e-12
+    m1 = compute_stats(p, f)[0]
+    assert abs(m1 - m0) / m0 <= 1e-13
+    s = f.state[:, 2:-2, 2:-2]
+    mir = torch.flip(s, dims=[2])
+    sign = torch.tensor([1.0, -1.0, 1.0, 1.0], dtype=s.dtype, device=s.device).view(4, 1, 1)
+    asym = ((s - sign * mir).abs().amax(dim=(1, 2)) / scale).tolist()
+    print("mirror asymmetry:", ["%.2e" % e for e in asym])
+    assert max(asym) <= 1e-12
+    del nat, s0
+
+
+def test_reference_interpolate_tests():  # tests/unit/test_interpolate.py:11-63
+    scipy_signal = pytest.importorskip("scipy.signal")
+    p = make_params(200, 100, "thermal")
+    f = initialize_fields(p)
+    n = int(np.prod(f.shape))
+    st = np.arange(n, dtype=np.float64).reshape(f.shape)
+    k = np.array([-1.0 / 12, 7.0 / 12, 7.0 / 12, -1.0 / 12])
+    f.state.copy_(torch.from_numpy(st))
+    interpolate_x(p, f)
+    interpolate_z(p, f)
+    vx, vz = host(f.vals_x), host(f.vals_z)
+    for v in range(4):
+        ex = scipy_signal.convolve2d(st[v, 2:102, :], k[np.newaxis, :], mode="same")[:, 2:-1]
+        ez = scipy_signal.convolve2d(st[v, :, 2:202], k[:, np.newaxis], mode="same")[2:-1, :]
+        assert np.allclose(ex, vx[v]) and np.allclose(ez, vz[v])
+
+
+def test_errors_surface_as_exceptions():
+    p, f = setup("thermal", 32, 16)
+    bad = torch.zeros(4, 20, 36, dtype=torch.float32, device=f.device)
+    with pytest.raises(TypeError):
+        interpolate_x(p, f, bad)
+    with pytest.raises(_native.MiniWeatherError) as ei:
+        hb = [_native.ptr(a) for a in f.backgrounds()]
+        _native.call("mw_dirstage_f64", f.nx, f.nz, p["dx"], p["dz"], p["dt"], *hb, None, _native.ptr(f.state),
+                     _native.ptr(f.state), _native.ptr(f.state), p["dt"], 0, 1, 1, _native.stream_handle())
+    assert ei.value.status == 4
+    with pytest.raises(NotImplementedError):
+        evolve(dict(p, ic_type="injection"), f, None, dt=p["dt"])
+    torch.cuda.synchronize()
