@@ -125,7 +125,7 @@ def main():
     # odd, tile-unfriendly sizes
     run_case(R, "collision_37x13", 37, 13, "collision", [3], keep_tmp=True)
     # the other initial conditions, including the gravity-wave forcing
-    run_case(R, "gravity_48x24", 48, 24, "gravity", [5])
+    run_case(R, "gravity_48x24", 48, 24, "gravity", [5, 100])
     run_case(R, "density_current_40x20", 40, 20, "density-current", [5])
     # per-stage intermediates
     run_stage_intermediates(R, "stage_collision_24x12", 24, 12, "collision", presteps=3)

@@ -17,7 +17,7 @@ from pyminiweather_gb300.post import compute_solution_variables, compute_stats
 from pyminiweather_gb300.solve import (add_source_terms, compute_flux_x, compute_flux_z, compute_tend_x,
                                        compute_tend_z, discrete_step, evolve, interpolate_x, interpolate_z,
                                        reset_direction)
-from tests.helpers import BACKGROUNDS, CASES, TOL_STEP, golden, make_params, normwise, rel_l2
+from tests.helpers import BACKGROUNDS, CASES, TOL_CASE, TOL_STEP, golden, make_params, normwise, rel_l2
 
 pytestmark = pytest.mark.gpu
 MODES = ["split", "native"]
@@ -67,6 +67,7 @@ def test_thermal_initial_fields():  # tests/unit/test_initial_conditions.py:13-4
 def test_time_steps_vs_reference(mode, name, ic, nx, nz):
     g = golden(name)
     p, f = setup(ic, nx, nz, mode=mode)
+    tol = TOL_CASE.get(name, TOL_STEP)
     done = 0
     worst = 0.0
     for c in g["checkpoints"]:
@@ -79,12 +80,12 @@ def test_time_steps_vs_reference(mode, name, ic, nx, nz):
         worst = max(worst, max(err))
         print("%s %s step %d normwise %s halo %.2e tmp %.2e" % (mode, name, c, ["%.2e" % e for e in err],
                                                               max(errh), max(errt)))
-        assert max(err) <= TOL_STEP and max(errh) <= TOL_STEP and max(errt) <= TOL_STEP, (c, err, errh, errt)
+        assert max(err) <= tol and max(errh) <= tol and max(errt) <= tol, (c, err, errh, errt)
         np.testing.assert_allclose(compute_stats(p, f), g["stats_%d" % c], rtol=1e-12)
     sv = host(compute_solution_variables(p, f))
     gs = g["svars_%d" % done]
     for v in range(4):
-        assert np.abs(sv[v] - gs[v]).max() <= TOL_STEP * max(np.abs(gs[v]).max(), 1e-300) * 10
+        assert np.abs(sv[v] - gs[v]).max() <= tol * max(np.abs(gs[v]).max(), 1e-300) * 10
 
 
 def _stage_fields(g, p, mode="split"):
@@ -189,38 +190,37 @@ def test_fp32_form_error_and_mass():
     assert abs(m1 - m0) / m0 <= 1e-9
 
 
-def test_split_matches_native_full_size():
-    """8192 x 4096 collision, one step: the GB300 split form against the
-    native FP64 form, plus size-independent properties: mass conservation
-    and the mirror symmetry of the collision case about x = xlen/2."""
-    nx, nz = 8192, 4096
+@pytest.mark.parametrize("mode", ["split"])
+def test_fullsize_200_steps_vs_oracle(mode):
+    """The benchmark's stated criterion: 8192 x 4096 collision, 200 steps,
+    within 1e-10 per-variable normwise of the reference algorithm (the oracle,
+    pinned to the reference at small sizes).  Also mass conservation and the
+    mirror symmetry of the collision case about x = xlen/2."""
+    import os
+    nx, nz, steps = 8192, 4096, 200
     p = make_params(nx, nz, "collision")
+    p["f64_mode"] = mode
     f = initialize_fields(p)
     init(f, p)
-    s0 = f.state.clone()
     m0 = compute_stats(p, f)[0]
     reset_direction()
-    p["f64_mode"] = "native"
-    evolve(p, f, None, dt=p["dt"], nsteps=1)
-    nat = f.state.clone()
-    f.state.copy_(s0)
-    reset_direction()
-    p["f64_mode"] = "split"
-    evolve(p, f, None, dt=p["dt"], nsteps=1)
-    dif = (f.state - nat)[:, 2:-2, 2:-2].abs().amax(dim=(1, 2))
-    scale = nat[:, 2:-2, 2:-2].abs().amax(dim=(1, 2))
-    err = (dif / scale).tolist()
-    print("8192x4096 split vs native after 1 step:", ["%.2e" % e for e in err])
-    assert max(err) <= 1e-12
+    evolve(p, f, None, dt=p["dt"], nsteps=steps)
     m1 = compute_stats(p, f)[0]
-    assert abs(m1 - m0) / m0 <= 1e-13
+    got = host(f.state)
     s = f.state[:, 2:-2, 2:-2]
-    mir = torch.flip(s, dims=[2])
+    scale = s.abs().amax(dim=(1, 2))
     sign = torch.tensor([1.0, -1.0, 1.0, 1.0], dtype=s.dtype, device=s.device).view(4, 1, 1)
-    asym = ((s - sign * mir).abs().amax(dim=(1, 2)) / scale).tolist()
-    print("mirror asymmetry:", ["%.2e" % e for e in asym])
-    assert max(asym) <= 1e-12
-    del nat, s0
+    asym = ((s - sign * torch.flip(s, dims=[2])).abs().amax(dim=(1, 2)) / scale).tolist()
+    del f, s
+    torch.cuda.empty_cache()
+    o = O.OracleSim(O.make_params(nx, nz, "collision"), threads=os.cpu_count())
+    o.evolve(steps)
+    err = normwise(got, o.state)
+    print("%s 8192x4096 collision 200 steps vs oracle: %s  mirror asymmetry %s  mass drift %.2e" % (
+        mode, ["%.2e" % e for e in err], ["%.1e" % a for a in asym], (m1 - m0) / m0))
+    assert max(err) <= TOL_STEP
+    assert max(asym) <= TOL_STEP
+    assert abs(m1 - m0) / m0 <= 1e-13
 
 
 def test_reference_interpolate_tests():  # tests/unit/test_interpolate.py:11-63
