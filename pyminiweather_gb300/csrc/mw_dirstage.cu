@@ -6,10 +6,11 @@
 // update.  Halo cells are never read: the periodic (x) and wall (z) rules of
 // ics/bcs.py are applied to the indices / values as they are loaded.
 //
-// x pass: one CTA row-segment per (row, 255 cells).  Thread t evaluates the
-// flux at interface x0+t into shared memory; after one barrier thread t
-// updates cell x0+t from interfaces t and t+1.  Interface loads are
-// coalesced rows; the four taps hit L1.
+// x pass: a CTA walks a run of 255-cell chunks of one row.  Thread t
+// evaluates the flux at interface x0+t into shared memory; after one barrier
+// thread t updates cell x0+t from interfaces t and t+1.  Interface loads are
+// coalesced rows; the four taps hit L1.  Row constants are formed once per
+// CTA and row.
 // z pass: one thread per column marching down a tile of kZTile rows with a
 // rolling 4-row register window, so every forcing value is loaded once per
 // tile and every interface flux is evaluated once; rows are coalesced across
@@ -19,10 +20,11 @@
 
 namespace mw {
 
-constexpr int kXThreads = 256;          // interfaces per x CTA
-constexpr int kXCells = kXThreads - 1;  // cells updated per x CTA
+constexpr int kXThreads = 256;          // interfaces per x chunk
+constexpr int kXCells = kXThreads - 1;  // cells updated per x chunk
+constexpr int kXBlocksPerRow = 4;       // x CTAs per row; each walks a run of chunks
 constexpr int kZThreads = 128;          // columns per z CTA
-constexpr int kZTile = 32;              // rows marched per z thread
+constexpr int kZTile = 64;              // rows marched per z thread
 
 enum Mode { MODE_NATIVE64 = 0, MODE_SPLIT64 = 1, MODE_F32 = 2 };
 
@@ -43,6 +45,7 @@ struct StageArgs {
   T* forcing;
   T* out;
   unsigned flags;
+  int chunks_per_block;
 };
 
 // ---- interpolation in the accumulation order of scipy.signal.convolve ----
@@ -104,7 +107,23 @@ __device__ __forceinline__ void flux_z_native(const double s[4][4], double hyi, 
 // reference's p - hy_pressure_int; in x the row constant C0 (rho theta)_bg^gamma
 // cancels in the flux difference, so the tendency is unchanged while FP32 no
 // longer differences two values near 1e5.  rho*u is formed as (rho u)' itself.
+// (1+d)^gamma - 1: the binomial series to degree 6 for |d| <= 1/8 (tail below
+// 2^-26 relative), else expm1f(gamma log1pf(d)).
 __device__ __forceinline__ float pgm1f(float d) {
+  constexpr float c1 = float(kGamma);
+  constexpr float c2 = float(kGamma * (kGamma - 1) / 2);
+  constexpr float c3 = float(kGamma * (kGamma - 1) * (kGamma - 2) / 6);
+  constexpr float c4 = float(kGamma * (kGamma - 1) * (kGamma - 2) * (kGamma - 3) / 24);
+  constexpr float c5 = float(kGamma * (kGamma - 1) * (kGamma - 2) * (kGamma - 3) * (kGamma - 4) / 120);
+  constexpr float c6 = float(kGamma * (kGamma - 1) * (kGamma - 2) * (kGamma - 3) * (kGamma - 4) * (kGamma - 5) / 720);
+  if (fabsf(d) <= 0.125f) {
+    float y = fmaf(c6, d, c5);
+    y = fmaf(y, d, c4);
+    y = fmaf(y, d, c3);
+    y = fmaf(y, d, c2);
+    y = fmaf(y, d, c1);
+    return y * d;
+  }
   return expm1f(float(kGamma) * log1pf(d));
 }
 
@@ -186,65 +205,76 @@ __device__ __forceinline__ void write_z_halo_column(const StageArgs<T>& a, int c
 }
 
 // ---------------------------------------------------------------------------
-// x direction-stage
+// x direction-stage: CTA (blockIdx.x, row) walks chunks of kXCells cells.
 template <typename T, int MODE>
 __global__ void __launch_bounds__(kXThreads) k_stage_x(StageArgs<T> a) {
   __shared__ T sF[4][kXThreads];
+  __shared__ RowF sRow;
   const int t = threadIdx.x;
-  const int x0 = blockIdx.x * kXCells;
-  const int i = x0 + t;  // interface index 0..nx (between cells i-1 and i)
+  const int nchunks = (a.nx + kXCells - 1) / kXCells;
+  const int cbeg = blockIdx.x * a.chunks_per_block;
+  const int cend = min(cbeg + a.chunks_per_block, nchunks);
   for (int k = blockIdx.y; k < a.nz; k += gridDim.y) {
     const long long row = (long long)(k + kHs) * a.pitch;
+    if constexpr (MODE != MODE_NATIVE64) {
+      if (t == 0) {
+        RowF r;
+        r.hy_r = split::d2f(a.hyc[k + kHs]);
+        r.hy_rt = split::d2f(a.hytc[k + kHs]);
+        r.inv_hy_rt = 1.0f / r.hy_rt;
+        r.P = float(kC0) * powf(r.hy_rt, float(kGamma));
+        sRow = r;
+      }
+    }
     if ((a.flags & MW_FLAG_WRITE_HALO) && blockIdx.x == 0 && t < 4) {
       const int dst[4] = {0, 1, a.nx + kHs, a.nx + kHs + 1};
       const int src[4] = {a.nx, a.nx + 1, kHs, kHs + 1};
 #pragma unroll
       for (int q = 0; q < 4; ++q) a.forcing[q * a.plane + row + dst[t]] = a.forcing[q * a.plane + row + src[t]];
     }
-    if (i <= a.nx) {
-      T s[4][4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const long long col = wrap_x(i - 2 + j, a.nx) + kHs;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) s[q][j] = __ldg(a.forcing + q * a.plane + row + col);
-      }
-      T F[4];
-      if constexpr (MODE == MODE_NATIVE64) {
-        flux_x_native(s, a.hyc[k + kHs], a.hytc[k + kHs], a.hv, F);
-      } else {
-        const double hr = a.hyc[k + kHs], hrt = a.hytc[k + kHs];
-        RowF r;
-        r.hy_r = split::d2f(hr);
-        r.hy_rt = split::d2f(hrt);
-        r.inv_hy_rt = 1.0f / r.hy_rt;
-        r.P = float(kC0) * powf(r.hy_rt, float(kGamma));
-        flux_x_f32(s, r, float(a.hv), F);
-      }
-#pragma unroll
-      for (int q = 0; q < 4; ++q) sF[q][t] = F[q];
-    }
     __syncthreads();
-    if (t < kXCells && i < a.nx) {
-      const long long o = row + i + kHs;
-      if constexpr (MODE == MODE_NATIVE64) {
-        double tend[4];
+    for (int chunk = cbeg; chunk < cend; ++chunk) {
+      const int x0 = chunk * kXCells;
+      const int i = x0 + t;  // interface index 0..nx (between cells i-1 and i)
+      if (i <= a.nx) {
+        T s[4][4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) tend[q] = -(sF[q][t + 1] - sF[q][t]) / a.dx;
-        if (a.srcw) tend[WMOM] = tend[WMOM] + a.srcw[(long long)k * a.nx + i];
+        for (int j = 0; j < 4; ++j) {
+          const long long col = wrap_x(i - 2 + j, a.nx) + kHs;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = a.init[q * a.plane + o] + a.dt_stage * tend[q];
-      } else {
-        const float c = float(a.dt_stage / a.dx), dt = float(a.dt_stage);
-        float inc[4];
+          for (int q = 0; q < 4; ++q) s[q][j] = __ldg(a.forcing + q * a.plane + row + col);
+        }
+        T F[4];
+        if constexpr (MODE == MODE_NATIVE64) {
+          flux_x_native(s, a.hyc[k + kHs], a.hytc[k + kHs], a.hv, F);
+        } else {
+          flux_x_f32(s, sRow, float(a.hv), F);
+        }
 #pragma unroll
-        for (int q = 0; q < 4; ++q) inc[q] = (sF[q][t] - sF[q][t + 1]) * c;
-        if (a.srcw) inc[WMOM] += dt * split::d2f(a.srcw[(long long)k * a.nx + i]);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = a.init[q * a.plane + o] + inc[q];
+        for (int q = 0; q < 4; ++q) sF[q][t] = F[q];
       }
+      __syncthreads();
+      if (t < kXCells && i < a.nx) {
+        const long long o = row + i + kHs;
+        if constexpr (MODE == MODE_NATIVE64) {
+          double tend[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) tend[q] = -(sF[q][t + 1] - sF[q][t]) / a.dx;
+          if (a.srcw) tend[WMOM] = tend[WMOM] + a.srcw[(long long)k * a.nx + i];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = a.init[q * a.plane + o] + a.dt_stage * tend[q];
+        } else {
+          const float c = float(a.dt_stage / a.dx), dt = float(a.dt_stage);
+          float inc[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) inc[q] = (sF[q][t] - sF[q][t + 1]) * c;
+          if (a.srcw) inc[WMOM] += dt * split::d2f(a.srcw[(long long)k * a.nx + i]);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = a.init[q * a.plane + o] + inc[q];
+        }
+      }
+      __syncthreads();
     }
-    __syncthreads();
   }
 }
 
@@ -281,6 +311,9 @@ __global__ void __launch_bounds__(kZThreads) k_stage_z(StageArgs<T> a) {
       flux_z_f32(w, r, float(a.hv), wall, F);
     }
   };
+  T nxt[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) nxt[q] = zval(a, q, z0 + 2, col);
   T Fp[4];
   flux_at(z0, Fp);
   for (int k = z0; k < z1; ++k) {
@@ -290,7 +323,11 @@ __global__ void __launch_bounds__(kZThreads) k_stage_z(StageArgs<T> a) {
       w[q][0] = w[q][1];
       w[q][1] = w[q][2];
       w[q][2] = w[q][3];
-      w[q][3] = zval(a, q, k + 2, col);
+      w[q][3] = nxt[q];
+    }
+    if (k + 1 < z1) {  // load the row needed by the next iteration now
+#pragma unroll
+      for (int q = 0; q < 4; ++q) nxt[q] = zval(a, q, k + 3, col);
     }
     T Fn[4];
     flux_at(k + 1, Fn);
@@ -366,8 +403,10 @@ static int launch_stage(int nx, int nz, double dx, double dz, double dt_full, co
   a.forcing = forcing;
   a.out = out;
   a.flags = flags;
+  const int nchunks = (nx + kXCells - 1) / kXCells;
+  a.chunks_per_block = (nchunks + kXBlocksPerRow - 1) / kXBlocksPerRow;
   if (direction == MW_DIR_X) {
-    dim3 grid((nx + kXCells - 1) / kXCells, (unsigned)min(nz, 65535));
+    dim3 grid((nchunks + a.chunks_per_block - 1) / a.chunks_per_block, (unsigned)min(nz, 65535));
     k_stage_x<T, MODE><<<grid, kXThreads, 0, stream>>>(a);
   } else {
     dim3 grid((nx + kZThreads - 1) / kZThreads, (nz + kZTile - 1) / kZTile);

@@ -15,9 +15,11 @@
 // with P_row = C0 (rho theta)_bg^gamma.  In z this is the reference's
 // p - hy_pressure_int (interpolate.py:163-165); in x the row constant cancels
 // in the flux difference.  (1 + delta)^gamma - 1 is the binomial series
-// sum_{n=1..16} C(gamma, n) delta^n, whose terms beyond n = 16 are below
-// 2^-56 relative for |delta| <= 1/8; terms 7..16 are summed in FP32, 1..6 in
-// double-FP32.  |delta| > 1/8 falls back to expm1(gamma log1p(delta)) in FP64.
+// sum_n C(gamma, n) delta^n.  For |delta| <= 1/64 (most cells) degree 8 leaves
+// a tail below 2^-56 relative; terms 4..8 are summed in FP32, 1..3 in
+// double-FP32 (the FP32 rounding of a Horner partial sum y_k reaches the
+// result scaled by |delta|^(k-1)).  For |delta| <= 1/8, degree 16 with terms
+// 7..16 in FP32; beyond that, expm1(gamma log1p(delta)) in FP64.
 #include "mw_common.cuh"
 #include "mw_split.cuh"
 
@@ -40,17 +42,20 @@ __constant__ float c_pow_h[7] = {0.f,
 __constant__ float c_pow_l[7] = {0.f,
                                  lo_of(binom_gamma(1)), lo_of(binom_gamma(2)), lo_of(binom_gamma(3)),
                                  lo_of(binom_gamma(4)), lo_of(binom_gamma(5)), lo_of(binom_gamma(6))};
-__constant__ float c_pow_tail[17] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f,
-                                     (float)binom_gamma(7), (float)binom_gamma(8), (float)binom_gamma(9),
-                                     (float)binom_gamma(10), (float)binom_gamma(11), (float)binom_gamma(12),
-                                     (float)binom_gamma(13), (float)binom_gamma(14), (float)binom_gamma(15),
-                                     (float)binom_gamma(16)};
+__constant__ float c_pow_f[17] = {0.f,
+                                  (float)binom_gamma(1), (float)binom_gamma(2), (float)binom_gamma(3),
+                                  (float)binom_gamma(4), (float)binom_gamma(5), (float)binom_gamma(6),
+                                  (float)binom_gamma(7), (float)binom_gamma(8), (float)binom_gamma(9),
+                                  (float)binom_gamma(10), (float)binom_gamma(11), (float)binom_gamma(12),
+                                  (float)binom_gamma(13), (float)binom_gamma(14), (float)binom_gamma(15),
+                                  (float)binom_gamma(16)};
 
 constexpr int kXThreads = 256;
 constexpr int kXCells = kXThreads - 1;
 constexpr int kXTile = kXThreads + 3;  // cells x0-2 .. x0+256
 constexpr int kZThreads = 128;
-constexpr int kZTile = 32;
+constexpr int kZTile = 64;
+constexpr int kXBlocksPerRow = 4;  // x CTAs per row; each walks a run of chunks
 
 struct RowS {
   dw R;    // 12 * background rho
@@ -72,19 +77,31 @@ struct SplitArgs {
   double* forcing;
   double* out;
   unsigned flags;
-  dwc hv12;  // 12 * hv
-  dwc c12;   // dt_stage / (12 d)
-  dwc dt;    // dt_stage
-  dwc dtg;   // dt_stage * grav
+  int chunks_per_block;  // x: 255-cell chunks walked by one CTA
+  dwc hv12;              // 12 * hv
+  double c12;            // dt_stage / (12 d): out = init + c12 * (F(i) - F(i+1))
+  dwc d12;               // 12 d (source term: dt * src = c12 * 12 d * src)
+  dwc gz12;              // 12 dz grav (z gravity term: dt g rho' = c12 * 12 dz g rho')
 };
 
 // (1 + d)^gamma - 1
 __device__ __forceinline__ dw pgm1(dw d) {
-  if (fabsf(d.h) <= 0.125f) {
-    const float df = d.h;
-    float t = c_pow_tail[16];
+  const float ad = fabsf(d.h);
+  const float df = d.h;
+  if (ad <= 0.015625f) {
+    float t = fmaf(c_pow_f[8], df, c_pow_f[7]);
+    t = fmaf(t, df, c_pow_f[6]);
+    t = fmaf(t, df, c_pow_f[5]);
+    t = fmaf(t, df, c_pow_f[4]);
+    dw y = add(mulf(d, t), dw{c_pow_h[3], c_pow_l[3]});
+    y = add(mul(y, d), dw{c_pow_h[2], c_pow_l[2]});
+    y = add(mul(y, d), dw{c_pow_h[1], c_pow_l[1]});
+    return mul(y, d);
+  }
+  if (ad <= 0.125f) {
+    float t = c_pow_f[16];
 #pragma unroll
-    for (int n = 15; n >= 7; --n) t = fmaf(t, df, c_pow_tail[n]);
+    for (int n = 15; n >= 7; --n) t = fmaf(t, df, c_pow_f[n]);
     dw y = add(mulf(d, t), dw{c_pow_h[6], c_pow_l[6]});
 #pragma unroll
     for (int n = 5; n >= 1; --n) y = add(mul(y, d), dw{c_pow_h[n], c_pow_l[n]});
@@ -94,49 +111,59 @@ __device__ __forceinline__ dw pgm1(dw d) {
   return from_f64(expm1(kGamma * log1p(dd)));
 }
 
-// 12 * (4-point interpolation) and the third difference, in the arrangement
-// 7 (s1 + s2) - (s0 + s3) and (s3 - s0) + 3 (s1 - s2).
+// 12 * (4-point interpolation) = 7 (s1 + s2) - (s0 + s3) and the third
+// difference (s3 - s0) - 3 (s2 - s1).  The leading floats are combined with
+// error-free transformations (exact), the trailing floats and the rounding
+// errors are summed in FP32 (error about 2^-48 of the operands), and the pair
+// is renormalised once.
 __device__ __forceinline__ void interp_split(dw s0, dw s1, dw s2, dw s3, dw& A, dw& D) {
-  A = sub(mulf(add(s1, s2), 7.0f), add(s0, s3));
-  D = add(sub(s3, s0), mulf(sub(s1, s2), 3.0f));
+  const dw a = two_sum(s1.h, s2.h);
+  const dw b = two_sum(s0.h, s3.h);
+  const dw a7 = two_prod(a.h, 7.0f);
+  const dw r = two_sum(a7.h, -b.h);
+  const float lo = (fmaf(7.0f, (s1.l + s2.l) + a.l, a7.l) - ((s0.l + s3.l) + b.l)) + r.l;
+  A = fast_two_sum(r.h, lo);
+  const dw p = two_sum(s3.h, -s0.h);
+  const dw q = two_sum(s2.h, -s1.h);
+  const dw q3 = two_prod(q.h, 3.0f);
+  const dw t = two_sum(p.h, -q3.h);
+  const float lo2 = (((s3.l - s0.l) + p.l) - fmaf(3.0f, (s2.l - s1.l) + q.l, q3.l)) + t.l;
+  D = fast_two_sum(t.h, lo2);
 }
 
+// x flux times 12 (interpolate.py:105-129): with q = u = (rho u)'/rho,
+// F = ((rho u)', q (rho u)' + p', q (rho w)', q (rho theta)) - hv d3.
 __device__ __forceinline__ void flux_x_split(const dw s[4][4], const RowS& r, dw hv12, dw F[4]) {
   dw A[4], D[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) interp_split(s[q][0], s[q][1], s[q][2], s[q][3], A[q], D[q]);
-  const dw rho = add(A[DENS], r.R);
-  const dw ri = rcp(rho);
+  const dw ri = rcp(add(A[DENS], r.R));
   const dw u = mul(A[UMOM], ri);
-  const dw w = mul(A[WMOM], ri);
-  const dw th = mul(add(A[RHOT], r.RT), ri);
   const dw pp = mul(r.P12, pgm1(mul(A[RHOT], r.IRT)));
   F[0] = sub(A[UMOM], mul(hv12, D[DENS]));
-  F[1] = sub(add(mul(A[UMOM], u), pp), mul(hv12, D[UMOM]));
-  F[2] = sub(mul(A[UMOM], w), mul(hv12, D[WMOM]));
-  F[3] = sub(mul(A[UMOM], th), mul(hv12, D[RHOT]));
+  F[1] = sub(add(mul(u, A[UMOM]), pp), mul(hv12, D[UMOM]));
+  F[2] = sub(mul(u, A[WMOM]), mul(hv12, D[WMOM]));
+  F[3] = sub(mul(u, add(A[RHOT], r.RT)), mul(hv12, D[RHOT]));
 }
 
+// z flux times 12 (interpolate.py:153-186); w and d3[DENS] vanish at the walls.
 __device__ __forceinline__ void flux_z_split(const dw s[4][4], const RowS& r, dw hv12, bool wall, dw F[4]) {
   dw A[4], D[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) interp_split(s[q][0], s[q][1], s[q][2], s[q][3], A[q], D[q]);
-  const dw rho = add(A[DENS], r.R);
-  const dw ri = rcp(rho);
-  const dw u = mul(A[UMOM], ri);
-  const dw th = mul(add(A[RHOT], r.RT), ri);
+  const dw ri = rcp(add(A[DENS], r.R));
   const dw pp = mul(r.P12, pgm1(mul(A[RHOT], r.IRT)));
   dw rw = A[WMOM];
   dw dd = D[DENS];
-  if (wall) {  // interpolate.py:167-173: w and d3[DENS] vanish at the walls
+  if (wall) {
     rw = dw{0.f, 0.f};
     dd = dw{0.f, 0.f};
   }
   const dw w = mul(rw, ri);
   F[0] = sub(rw, mul(hv12, dd));
-  F[1] = sub(mul(rw, u), mul(hv12, D[UMOM]));
-  F[2] = sub(add(mul(rw, w), pp), mul(hv12, D[WMOM]));
-  F[3] = sub(mul(rw, th), mul(hv12, D[RHOT]));
+  F[1] = sub(mul(w, A[UMOM]), mul(hv12, D[UMOM]));
+  F[2] = sub(add(mul(w, rw), pp), mul(hv12, D[WMOM]));
+  F[3] = sub(mul(w, add(A[RHOT], r.RT)), mul(hv12, D[RHOT]));
 }
 
 __device__ __forceinline__ RowS row_consts(double hy_r, double hy_rt, double P) {
@@ -171,68 +198,84 @@ __device__ __forceinline__ void write_z_halo_column(const SplitArgs& a, int col)
   }
 }
 
+// out = init + c12 (F(i) - F(i+1)): one FP64 add (merging the pair) and one
+// FP64 FMA per value.
+__device__ __forceinline__ double update(double init, dw dF, double c12) { return fma(c12, to_f64(dF), init); }
+
 // ---------------------------------------------------------------------------
+// x: CTA (blockIdx.x, row) walks chunks [blockIdx.x * chunks_per_block, ...)
+// of 255 cells.  Per chunk: stage the 259 forcing values (split once) in
+// shared memory, thread t evaluates the flux at interface x0+t, thread t
+// updates cell x0+t.  The row constants (an FP64 pow) are computed once per
+// CTA and row.
 __global__ void __launch_bounds__(kXThreads) k_stage_x_split(SplitArgs a) {
-  __shared__ dw sS[4][kXTile];
+  __shared__ dw sS[4][kXTile + 1];
   __shared__ dw sF[4][kXThreads];
   __shared__ RowS sRow;
   const int t = threadIdx.x;
-  const int x0 = blockIdx.x * kXCells;
-  const int i = x0 + t;
-  const dw hv12 = ld(a.hv12), c12 = ld(a.c12), dts = ld(a.dt);
+  const int nchunks = (a.nx + kXCells - 1) / kXCells;
+  const int cbeg = blockIdx.x * a.chunks_per_block;
+  const int cend = min(cbeg + a.chunks_per_block, nchunks);
+  const dw hv12 = ld(a.hv12), d12 = ld(a.d12);
   for (int k = blockIdx.y; k < a.nz; k += gridDim.y) {
     const long long row = (long long)(k + kHs) * a.pitch;
+    if (t == 0) {
+      const double hrt = a.hytc[k + kHs];
+      sRow = row_consts(a.hyc[k + kHs], hrt, kC0 * pow(hrt, kGamma));
+    }
     if ((a.flags & MW_FLAG_WRITE_HALO) && blockIdx.x == 0 && t < 4) {
       const int dst[4] = {0, 1, a.nx + kHs, a.nx + kHs + 1};
       const int src[4] = {a.nx, a.nx + 1, kHs, kHs + 1};
 #pragma unroll
       for (int q = 0; q < 4; ++q) a.forcing[q * a.plane + row + dst[t]] = a.forcing[q * a.plane + row + src[t]];
     }
-    for (int j = t; j < kXTile; j += kXThreads) {
-      const int ci = x0 - 2 + j;
-      if (ci <= a.nx + 1) {
-        const long long col = wrap_x(ci, a.nx) + kHs;
+    for (int chunk = cbeg; chunk < cend; ++chunk) {
+      const int x0 = chunk * kXCells;
+      const int i = x0 + t;
+      for (int j = t; j < kXTile; j += kXThreads) {
+        const int ci = x0 - 2 + j;
+        if (ci <= a.nx + 1) {
+          const long long col = wrap_x(ci, a.nx) + kHs;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) sS[q][j] = from_f64(__ldg(a.forcing + q * a.plane + row + col));
+          for (int q = 0; q < 4; ++q) sS[q][j] = from_f64(__ldg(a.forcing + q * a.plane + row + col));
+        }
       }
-    }
-    if (t == 0) {
-      const double hrt = a.hytc[k + kHs];
-      sRow = row_consts(a.hyc[k + kHs], hrt, kC0 * pow(hrt, kGamma));
-    }
-    __syncthreads();
-    if (i <= a.nx) {
-      dw s[4][4];
+      __syncthreads();
+      if (i <= a.nx) {
+        dw s[4][4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q)
+        for (int q = 0; q < 4; ++q)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) s[q][j] = sS[q][t + j];
-      dw F[4];
-      flux_x_split(s, sRow, hv12, F);
+          for (int j = 0; j < 4; ++j) s[q][j] = sS[q][t + j];
+        dw F[4];
+        flux_x_split(s, sRow, hv12, F);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) sF[q][t] = F[q];
-    }
-    __syncthreads();
-    if (t < kXCells && i < a.nx) {
-      const long long o = row + i + kHs;
-      dw inc[4];
+        for (int q = 0; q < 4; ++q) sF[q][t] = F[q];
+      }
+      __syncthreads();
+      if (t < kXCells && i < a.nx) {
+        const long long o = row + i + kHs;
+        dw dF[4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) inc[q] = mul(sub(sF[q][t], sF[q][t + 1]), c12);
-      if (a.srcw) inc[WMOM] = add(inc[WMOM], mul(from_f64(a.srcw[(long long)k * a.nx + i]), dts));
+        for (int q = 0; q < 4; ++q) dF[q] = sub(sF[q][t], sF[q][t + 1]);
+        if (a.srcw) dF[WMOM] = add(dF[WMOM], mul(from_f64(a.srcw[(long long)k * a.nx + i]), d12));
 #pragma unroll
-      for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = a.init[q * a.plane + o] + to_f64(inc[q]);
+        for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = update(a.init[q * a.plane + o], dF[q], a.c12);
+      }
     }
     __syncthreads();
   }
 }
 
+// z: one thread per column marching kZTile rows with a rolling window; the
+// next row is loaded one iteration ahead.
 __global__ void __launch_bounds__(kZThreads) k_stage_z_split(SplitArgs a) {
   __shared__ RowS sRow[kZTile + 1];
   const int z0 = blockIdx.y * kZTile;
   const int z1 = min(z0 + kZTile, a.nz);
-  if (threadIdx.x <= z1 - z0) {
-    const int k = z0 + threadIdx.x;
-    sRow[threadIdx.x] = row_consts(a.hyi[k], a.hyti[k], a.hypi[k]);
+  for (int r = threadIdx.x; r <= z1 - z0; r += kZThreads) {
+    const int k = z0 + r;
+    sRow[r] = row_consts(a.hyi[k], a.hyti[k], a.hypi[k]);
   }
   __syncthreads();
   const int c = blockIdx.x * kZThreads + threadIdx.x;
@@ -243,33 +286,43 @@ __global__ void __launch_bounds__(kZThreads) k_stage_z_split(SplitArgs a) {
   if (c >= a.nx) return;
   const int col = c + kHs;
   if ((a.flags & MW_FLAG_WRITE_HALO) && blockIdx.y == 0) write_z_halo_column(a, col);
-  const dw hv12 = ld(a.hv12), c12 = ld(a.c12), dts = ld(a.dt), dtg = ld(a.dtg);
+  const dw hv12 = ld(a.hv12), d12 = ld(a.d12), gz12 = ld(a.gz12);
   dw w[4][4];
 #pragma unroll
   for (int j = 0; j < 4; ++j)
 #pragma unroll
     for (int q = 0; q < 4; ++q) w[q][j] = from_f64(zval64(a, q, z0 - 2 + j, col));
+  double nxt[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) nxt[q] = zval64(a, q, z0 + 2, col);
   dw Fp[4];
   flux_z_split(w, sRow[0], hv12, z0 == 0, Fp);
   for (int k = z0; k < z1; ++k) {
+    double cur[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) cur[q] = nxt[q];
+    if (k + 1 < z1) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) nxt[q] = zval64(a, q, k + 3, col);
+    }
     const dw rho_k = w[DENS][2];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       w[q][0] = w[q][1];
       w[q][1] = w[q][2];
       w[q][2] = w[q][3];
-      w[q][3] = from_f64(zval64(a, q, k + 2, col));
+      w[q][3] = from_f64(cur[q]);
     }
     dw Fn[4];
     flux_z_split(w, sRow[k + 1 - z0], hv12, k + 1 == a.nz, Fn);
     const long long o = (long long)(k + kHs) * a.pitch + col;
-    dw inc[4];
+    dw dF[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) inc[q] = mul(sub(Fp[q], Fn[q]), c12);
-    inc[WMOM] = sub(inc[WMOM], mul(rho_k, dtg));
-    if (a.srcw) inc[WMOM] = add(inc[WMOM], mul(from_f64(a.srcw[(long long)k * a.nx + c]), dts));
+    for (int q = 0; q < 4; ++q) dF[q] = sub(Fp[q], Fn[q]);
+    dF[WMOM] = sub(dF[WMOM], mul(rho_k, gz12));
+    if (a.srcw) dF[WMOM] = add(dF[WMOM], mul(from_f64(a.srcw[(long long)k * a.nx + c]), d12));
 #pragma unroll
-    for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = a.init[q * a.plane + o] + to_f64(inc[q]);
+    for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = update(a.init[q * a.plane + o], dF[q], a.c12);
 #pragma unroll
     for (int q = 0; q < 4; ++q) Fp[q] = Fn[q];
   }
@@ -300,11 +353,13 @@ int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, con
   const double d = direction == MW_DIR_X ? dx : dz;
   const double hv = -kHvBeta * d / (16 * dt_full);
   a.hv12 = split_host(12.0 * hv);
-  a.c12 = split_host(dt_stage / (12.0 * d));
-  a.dt = split_host(dt_stage);
-  a.dtg = split_host(dt_stage * kGrav);
+  a.c12 = dt_stage / (12.0 * d);
+  a.d12 = split_host(12.0 * d);
+  a.gz12 = split_host(12.0 * dz * kGrav);
+  const int nchunks = (nx + kXCells - 1) / kXCells;
+  a.chunks_per_block = (nchunks + kXBlocksPerRow - 1) / kXBlocksPerRow;
   if (direction == MW_DIR_X) {
-    dim3 grid((nx + kXCells - 1) / kXCells, (unsigned)min(nz, 65535));
+    dim3 grid((nchunks + a.chunks_per_block - 1) / a.chunks_per_block, (unsigned)min(nz, 65535));
     k_stage_x_split<<<grid, kXThreads, 0, stream>>>(a);
   } else {
     dim3 grid((nx + kZThreads - 1) / kZThreads, (nz + kZTile - 1) / kZTile);
