@@ -236,6 +236,13 @@ __global__ void __launch_bounds__(kXThreads) k_stage_x(StageArgs<T> a) {
     for (int chunk = cbeg; chunk < cend; ++chunk) {
       const int x0 = chunk * kXCells;
       const int i = x0 + t;  // interface index 0..nx (between cells i-1 and i)
+      const bool upd = t < kXCells && i < a.nx;
+      const long long o = row + i + kHs;
+      T iv[4];
+      if (upd) {  // issued before the flux so the load latency is covered
+#pragma unroll
+        for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
+      }
       if (i <= a.nx) {
         T s[4][4];
 #pragma unroll
@@ -254,15 +261,14 @@ __global__ void __launch_bounds__(kXThreads) k_stage_x(StageArgs<T> a) {
         for (int q = 0; q < 4; ++q) sF[q][t] = F[q];
       }
       __syncthreads();
-      if (t < kXCells && i < a.nx) {
-        const long long o = row + i + kHs;
+      if (upd) {
         if constexpr (MODE == MODE_NATIVE64) {
           double tend[4];
 #pragma unroll
           for (int q = 0; q < 4; ++q) tend[q] = -(sF[q][t + 1] - sF[q][t]) / a.dx;
           if (a.srcw) tend[WMOM] = tend[WMOM] + a.srcw[(long long)k * a.nx + i];
 #pragma unroll
-          for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = a.init[q * a.plane + o] + a.dt_stage * tend[q];
+          for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = iv[q] + a.dt_stage * tend[q];
         } else {
           const float c = float(a.dt_stage / a.dx), dt = float(a.dt_stage);
           float inc[4];
@@ -270,7 +276,7 @@ __global__ void __launch_bounds__(kXThreads) k_stage_x(StageArgs<T> a) {
           for (int q = 0; q < 4; ++q) inc[q] = (sF[q][t] - sF[q][t + 1]) * c;
           if (a.srcw) inc[WMOM] += dt * split::d2f(a.srcw[(long long)k * a.nx + i]);
 #pragma unroll
-          for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = a.init[q * a.plane + o] + inc[q];
+          for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = iv[q] + inc[q];
         }
       }
       __syncthreads();
@@ -317,6 +323,10 @@ __global__ void __launch_bounds__(kZThreads) k_stage_z(StageArgs<T> a) {
   T Fp[4];
   flux_at(z0, Fp);
   for (int k = z0; k < z1; ++k) {
+    const long long o = (long long)(k + kHs) * a.pitch + col;
+    T iv[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
     const T rho_k = w[DENS][2];  // forcing rho' at cell k (interpolate.py:248-250)
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -331,7 +341,6 @@ __global__ void __launch_bounds__(kZThreads) k_stage_z(StageArgs<T> a) {
     }
     T Fn[4];
     flux_at(k + 1, Fn);
-    const long long o = (long long)(k + kHs) * a.pitch + col;
     if constexpr (MODE == MODE_NATIVE64) {
       double tend[4];
 #pragma unroll
@@ -339,7 +348,7 @@ __global__ void __launch_bounds__(kZThreads) k_stage_z(StageArgs<T> a) {
       tend[WMOM] = tend[WMOM] - rho_k * kGrav;
       if (a.srcw) tend[WMOM] = tend[WMOM] + a.srcw[(long long)k * a.nx + c];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = a.init[q * a.plane + o] + a.dt_stage * tend[q];
+      for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = iv[q] + a.dt_stage * tend[q];
     } else {
       const float cz = float(a.dt_stage / a.dz), dt = float(a.dt_stage);
       float inc[4];
@@ -348,7 +357,7 @@ __global__ void __launch_bounds__(kZThreads) k_stage_z(StageArgs<T> a) {
       inc[WMOM] -= dt * (rho_k * float(kGrav));
       if (a.srcw) inc[WMOM] += dt * split::d2f(a.srcw[(long long)k * a.nx + c]);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = a.init[q * a.plane + o] + inc[q];
+      for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = iv[q] + inc[q];
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) Fp[q] = Fn[q];

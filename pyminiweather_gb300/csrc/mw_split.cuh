@@ -92,45 +92,48 @@ __device__ __forceinline__ dw rcp(dw y) {
 // Conversions by integer operations on the IEEE-754 bit patterns.
 
 // FP64 -> double-word.  h takes the leading 24 significand bits (truncated),
-// l the next 23 rounded to nearest, so |x - (h + l)| <= 2^-47 |x|.  Values
-// below 2^-126 in magnitude become 0 (absolute error < 1.2e-38); NaN and Inf
-// become NaN.
+// l the next 23 rounded to nearest, so |x - (h + l)| <= 2^-47 |x|.
+//   h: the float bit pattern is bits 60..29 of the double (one funnel shift)
+//      with the exponent rebiased from 1023 to 127: adding 0x40000000 modulo
+//      2^32 turns the low 8 exponent bits into the float exponent for every
+//      exponent in float range; the sign is put back with one LOP3.
+//   l: the 29 remaining significand bits, rounded to 23, placed under the
+//      exponent of h minus 23 with an implicit 1 that a float subtraction
+//      removes exactly.
+// |x| < 2^-100 (zero included) gives (0, 0), absolute error < 8e-31; NaN, Inf
+// and |x| >= 2^128 give NaN.
 __device__ __forceinline__ dw from_f64(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
-  const unsigned sign = hi & 0x80000000u;
-  const int E = (int)((hi >> 20) & 0x7ffu);
-  const int ef = E - 1023 + 127;  // biased float exponent of h
-  const unsigned hbits = sign | ((unsigned)ef << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
-  float h = __uint_as_float(hbits);
-  const int el = ef - 23;  // exponent of the unit of the 23-bit remainder field
+  const unsigned ex = hi & 0x7ff00000u;
+  const unsigned sh = __funnelshift_l(lo, hi, 3);
+  const unsigned hb = ((sh + 0x40000000u) & 0x7fffffffu) | (hi & 0x80000000u);
+  const unsigned base = (hb & 0xff800000u) - (23u << 23);
   const unsigned m23 = ((lo & 0x1fffffffu) + 32u) >> 6;
-  const unsigned base = sign | ((unsigned)(el > 0 ? el : 1) << 23);
+  float h = __uint_as_float(hb);
   float l = __uint_as_float(base + m23) - __uint_as_float(base);
-  if (el <= 0) l = 0.0f;
-  if (ef <= 0) {
-    h = __uint_as_float(sign);
+  if (ex < ((1023u - 100u) << 20)) {
+    h = 0.0f;
     l = 0.0f;
   }
-  if (ef >= 255) {
+  if (ex > ((1023u + 127u) << 20)) {
     h = __uint_as_float(0x7fc00000u);
     l = 0.0f;
   }
   return {h, l};
 }
 
-// FP32 -> FP64, exact; subnormal floats become 0.
+// FP32 -> FP64, exact (subnormal floats become 0, Inf/NaN stay Inf/NaN).
 __device__ __forceinline__ double f2d(float f) {
   const unsigned u = __float_as_uint(f);
-  const unsigned sign = u & 0x80000000u;
-  const unsigned ex = (u >> 23) & 0xffu;
-  const unsigned exd = ex == 255u ? 2047u : ex + 896u;
-  unsigned hi = sign | (exd << 20) | ((u & 0x7fffffu) >> 3);
-  unsigned lo = (u & 7u) << 29;
+  const unsigned ex = u & 0x7f800000u;
+  unsigned hi = (((u >> 3) & 0x0fffffffu) + (896u << 20)) | (u & 0x80000000u);
+  unsigned lo = u << 29;
   if (ex == 0u) {
-    hi = sign;
+    hi = u & 0x80000000u;
     lo = 0u;
   }
+  if (ex == 0x7f800000u) hi |= 0x7ff00000u;
   return __longlong_as_double((long long)(((unsigned long long)hi << 32) | lo));
 }
 

@@ -55,7 +55,7 @@ constexpr int kXCells = kXThreads - 1;
 constexpr int kXTile = kXThreads + 3;  // cells x0-2 .. x0+256
 constexpr int kZThreads = 128;
 constexpr int kZTile = 64;
-constexpr int kXBlocksPerRow = 4;  // x CTAs per row; each walks a run of chunks
+constexpr int kXBlocksPerRow = 2;  // x CTAs per row; each walks a run of chunks
 
 struct RowS {
   dw R;    // 12 * background rho
@@ -206,7 +206,9 @@ __device__ __forceinline__ double update(double init, dw dF, double c12) { retur
 // x: CTA (blockIdx.x, row) walks chunks [blockIdx.x * chunks_per_block, ...)
 // of 255 cells.  Per chunk: stage the 259 forcing values (split once) in
 // shared memory, thread t evaluates the flux at interface x0+t, thread t
-// updates cell x0+t.  The row constants (an FP64 pow) are computed once per
+// updates cell x0+t.  The loads of the next chunk's forcing values and of this
+// chunk's init values are issued before the flux evaluation so their latency
+// is covered by it.  The row constants (an FP64 pow) are computed once per
 // CTA and row.
 __global__ void __launch_bounds__(kXThreads) k_stage_x_split(SplitArgs a) {
   __shared__ dw sS[4][kXTile + 1];
@@ -217,6 +219,20 @@ __global__ void __launch_bounds__(kXThreads) k_stage_x_split(SplitArgs a) {
   const int cbeg = blockIdx.x * a.chunks_per_block;
   const int cend = min(cbeg + a.chunks_per_block, nchunks);
   const dw hv12 = ld(a.hv12), d12 = ld(a.d12);
+  // this thread stages tile slots t and (t < 3) t + 256
+  auto load_stage = [&](long long row, int x0, double v0[4], double v1[4]) {
+    const int c0 = x0 - 2 + t, c1 = c0 + kXThreads;
+    if (c0 <= a.nx + 1) {
+      const long long col = wrap_x(c0, a.nx) + kHs;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) v0[q] = __ldg(a.forcing + q * a.plane + row + col);
+    }
+    if (t < kXTile - kXThreads && c1 <= a.nx + 1) {
+      const long long col = wrap_x(c1, a.nx) + kHs;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) v1[q] = __ldg(a.forcing + q * a.plane + row + col);
+    }
+  };
   for (int k = blockIdx.y; k < a.nz; k += gridDim.y) {
     const long long row = (long long)(k + kHs) * a.pitch;
     if (t == 0) {
@@ -229,18 +245,26 @@ __global__ void __launch_bounds__(kXThreads) k_stage_x_split(SplitArgs a) {
 #pragma unroll
       for (int q = 0; q < 4; ++q) a.forcing[q * a.plane + row + dst[t]] = a.forcing[q * a.plane + row + src[t]];
     }
+    double v0[4] = {0, 0, 0, 0}, v1[4] = {0, 0, 0, 0};
+    if (cbeg < cend) load_stage(row, cbeg * kXCells, v0, v1);
     for (int chunk = cbeg; chunk < cend; ++chunk) {
       const int x0 = chunk * kXCells;
       const int i = x0 + t;
-      for (int j = t; j < kXTile; j += kXThreads) {
-        const int ci = x0 - 2 + j;
-        if (ci <= a.nx + 1) {
-          const long long col = wrap_x(ci, a.nx) + kHs;
 #pragma unroll
-          for (int q = 0; q < 4; ++q) sS[q][j] = from_f64(__ldg(a.forcing + q * a.plane + row + col));
-        }
+      for (int q = 0; q < 4; ++q) sS[q][t] = from_f64(v0[q]);
+      if (t < kXTile - kXThreads) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) sS[q][t + kXThreads] = from_f64(v1[q]);
       }
       __syncthreads();
+      const bool upd = t < kXCells && i < a.nx;
+      const long long o = row + i + kHs;
+      double iv[4];
+      if (upd) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
+      }
+      if (chunk + 1 < cend) load_stage(row, x0 + kXCells, v0, v1);
       if (i <= a.nx) {
         dw s[4][4];
 #pragma unroll
@@ -253,14 +277,13 @@ __global__ void __launch_bounds__(kXThreads) k_stage_x_split(SplitArgs a) {
         for (int q = 0; q < 4; ++q) sF[q][t] = F[q];
       }
       __syncthreads();
-      if (t < kXCells && i < a.nx) {
-        const long long o = row + i + kHs;
+      if (upd) {
         dw dF[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) dF[q] = sub(sF[q][t], sF[q][t + 1]);
         if (a.srcw) dF[WMOM] = add(dF[WMOM], mul(from_f64(a.srcw[(long long)k * a.nx + i]), d12));
 #pragma unroll
-        for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = update(a.init[q * a.plane + o], dF[q], a.c12);
+        for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = update(iv[q], dF[q], a.c12);
       }
     }
     __syncthreads();
@@ -269,7 +292,7 @@ __global__ void __launch_bounds__(kXThreads) k_stage_x_split(SplitArgs a) {
 
 // z: one thread per column marching kZTile rows with a rolling window; the
 // next row is loaded one iteration ahead.
-__global__ void __launch_bounds__(kZThreads) k_stage_z_split(SplitArgs a) {
+__global__ void __launch_bounds__(kZThreads, 6) k_stage_z_split(SplitArgs a) {
   __shared__ RowS sRow[kZTile + 1];
   const int z0 = blockIdx.y * kZTile;
   const int z1 = min(z0 + kZTile, a.nz);
@@ -298,6 +321,10 @@ __global__ void __launch_bounds__(kZThreads) k_stage_z_split(SplitArgs a) {
   dw Fp[4];
   flux_z_split(w, sRow[0], hv12, z0 == 0, Fp);
   for (int k = z0; k < z1; ++k) {
+    const long long o = (long long)(k + kHs) * a.pitch + col;
+    double iv[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
     double cur[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) cur[q] = nxt[q];
@@ -315,14 +342,13 @@ __global__ void __launch_bounds__(kZThreads) k_stage_z_split(SplitArgs a) {
     }
     dw Fn[4];
     flux_z_split(w, sRow[k + 1 - z0], hv12, k + 1 == a.nz, Fn);
-    const long long o = (long long)(k + kHs) * a.pitch + col;
     dw dF[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) dF[q] = sub(Fp[q], Fn[q]);
     dF[WMOM] = sub(dF[WMOM], mul(rho_k, gz12));
     if (a.srcw) dF[WMOM] = add(dF[WMOM], mul(from_f64(a.srcw[(long long)k * a.nx + c]), d12));
 #pragma unroll
-    for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = update(a.init[q * a.plane + o], dF[q], a.c12);
+    for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = update(iv[q], dF[q], a.c12);
 #pragma unroll
     for (int q = 0; q < 4; ++q) Fp[q] = Fn[q];
   }
