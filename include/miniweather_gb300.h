@@ -113,6 +113,28 @@ int mw_step_f32(int nx, int nz, double dx, double dz, double dt_full, double dt,
                 int nsteps, int* reverse, unsigned flags, void* stream);
 
 /* ---------------------------------------------------------------------------
+ * mw_step_f64 for callers that cannot allocate device memory.  No counterpart
+ * in the reference: it exists for hosts that own every buffer they hand over
+ * (a Fortran or C model embedding the solver, a custom call in a framework
+ * that pre-allocates all buffers, a real-time loop that forbids allocation
+ * once running) and so cannot supply mw_step_f64's third state-sized array.
+ * That array is instead a fixed device array inside this library, sized for
+ * grids up to 512 x 256 cells ((nx+4)(nz+4) <= 134160); larger grids return
+ * MW_ERR_WORKSPACE with the limit in mw_last_error().  Every GPU that loads
+ * the library holds the array (4.3 MB) until the process exits.  The first
+ * call on each device looks up the array's device address (once per device,
+ * with that device current); make that first call before any stream capture.
+ * All calls share the one array and nothing in it needs to start at zero:
+ * calls that overlap on the GPU (other streams, other host threads) race on
+ * it, so issue them one after another.  Arguments and results are those of
+ * mw_step_f64 without `scratch`; it never calls cudaMalloc or cudaFree.
+ * ------------------------------------------------------------------------- */
+int mw_step_f64_noalloc(int nx, int nz, double dx, double dz, double dt_full, double dt, const double* hy_dens_cell,
+                        const double* hy_dens_theta_cell, const double* hy_dens_int, const double* hy_dens_theta_int,
+                        const double* hy_pressure_int, const double* src_w, double* state, double* state_tmp,
+                        int nsteps, int* reverse, int f64_mode, unsigned flags, void* stream);
+
+/* ---------------------------------------------------------------------------
  * Initial condition: replaces init (pyminiweather/ics/initial.py:11-105):
  * 3x3 Gauss-Legendre cell averages over all (nz+4)(nx+4) cells of the bubbles
  * (sample_ellipse_cosine, utils/utils.py:5-51), plus the hydrostatic

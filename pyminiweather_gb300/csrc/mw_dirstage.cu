@@ -15,6 +15,8 @@
 // rolling 4-row register window, so every forcing value is loaded once per
 // tile and every interface flux is evaluated once; rows are coalesced across
 // the warp.
+#include <mutex>
+
 #include "mw_common.cuh"
 #include "mw_split.cuh"
 
@@ -534,4 +536,79 @@ extern "C" int mw_step_f32(int nx, int nz, double dx, double dz, double dt_full,
                             return launch_stage<float, MODE_F32>(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi,
                                                                  src_w, init, forcing, out, dts, dir, flags, s);
                           });
+}
+
+// ---------------------------------------------------------------------------
+// Time step that allocates nothing.
+//
+// Some callers cannot hand this library a third state-sized array: a host
+// model that keeps its fields in buffers it allocated itself and passes only
+// those (a Fortran or C weather code embedding this solver), a custom call in
+// a framework that pre-allocates every buffer it gives out, or a real-time
+// loop whose rules forbid allocation once it is running.  For them the array
+// the fused step ping-pongs through (see mw_step_f64) is this fixed device
+// array, sized for grids up to 512 x 256 cells; every GPU that loads the
+// library keeps it (4.3 MB) until the process exits.
+namespace mw {
+namespace {
+
+constexpr int kNoAllocMaxNx = 512, kNoAllocMaxNz = 256;
+constexpr long long kNoAllocValues = 4LL * (kNoAllocMaxNx + 2 * kHs) * (kNoAllocMaxNz + 2 * kHs);
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocValues];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+double* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device.  The host-side
+// name is only a stand-in for the symbol, so the address is asked of the
+// runtime once per device, with that device current.
+int noalloc_scratch(double** out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail(MW_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+  if (dev < 0 || dev >= kNoAllocMaxDevices)
+    return fail(MW_ERR_INVALID_ARG, "device %d beyond the %d devices this entry point supports", dev,
+                kNoAllocMaxDevices);
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (g_noalloc_addr[dev] == nullptr) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr)
+      return fail(MW_ERR_CUDA, "cudaGetSymbolAddress of the built-in scratch array: %s", cudaGetErrorString(e));
+    g_noalloc_addr[dev] = (double*)p;
+  }
+  *out = g_noalloc_addr[dev];
+  return MW_OK;
+}
+
+}  // namespace
+}  // namespace mw
+
+extern "C" int mw_step_f64_noalloc(int nx, int nz, double dx, double dz, double dt_full, double dt, const double* hyc,
+                                   const double* hytc, const double* hyi, const double* hyti, const double* hypi,
+                                   const double* src_w, double* state, double* state_tmp, int nsteps, int* reverse,
+                                   int f64_mode, unsigned flags, void* stream) {
+  int st = check_grid(nx, nz);
+  if (st) return st;
+  const long long need = 4LL * (nx + 2 * kHs) * (nz + 2 * kHs);
+  MW_REQUIRE(need <= kNoAllocValues, MW_ERR_WORKSPACE,
+             "grid %d x %d needs %lld scratch values; the built-in array holds %lld (grids up to %d x %d cells, "
+             "or any shape with (nx+4)(nz+4) <= %lld); use mw_step_f64 with a caller-provided scratch array",
+             nx, nz, need, kNoAllocValues, kNoAllocMaxNx, kNoAllocMaxNz, kNoAllocValues / 4);
+  double* scratch = nullptr;
+  st = noalloc_scratch(&scratch);
+  if (st) return st;
+  st = validate_step<double>(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, state, state_tmp, scratch, nsteps,
+                             reverse);
+  if (st) return st;
+  MW_REQUIRE(finite_pos(dt), MW_ERR_INVALID_ARG, "dt must be finite and positive");
+  MW_REQUIRE(f64_mode == MW_F64_NATIVE || f64_mode == MW_F64_SPLIT, MW_ERR_INVALID_ARG, "unknown f64_mode %d",
+             f64_mode);
+  cudaStream_t s = (cudaStream_t)stream;
+  return run_steps<double>(dt, state, state_tmp, scratch, nsteps, reverse,
+                           [&](const double* init, double* forcing, double* out, double dts, int dir) {
+                             return stage_f64(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, src_w, init,
+                                              forcing, out, dts, dir, f64_mode, flags, s);
+                           });
 }
