@@ -266,6 +266,33 @@ def e2e_run(torch, p, f, steps, warmup):
     return ms, nbytes
 
 
+def ensemble_run(torch, steps, warmup, dtype):
+    """The batching form: 256 thermal members of uneven sizes (nx log-uniform in
+    [64, 1024]), autotuned, two steps per CUDA-graph replay."""
+    from pyminiweather_gb300.ensemble import Ensemble, thermal_ensemble
+    ens = Ensemble(thermal_ensemble(256, seed=0), dtype=dtype)
+    tuned = ens.autotune(steps=1)
+    replay = ens.graph()
+    for _ in range(max(1, (warmup + 1) // 2)):
+        replay()
+    torch.cuda.synchronize()
+    reps = max(1, (steps + 1) // 2)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        replay()
+    e1.record()
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    n = 2 * reps
+    out = {"value": ens.cells() * n / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms / n, "steps": n,
+           "members": ens.n_members(), "cells": ens.cells(), "cuda_graph": True, "launches_per_step": 6,
+           "tuning": {k: tuned[k] for k in ("z_tile", "grid_x", "grid_z")}}
+    del ens
+    torch.cuda.empty_cache()
+    return out
+
+
 def cpu_baseline(args, steps):
     from oracle import oracle as O
     threads = os.cpu_count() or 1
@@ -388,6 +415,9 @@ def run_gb300(args):
         line["fp64_" + other] = {"value": world * cells * ks / (mso * 1e-3), "ms_per_step": mso / ks,
                                  "roofline": roofline(pero, cells, 8, peak, peak_kind, kernel_names(True, other),
                                                       traffic)}
+        # the batching form (ensemble of uneven grids), FP64 split and FP32
+        line["ensemble"] = {"fp64": ensemble_run(torch, args.steps, args.warmup, torch.float64),
+                            "fp32": ensemble_run(torch, args.steps, args.warmup, torch.float32)}
         # end to end through the public API with host buffers
         init(fo, p)
         ms_e, nbytes = e2e_run(torch, p, fo, args.steps, 1)

@@ -135,6 +135,50 @@ int mw_step_f64_noalloc(int nx, int nz, double dx, double dz, double dt_full, do
                         int nsteps, int* reverse, int f64_mode, unsigned flags, void* stream);
 
 /* ---------------------------------------------------------------------------
+ * Ensembles of uneven grids.  No counterpart in the reference (one grid per
+ * process there): many members, each a full simulation with its own nx, nz,
+ * dx, dz and dt, advance together, one persistent kernel launch per
+ * direction-stage walking a work list over all members.  Each member's state
+ * is a (4, nz+4, nx+4) block at state_off (elements) in the shared state,
+ * state_tmp and scratch buffers; its backgrounds sit at cell_off (nz+4
+ * values) and int_off (nz+1 values) in the shared background buffers.  dt is
+ * the member's params["dt"]: the RK step and the hyperviscosity time scale.
+ * ------------------------------------------------------------------------- */
+typedef struct mw_ens_member {
+  int nx, nz;
+  double dx, dz, dt;
+  long long state_off, cell_off, int_off;
+} mw_ens_member;
+
+typedef struct mw_ens_plan_info {
+  int n_members, n_x_items, n_z_items, z_tile;
+  size_t members_off, x_items_off, z_items_off, bytes; /* byte offsets / size of the device plan */
+} mw_ens_plan_info;
+
+/* Size and layout of the work plan for these members (host array) with z
+ * work items of z_tile rows (1..64). */
+int mw_ensemble_plan_info(int n_members, const mw_ens_member* members, int z_tile, mw_ens_plan_info* info);
+/* Write the plan into plan_device (info.bytes bytes, 16-byte aligned); the
+ * copy to the device is synchronous. */
+int mw_ensemble_plan(int n_members, const mw_ens_member* members, int z_tile, void* plan_device, size_t plan_bytes,
+                     mw_ens_plan_info* info, void* stream);
+/* nsteps time steps of every member: 6 persistent launches per step, grid_x
+ * and grid_z CTAs (0 = one full-occupancy wave).  The direction order follows
+ * *reverse as in mw_step_f64 (all members alike).  FP64 storage supports
+ * f64_mode MW_F64_SPLIT. */
+int mw_ensemble_step_f64(const void* plan_device, const mw_ens_plan_info* info, const double* hy_dens_cell,
+                         const double* hy_dens_theta_cell, const double* hy_dens_int, const double* hy_dens_theta_int,
+                         const double* hy_pressure_int, double* state, double* state_tmp, double* scratch, int nsteps,
+                         int* reverse, int f64_mode, unsigned flags, int grid_x, int grid_z, void* stream);
+/* Resident CTAs per SM of the persistent ensemble kernels (FP64 split or FP32
+ * storage, x or z direction): a default grid is this times the SM count. */
+int mw_ensemble_occupancy(int f32_storage, int direction, int* blocks_per_sm);
+int mw_ensemble_step_f32(const void* plan_device, const mw_ens_plan_info* info, const double* hy_dens_cell,
+                         const double* hy_dens_theta_cell, const double* hy_dens_int, const double* hy_dens_theta_int,
+                         const double* hy_pressure_int, float* state, float* state_tmp, float* scratch, int nsteps,
+                         int* reverse, unsigned flags, int grid_x, int grid_z, void* stream);
+
+/* ---------------------------------------------------------------------------
  * Initial condition: replaces init (pyminiweather/ics/initial.py:11-105):
  * 3x3 Gauss-Legendre cell averages over all (nz+4)(nx+4) cells of the bubbles
  * (sample_ellipse_cosine, utils/utils.py:5-51), plus the hydrostatic

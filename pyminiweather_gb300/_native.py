@@ -36,6 +36,11 @@ _SIGNATURES = {
     "mw_step_f32": [_i, _i, _d, _d, _d, _d, _P, _P, _P, _P, _P, _P, _P, _P, _P, _i, ctypes.POINTER(_i), _u, _P],
     "mw_step_f64_noalloc": [_i, _i, _d, _d, _d, _d, _P, _P, _P, _P, _P, _P, _P, _P, _i, ctypes.POINTER(_i), _i, _u,
                             _P],
+    "mw_ensemble_plan_info": [_i, _P, _i, _P],
+    "mw_ensemble_plan": [_i, _P, _i, _P, _sz, _P, _P],
+    "mw_ensemble_step_f64": [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _i, ctypes.POINTER(_i), _i, _u, _i, _i, _P],
+    "mw_ensemble_step_f32": [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _i, ctypes.POINTER(_i), _u, _i, _i, _P],
+    "mw_ensemble_occupancy": [_i, _i, ctypes.POINTER(_i)],
     "mw_init_f64": [_i, _i, _d, _d, _i, _d, _i, _P, _P, _P, _P, _P, _P, _P, _P],
     "mw_init_f32": [_i, _i, _d, _d, _i, _d, _i, _P, _P, _P, _P, _P, _P, _P, _P],
     "mw_gravity_source_f64": [_i, _i, _d, _d, _P, _P, _P],
@@ -55,6 +60,20 @@ _SIGNATURES = {
 }
 _RESTYPES = {"mw_last_error": ctypes.c_char_p, "mw_status_string": ctypes.c_char_p,
              "mw_stats_workspace_bytes": _sz}
+
+
+class EnsMember(ctypes.Structure):
+    """mw_ens_member of include/miniweather_gb300.h."""
+    _fields_ = [("nx", ctypes.c_int), ("nz", ctypes.c_int), ("dx", ctypes.c_double), ("dz", ctypes.c_double),
+                ("dt", ctypes.c_double), ("state_off", ctypes.c_longlong), ("cell_off", ctypes.c_longlong),
+                ("int_off", ctypes.c_longlong)]
+
+
+class EnsPlanInfo(ctypes.Structure):
+    """mw_ens_plan_info of include/miniweather_gb300.h."""
+    _fields_ = [("n_members", ctypes.c_int), ("n_x_items", ctypes.c_int), ("n_z_items", ctypes.c_int),
+                ("z_tile", ctypes.c_int), ("members_off", ctypes.c_size_t), ("x_items_off", ctypes.c_size_t),
+                ("z_items_off", ctypes.c_size_t), ("bytes", ctypes.c_size_t)]
 
 
 class MiniWeatherError(RuntimeError):

@@ -18,6 +18,7 @@
 #include <mutex>
 
 #include "mw_common.cuh"
+#include "mw_ensemble.cuh"
 #include "mw_split.cuh"
 
 namespace mw {
@@ -207,163 +208,268 @@ __device__ __forceinline__ void write_z_halo_column(const StageArgs<T>& a, int c
 }
 
 // ---------------------------------------------------------------------------
-// x direction-stage: CTA (blockIdx.x, row) walks chunks of kXCells cells.
+// Tiles, called by the single-grid kernels and the persistent ensemble
+// kernels alike; every thread of the CTA must call them (they contain barriers).
+template <typename T>
+struct SmemXT {
+  T sF[4][kXThreads];
+  RowF row;
+};
+struct SmemZT {
+  RowF row[kEnsZTileMax + 1];
+};
+
+__device__ __forceinline__ RowF rowf_x(double hy_r, double hy_rt) {
+  RowF r;
+  r.hy_r = split::d2f(hy_r);
+  r.hy_rt = split::d2f(hy_rt);
+  r.inv_hy_rt = 1.0f / r.hy_rt;
+  r.P = float(kC0) * powf(r.hy_rt, float(kGamma));
+  return r;
+}
+
+__device__ __forceinline__ RowF rowf_z(double hy_r, double hy_rt, double hy_p) {
+  RowF r;
+  r.hy_r = split::d2f(hy_r);
+  r.hy_rt = split::d2f(hy_rt);
+  r.inv_hy_rt = 1.0f / r.hy_rt;
+  r.P = split::d2f(hy_p);
+  return r;
+}
+
+// x: row k, chunks [cbeg, cend) of kXCells cells.  Thread t evaluates the
+// flux at interface x0+t into shared memory; after one barrier thread t
+// updates cell x0+t.  halo: write this row's periodic halo into forcing.
 template <typename T, int MODE>
-__global__ void __launch_bounds__(kXThreads) k_stage_x(StageArgs<T> a) {
-  __shared__ T sF[4][kXThreads];
-  __shared__ RowF sRow;
+__device__ __forceinline__ void x_rowrun_t(const StageArgs<T>& a, int k, int cbeg, int cend, bool halo,
+                                           SmemXT<T>& sm) {
   const int t = threadIdx.x;
-  const int nchunks = (a.nx + kXCells - 1) / kXCells;
-  const int cbeg = blockIdx.x * a.chunks_per_block;
-  const int cend = min(cbeg + a.chunks_per_block, nchunks);
-  for (int k = blockIdx.y; k < a.nz; k += gridDim.y) {
-    const long long row = (long long)(k + kHs) * a.pitch;
-    if constexpr (MODE != MODE_NATIVE64) {
-      if (t == 0) {
-        RowF r;
-        r.hy_r = split::d2f(a.hyc[k + kHs]);
-        r.hy_rt = split::d2f(a.hytc[k + kHs]);
-        r.inv_hy_rt = 1.0f / r.hy_rt;
-        r.P = float(kC0) * powf(r.hy_rt, float(kGamma));
-        sRow = r;
-      }
-    }
-    if ((a.flags & MW_FLAG_WRITE_HALO) && blockIdx.x == 0 && t < 4) {
-      const int dst[4] = {0, 1, a.nx + kHs, a.nx + kHs + 1};
-      const int src[4] = {a.nx, a.nx + 1, kHs, kHs + 1};
+  const long long row = (long long)(k + kHs) * a.pitch;
+  if constexpr (MODE != MODE_NATIVE64) {
+    if (t == 0) sm.row = rowf_x(a.hyc[k + kHs], a.hytc[k + kHs]);
+  }
+  if (halo && t < 4) {
+    const int dst[4] = {0, 1, a.nx + kHs, a.nx + kHs + 1};
+    const int src[4] = {a.nx, a.nx + 1, kHs, kHs + 1};
 #pragma unroll
-      for (int q = 0; q < 4; ++q) a.forcing[q * a.plane + row + dst[t]] = a.forcing[q * a.plane + row + src[t]];
+    for (int q = 0; q < 4; ++q) a.forcing[q * a.plane + row + dst[t]] = a.forcing[q * a.plane + row + src[t]];
+  }
+  __syncthreads();
+  for (int chunk = cbeg; chunk < cend; ++chunk) {
+    const int x0 = chunk * kXCells;
+    const int i = x0 + t;  // interface index 0..nx (between cells i-1 and i)
+    const bool upd = t < kXCells && i < a.nx;
+    const long long o = row + i + kHs;
+    T iv[4];
+    if (upd) {  // issued before the flux so the load latency is covered
+#pragma unroll
+      for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
+    }
+    if (i <= a.nx) {
+      T s[4][4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const long long col = wrap_x(i - 2 + j, a.nx) + kHs;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) s[q][j] = __ldg(a.forcing + q * a.plane + row + col);
+      }
+      T F[4];
+      if constexpr (MODE == MODE_NATIVE64) {
+        flux_x_native(s, a.hyc[k + kHs], a.hytc[k + kHs], a.hv, F);
+      } else {
+        flux_x_f32(s, sm.row, float(a.hv), F);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) sm.sF[q][t] = F[q];
     }
     __syncthreads();
-    for (int chunk = cbeg; chunk < cend; ++chunk) {
-      const int x0 = chunk * kXCells;
-      const int i = x0 + t;  // interface index 0..nx (between cells i-1 and i)
-      const bool upd = t < kXCells && i < a.nx;
-      const long long o = row + i + kHs;
-      T iv[4];
-      if (upd) {  // issued before the flux so the load latency is covered
+    if (upd) {
+      if constexpr (MODE == MODE_NATIVE64) {
+        double tend[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
+        for (int q = 0; q < 4; ++q) tend[q] = -(sm.sF[q][t + 1] - sm.sF[q][t]) / a.dx;
+        if (a.srcw) tend[WMOM] = tend[WMOM] + a.srcw[(long long)k * a.nx + i];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = iv[q] + a.dt_stage * tend[q];
+      } else {
+        const float c = float(a.dt_stage / a.dx), dt = float(a.dt_stage);
+        float inc[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) inc[q] = (sm.sF[q][t] - sm.sF[q][t + 1]) * c;
+        if (a.srcw) inc[WMOM] += dt * split::d2f(a.srcw[(long long)k * a.nx + i]);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = iv[q] + inc[q];
       }
-      if (i <= a.nx) {
-        T s[4][4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const long long col = wrap_x(i - 2 + j, a.nx) + kHs;
-#pragma unroll
-          for (int q = 0; q < 4; ++q) s[q][j] = __ldg(a.forcing + q * a.plane + row + col);
-        }
-        T F[4];
-        if constexpr (MODE == MODE_NATIVE64) {
-          flux_x_native(s, a.hyc[k + kHs], a.hytc[k + kHs], a.hv, F);
-        } else {
-          flux_x_f32(s, sRow, float(a.hv), F);
-        }
-#pragma unroll
-        for (int q = 0; q < 4; ++q) sF[q][t] = F[q];
-      }
-      __syncthreads();
-      if (upd) {
-        if constexpr (MODE == MODE_NATIVE64) {
-          double tend[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) tend[q] = -(sF[q][t + 1] - sF[q][t]) / a.dx;
-          if (a.srcw) tend[WMOM] = tend[WMOM] + a.srcw[(long long)k * a.nx + i];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = iv[q] + a.dt_stage * tend[q];
-        } else {
-          const float c = float(a.dt_stage / a.dx), dt = float(a.dt_stage);
-          float inc[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) inc[q] = (sF[q][t] - sF[q][t + 1]) * c;
-          if (a.srcw) inc[WMOM] += dt * split::d2f(a.srcw[(long long)k * a.nx + i]);
-#pragma unroll
-          for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = iv[q] + inc[q];
-        }
-      }
-      __syncthreads();
     }
+    __syncthreads();
   }
 }
 
-// ---------------------------------------------------------------------------
-// z direction-stage
+// z: columns [cb*128, cb*128+128), rows [z0, z0+zt), zt <= kEnsZTileMax; one
+// thread per column marching the rows with a rolling 4-row window, the next
+// row loaded one step ahead.  halo: write the wall halo rows of these columns
+// (cb == 0 also does the four x-halo columns).
 template <typename T, int MODE>
-__global__ void __launch_bounds__(kZThreads) k_stage_z(StageArgs<T> a) {
-  const int c = blockIdx.x * kZThreads + threadIdx.x;  // interior column
-  if ((a.flags & MW_FLAG_WRITE_HALO) && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x < 4) {
+__device__ __forceinline__ void z_tile_t(const StageArgs<T>& a, int cb, int z0, int zt, bool halo, SmemZT& sm) {
+  const int z1 = min(z0 + zt, a.nz);
+  if constexpr (MODE != MODE_NATIVE64) {
+    for (int r = threadIdx.x; r <= z1 - z0; r += kZThreads) {
+      const int k = z0 + r;
+      sm.row[r] = rowf_z(a.hyi[k], a.hyti[k], a.hypi[k]);
+    }
+    __syncthreads();
+  }
+  const int c = cb * kZThreads + threadIdx.x;  // interior column
+  if (halo && cb == 0 && threadIdx.x < 4) {
     const int hcol[4] = {0, 1, a.nx + kHs, a.nx + kHs + 1};
     write_z_halo_column(a, hcol[threadIdx.x]);
   }
-  if (c >= a.nx) return;
-  const int col = c + kHs;
-  if ((a.flags & MW_FLAG_WRITE_HALO) && blockIdx.y == 0) write_z_halo_column(a, col);
-  const int z0 = blockIdx.y * kZTile;
-  const int z1 = min(z0 + kZTile, a.nz);
-  T w[4][4];
+  if (c < a.nx) {
+    const int col = c + kHs;
+    if (halo) write_z_halo_column(a, col);
+    T w[4][4];
 #pragma unroll
-  for (int j = 0; j < 4; ++j)
+    for (int j = 0; j < 4; ++j)
 #pragma unroll
-    for (int q = 0; q < 4; ++q) w[q][j] = zval(a, q, z0 - 2 + j, col);
-
-  auto flux_at = [&](int k, T F[4]) {
-    const bool wall = (k == 0) || (k == a.nz);
-    if constexpr (MODE == MODE_NATIVE64) {
-      flux_z_native(w, a.hyi[k], a.hyti[k], a.hypi[k], a.hv, wall, F);
-    } else {
-      RowF r;
-      r.hy_r = split::d2f(a.hyi[k]);
-      r.hy_rt = split::d2f(a.hyti[k]);
-      r.inv_hy_rt = 1.0f / r.hy_rt;
-      r.P = split::d2f(a.hypi[k]);
-      flux_z_f32(w, r, float(a.hv), wall, F);
+      for (int q = 0; q < 4; ++q) w[q][j] = zval(a, q, z0 - 2 + j, col);
+    auto flux_at = [&](int k, T F[4]) {
+      const bool wall = (k == 0) || (k == a.nz);
+      if constexpr (MODE == MODE_NATIVE64) {
+        flux_z_native(w, a.hyi[k], a.hyti[k], a.hypi[k], a.hv, wall, F);
+      } else {
+        flux_z_f32(w, sm.row[k - z0], float(a.hv), wall, F);
+      }
+    };
+    T nxt[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) nxt[q] = zval(a, q, z0 + 2, col);
+    T Fp[4];
+    flux_at(z0, Fp);
+    for (int k = z0; k < z1; ++k) {
+      const long long o = (long long)(k + kHs) * a.pitch + col;
+      T iv[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
+      const T rho_k = w[DENS][2];  // forcing rho' at cell k (interpolate.py:248-250)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        w[q][0] = w[q][1];
+        w[q][1] = w[q][2];
+        w[q][2] = w[q][3];
+        w[q][3] = nxt[q];
+      }
+      if (k + 1 < z1) {  // load the row needed by the next iteration now
+#pragma unroll
+        for (int q = 0; q < 4; ++q) nxt[q] = zval(a, q, k + 3, col);
+      }
+      T Fn[4];
+      flux_at(k + 1, Fn);
+      if constexpr (MODE == MODE_NATIVE64) {
+        double tend[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) tend[q] = -(Fn[q] - Fp[q]) / a.dz;
+        tend[WMOM] = tend[WMOM] - rho_k * kGrav;
+        if (a.srcw) tend[WMOM] = tend[WMOM] + a.srcw[(long long)k * a.nx + c];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = iv[q] + a.dt_stage * tend[q];
+      } else {
+        const float cz = float(a.dt_stage / a.dz), dt = float(a.dt_stage);
+        float inc[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) inc[q] = (Fp[q] - Fn[q]) * cz;
+        inc[WMOM] -= dt * (rho_k * float(kGrav));
+        if (a.srcw) inc[WMOM] += dt * split::d2f(a.srcw[(long long)k * a.nx + c]);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = iv[q] + inc[q];
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) Fp[q] = Fn[q];
     }
-  };
-  T nxt[4];
-#pragma unroll
-  for (int q = 0; q < 4; ++q) nxt[q] = zval(a, q, z0 + 2, col);
-  T Fp[4];
-  flux_at(z0, Fp);
-  for (int k = z0; k < z1; ++k) {
-    const long long o = (long long)(k + kHs) * a.pitch + col;
-    T iv[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
-    const T rho_k = w[DENS][2];  // forcing rho' at cell k (interpolate.py:248-250)
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      w[q][0] = w[q][1];
-      w[q][1] = w[q][2];
-      w[q][2] = w[q][3];
-      w[q][3] = nxt[q];
-    }
-    if (k + 1 < z1) {  // load the row needed by the next iteration now
-#pragma unroll
-      for (int q = 0; q < 4; ++q) nxt[q] = zval(a, q, k + 3, col);
-    }
-    T Fn[4];
-    flux_at(k + 1, Fn);
-    if constexpr (MODE == MODE_NATIVE64) {
-      double tend[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) tend[q] = -(Fn[q] - Fp[q]) / a.dz;
-      tend[WMOM] = tend[WMOM] - rho_k * kGrav;
-      if (a.srcw) tend[WMOM] = tend[WMOM] + a.srcw[(long long)k * a.nx + c];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = iv[q] + a.dt_stage * tend[q];
-    } else {
-      const float cz = float(a.dt_stage / a.dz), dt = float(a.dt_stage);
-      float inc[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) inc[q] = (Fp[q] - Fn[q]) * cz;
-      inc[WMOM] -= dt * (rho_k * float(kGrav));
-      if (a.srcw) inc[WMOM] += dt * split::d2f(a.srcw[(long long)k * a.nx + c]);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = iv[q] + inc[q];
-    }
-#pragma unroll
-    for (int q = 0; q < 4; ++q) Fp[q] = Fn[q];
   }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Single grid: x CTA (blockIdx.x, row) walks a run of chunks; z CTA is one tile.
+template <typename T, int MODE>
+__global__ void __launch_bounds__(kXThreads) k_stage_x(StageArgs<T> a) {
+  __shared__ SmemXT<T> sm;
+  const int nchunks = (a.nx + kXCells - 1) / kXCells;
+  const int cbeg = blockIdx.x * a.chunks_per_block;
+  const int cend = min(cbeg + a.chunks_per_block, nchunks);
+  const bool halo = (a.flags & MW_FLAG_WRITE_HALO) && blockIdx.x == 0;
+  for (int k = blockIdx.y; k < a.nz; k += gridDim.y) x_rowrun_t<T, MODE>(a, k, cbeg, cend, halo, sm);
+}
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(kZThreads) k_stage_z(StageArgs<T> a) {
+  __shared__ SmemZT sm;
+  z_tile_t<T, MODE>(a, blockIdx.x, blockIdx.y * kZTile, kZTile, (a.flags & MW_FLAG_WRITE_HALO) && blockIdx.y == 0,
+                    sm);
+}
+
+// ---------------------------------------------------------------------------
+// Ensemble (FP32 storage): one persistent launch per stage over all members.
+__device__ StageArgs<float> member_args_f32(const EnsStageT<float>& es, int e) {
+  const mw_ens_member m = es.members[e];
+  StageArgs<float> a;
+  a.nx = m.nx;
+  a.nz = m.nz;
+  a.pitch = m.nx + 2 * kHs;
+  a.plane = (long long)(m.nz + 2 * kHs) * a.pitch;
+  a.dx = m.dx;
+  a.dz = m.dz;
+  a.hv = -kHvBeta * (es.direction == MW_DIR_X ? m.dx : m.dz) / (16 * m.dt);
+  a.dt_stage = m.dt / (double)es.stage_div;
+  a.hyc = es.hyc + m.cell_off;
+  a.hytc = es.hytc + m.cell_off;
+  a.hyi = es.hyi + m.int_off;
+  a.hyti = es.hyti + m.int_off;
+  a.hypi = es.hypi + m.int_off;
+  a.srcw = nullptr;
+  a.init = es.init + m.state_off;
+  a.forcing = es.forcing + m.state_off;
+  a.out = es.out + m.state_off;
+  a.flags = es.flags;
+  a.chunks_per_block = 0;
+  return a;
+}
+
+__global__ void __launch_bounds__(kXThreads) k_ens_x_f32(EnsStageT<float> es) {
+  __shared__ SmemXT<float> sm;
+  for (int it = blockIdx.x; it < es.n_items; it += gridDim.x) {
+    const int2 item = es.items[it];
+    const StageArgs<float> a = member_args_f32(es, item.x);
+    x_rowrun_t<float, MODE_F32>(a, item.y, 0, (a.nx + kXCells - 1) / kXCells, a.flags & MW_FLAG_WRITE_HALO, sm);
+  }
+}
+
+__global__ void __launch_bounds__(kZThreads) k_ens_z_f32(EnsStageT<float> es) {
+  __shared__ SmemZT sm;
+  for (int it = blockIdx.x; it < es.n_items; it += gridDim.x) {
+    const int2 item = es.items[it];
+    const StageArgs<float> a = member_args_f32(es, item.x);
+    const int ncb = (a.nx + kZThreads - 1) / kZThreads;
+    const int cb = item.y % ncb, tile = item.y / ncb;
+    z_tile_t<float, MODE_F32>(a, cb, tile * es.z_tile, es.z_tile, (a.flags & MW_FLAG_WRITE_HALO) && tile == 0, sm);
+  }
+}
+
+int launch_ens_f32(const EnsStageT<float>& es, int grid) {
+  if (es.n_items == 0) return MW_OK;
+  if (es.direction == MW_DIR_X)
+    k_ens_x_f32<<<grid, kXThreads, 0, es.stream>>>(es);
+  else
+    k_ens_z_f32<<<grid, kZThreads, 0, es.stream>>>(es);
+  return check_launch("ensemble FP32 stage launch");
+}
+
+int ens_f32_occupancy(int direction, int* blocks_per_sm) {
+  cudaError_t e = direction == MW_DIR_X
+                      ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_ens_x_f32, kXThreads, 0)
+                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_ens_z_f32, kZThreads, 0);
+  if (e != cudaSuccess) return fail(MW_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
+  return MW_OK;
 }
 
 // ---------------------------------------------------------------------------

@@ -1,0 +1,41 @@
+// mw_ensemble.cuh -- shared types of the ensemble path: one persistent launch
+// per direction-stage advances every member of an ensemble of uneven grids.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "../../include/miniweather_gb300.h"
+
+namespace mw {
+
+// Arguments of one ensemble direction-stage launch (T = state storage type).
+template <typename T>
+struct EnsStageT {
+  const mw_ens_member* members;  // device
+  const int2* items;             // device work list of this direction
+  int n_items;
+  int z_tile;      // rows per z item
+  int direction;   // MW_DIR_X / MW_DIR_Z
+  int stage_div;   // the stage uses dt / stage_div (3, 2, 1)
+  unsigned flags;
+  const double* hyc;
+  const double* hytc;
+  const double* hyi;
+  const double* hyti;
+  const double* hypi;
+  const T* init;
+  T* forcing;
+  T* out;
+  cudaStream_t stream;
+};
+using EnsStage = EnsStageT<double>;
+
+// Launchers (defined next to the kernels they launch).
+int launch_ens_split(const EnsStage& es, int grid);
+int ens_split_occupancy(int direction, int* blocks_per_sm);
+int launch_ens_f32(const EnsStageT<float>& es, int grid);
+int ens_f32_occupancy(int direction, int* blocks_per_sm);
+
+constexpr int kEnsZTileMax = 64;
+
+}  // namespace mw

@@ -168,5 +168,12 @@ inline dwc split_host(double v) {
 }
 __device__ __forceinline__ dw ld(const dwc& c) { return {c.h, c.l}; }
 
+// Device-side split of a per-launch constant, rounded exactly as split_host
+// rounds it (two FP64->FP32 conversions; used once per work item, not per cell).
+__device__ __forceinline__ dwc split_rn(double v) {
+  const float h = __double2float_rn(v);
+  return {h, __double2float_rn(v - (double)h)};
+}
+
 }  // namespace split
 }  // namespace mw

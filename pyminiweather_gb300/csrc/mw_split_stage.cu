@@ -21,6 +21,7 @@
 // result scaled by |delta|^(k-1)).  For |delta| <= 1/8, degree 16 with terms
 // 7..16 in FP32; beyond that, expm1(gamma log1p(delta)) in FP64.
 #include "mw_common.cuh"
+#include "mw_ensemble.cuh"
 #include "mw_split.cuh"
 
 namespace mw {
@@ -55,6 +56,7 @@ constexpr int kXCells = kXThreads - 1;
 constexpr int kXTile = kXThreads + 3;  // cells x0-2 .. x0+256
 constexpr int kZThreads = 128;
 constexpr int kZTile = 64;
+constexpr int kZTileMax = 64;
 constexpr int kXBlocksPerRow = 2;  // x CTAs per row; each walks a run of chunks
 
 struct RowS {
@@ -203,24 +205,29 @@ __device__ __forceinline__ void write_z_halo_column(const SplitArgs& a, int col)
 __device__ __forceinline__ double update(double init, dw dF, double c12) { return fma(c12, to_f64(dF), init); }
 
 // ---------------------------------------------------------------------------
-// x: CTA (blockIdx.x, row) walks chunks [blockIdx.x * chunks_per_block, ...)
-// of 255 cells.  Per chunk: stage the 259 forcing values (split once) in
-// shared memory, thread t evaluates the flux at interface x0+t, thread t
-// updates cell x0+t.  The loads of the next chunk's forcing values and of this
-// chunk's init values are issued before the flux evaluation so their latency
-// is covered by it.  The row constants (an FP64 pow) are computed once per
-// CTA and row.
-__global__ void __launch_bounds__(kXThreads) k_stage_x_split(SplitArgs a) {
-  __shared__ dw sS[4][kXTile + 1];
-  __shared__ dw sF[4][kXThreads];
-  __shared__ RowS sRow;
+// Tiles.  Both the single-grid kernels and the persistent ensemble kernels
+// call these; every thread of the CTA must call them (they contain barriers).
+
+struct SmemX {
+  dw sS[4][kXTile + 1];
+  dw sF[4][kXThreads];
+  RowS row;
+};
+struct SmemZ {
+  RowS row[kZTileMax + 1];
+};
+
+// x: row k, chunks [cbeg, cend) of 255 cells.  Per chunk: stage the 259
+// forcing values (split once) in shared memory, thread t evaluates the flux at
+// interface x0+t, thread t updates cell x0+t.  The next chunk's forcing values
+// and this chunk's init values are loaded before the flux evaluation so their
+// latency is covered by it.  The row constants (an FP64 pow) are formed once
+// per call.  halo: write the periodic halo of this row of the forcing array.
+__device__ __forceinline__ void x_rowrun(const SplitArgs& a, int k, int cbeg, int cend, bool halo, SmemX& sm) {
   const int t = threadIdx.x;
-  const int nchunks = (a.nx + kXCells - 1) / kXCells;
-  const int cbeg = blockIdx.x * a.chunks_per_block;
-  const int cend = min(cbeg + a.chunks_per_block, nchunks);
   const dw hv12 = ld(a.hv12), d12 = ld(a.d12);
-  // this thread stages tile slots t and (t < 3) t + 256
-  auto load_stage = [&](long long row, int x0, double v0[4], double v1[4]) {
+  const long long row = (long long)(k + kHs) * a.pitch;
+  auto load_stage = [&](int x0, double v0[4], double v1[4]) {
     const int c0 = x0 - 2 + t, c1 = c0 + kXThreads;
     if (c0 <= a.nx + 1) {
       const long long col = wrap_x(c0, a.nx) + kHs;
@@ -233,128 +240,211 @@ __global__ void __launch_bounds__(kXThreads) k_stage_x_split(SplitArgs a) {
       for (int q = 0; q < 4; ++q) v1[q] = __ldg(a.forcing + q * a.plane + row + col);
     }
   };
-  for (int k = blockIdx.y; k < a.nz; k += gridDim.y) {
-    const long long row = (long long)(k + kHs) * a.pitch;
-    if (t == 0) {
-      const double hrt = a.hytc[k + kHs];
-      sRow = row_consts(a.hyc[k + kHs], hrt, kC0 * pow(hrt, kGamma));
-    }
-    if ((a.flags & MW_FLAG_WRITE_HALO) && blockIdx.x == 0 && t < 4) {
-      const int dst[4] = {0, 1, a.nx + kHs, a.nx + kHs + 1};
-      const int src[4] = {a.nx, a.nx + 1, kHs, kHs + 1};
+  if (t == 0) {
+    const double hrt = a.hytc[k + kHs];
+    sm.row = row_consts(a.hyc[k + kHs], hrt, kC0 * pow(hrt, kGamma));
+  }
+  if (halo && t < 4) {
+    const int dst[4] = {0, 1, a.nx + kHs, a.nx + kHs + 1};
+    const int src[4] = {a.nx, a.nx + 1, kHs, kHs + 1};
 #pragma unroll
-      for (int q = 0; q < 4; ++q) a.forcing[q * a.plane + row + dst[t]] = a.forcing[q * a.plane + row + src[t]];
-    }
-    double v0[4] = {0, 0, 0, 0}, v1[4] = {0, 0, 0, 0};
-    if (cbeg < cend) load_stage(row, cbeg * kXCells, v0, v1);
-    for (int chunk = cbeg; chunk < cend; ++chunk) {
-      const int x0 = chunk * kXCells;
-      const int i = x0 + t;
+    for (int q = 0; q < 4; ++q) a.forcing[q * a.plane + row + dst[t]] = a.forcing[q * a.plane + row + src[t]];
+  }
+  double v0[4] = {0, 0, 0, 0}, v1[4] = {0, 0, 0, 0};
+  if (cbeg < cend) load_stage(cbeg * kXCells, v0, v1);
+  for (int chunk = cbeg; chunk < cend; ++chunk) {
+    const int x0 = chunk * kXCells;
+    const int i = x0 + t;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) sS[q][t] = from_f64(v0[q]);
-      if (t < kXTile - kXThreads) {
+    for (int q = 0; q < 4; ++q) sm.sS[q][t] = from_f64(v0[q]);
+    if (t < kXTile - kXThreads) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q) sS[q][t + kXThreads] = from_f64(v1[q]);
-      }
-      __syncthreads();
-      const bool upd = t < kXCells && i < a.nx;
-      const long long o = row + i + kHs;
-      double iv[4];
-      if (upd) {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
-      }
-      if (chunk + 1 < cend) load_stage(row, x0 + kXCells, v0, v1);
-      if (i <= a.nx) {
-        dw s[4][4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-#pragma unroll
-          for (int j = 0; j < 4; ++j) s[q][j] = sS[q][t + j];
-        dw F[4];
-        flux_x_split(s, sRow, hv12, F);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) sF[q][t] = F[q];
-      }
-      __syncthreads();
-      if (upd) {
-        dw dF[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) dF[q] = sub(sF[q][t], sF[q][t + 1]);
-        if (a.srcw) dF[WMOM] = add(dF[WMOM], mul(from_f64(a.srcw[(long long)k * a.nx + i]), d12));
-#pragma unroll
-        for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = update(iv[q], dF[q], a.c12);
-      }
+      for (int q = 0; q < 4; ++q) sm.sS[q][t + kXThreads] = from_f64(v1[q]);
     }
     __syncthreads();
-  }
-}
-
-// z: one thread per column marching kZTile rows with a rolling window; the
-// next row is loaded one iteration ahead.
-__global__ void __launch_bounds__(kZThreads, 6) k_stage_z_split(SplitArgs a) {
-  __shared__ RowS sRow[kZTile + 1];
-  const int z0 = blockIdx.y * kZTile;
-  const int z1 = min(z0 + kZTile, a.nz);
-  for (int r = threadIdx.x; r <= z1 - z0; r += kZThreads) {
-    const int k = z0 + r;
-    sRow[r] = row_consts(a.hyi[k], a.hyti[k], a.hypi[k]);
+    const bool upd = t < kXCells && i < a.nx;
+    const long long o = row + i + kHs;
+    double iv[4];
+    if (upd) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
+    }
+    if (chunk + 1 < cend) load_stage(x0 + kXCells, v0, v1);
+    if (i <= a.nx) {
+      dw s[4][4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) s[q][j] = sm.sS[q][t + j];
+      dw F[4];
+      flux_x_split(s, sm.row, hv12, F);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) sm.sF[q][t] = F[q];
+    }
+    __syncthreads();
+    if (upd) {
+      dw dF[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) dF[q] = sub(sm.sF[q][t], sm.sF[q][t + 1]);
+      if (a.srcw) dF[WMOM] = add(dF[WMOM], mul(from_f64(a.srcw[(long long)k * a.nx + i]), d12));
+#pragma unroll
+      for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = update(iv[q], dF[q], a.c12);
+    }
   }
   __syncthreads();
-  const int c = blockIdx.x * kZThreads + threadIdx.x;
-  if ((a.flags & MW_FLAG_WRITE_HALO) && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x < 4) {
+}
+
+// z: columns [cb*128, cb*128+128), rows [z0, z0+zt): one thread per column
+// marching the rows with a rolling window; the next row and the init values
+// are loaded one step ahead.  halo: write the wall halo rows of these columns
+// of the forcing array (cb == 0 also does the four x-halo columns).
+__device__ __forceinline__ void z_tile(const SplitArgs& a, int cb, int z0, int zt, bool halo, SmemZ& sm) {
+  const int z1 = min(z0 + zt, a.nz);
+  for (int r = threadIdx.x; r <= z1 - z0; r += kZThreads) {
+    const int k = z0 + r;
+    sm.row[r] = row_consts(a.hyi[k], a.hyti[k], a.hypi[k]);
+  }
+  __syncthreads();
+  const int c = cb * kZThreads + threadIdx.x;
+  if (halo && cb == 0 && threadIdx.x < 4) {
     const int hcol[4] = {0, 1, a.nx + kHs, a.nx + kHs + 1};
     write_z_halo_column(a, hcol[threadIdx.x]);
   }
-  if (c >= a.nx) return;
-  const int col = c + kHs;
-  if ((a.flags & MW_FLAG_WRITE_HALO) && blockIdx.y == 0) write_z_halo_column(a, col);
-  const dw hv12 = ld(a.hv12), d12 = ld(a.d12), gz12 = ld(a.gz12);
-  dw w[4][4];
+  if (c < a.nx) {
+    const int col = c + kHs;
+    if (halo) write_z_halo_column(a, col);
+    const dw hv12 = ld(a.hv12), d12 = ld(a.d12), gz12 = ld(a.gz12);
+    dw w[4][4];
 #pragma unroll
-  for (int j = 0; j < 4; ++j)
+    for (int j = 0; j < 4; ++j)
 #pragma unroll
-    for (int q = 0; q < 4; ++q) w[q][j] = from_f64(zval64(a, q, z0 - 2 + j, col));
-  double nxt[4];
+      for (int q = 0; q < 4; ++q) w[q][j] = from_f64(zval64(a, q, z0 - 2 + j, col));
+    double nxt[4];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) nxt[q] = zval64(a, q, z0 + 2, col);
-  dw Fp[4];
-  flux_z_split(w, sRow[0], hv12, z0 == 0, Fp);
-  for (int k = z0; k < z1; ++k) {
-    const long long o = (long long)(k + kHs) * a.pitch + col;
-    double iv[4];
+    for (int q = 0; q < 4; ++q) nxt[q] = zval64(a, q, z0 + 2, col);
+    dw Fp[4];
+    flux_z_split(w, sm.row[0], hv12, z0 == 0, Fp);
+    for (int k = z0; k < z1; ++k) {
+      const long long o = (long long)(k + kHs) * a.pitch + col;
+      double iv[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
-    double cur[4];
+      for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
+      double cur[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) cur[q] = nxt[q];
-    if (k + 1 < z1) {
+      for (int q = 0; q < 4; ++q) cur[q] = nxt[q];
+      if (k + 1 < z1) {
 #pragma unroll
-      for (int q = 0; q < 4; ++q) nxt[q] = zval64(a, q, k + 3, col);
+        for (int q = 0; q < 4; ++q) nxt[q] = zval64(a, q, k + 3, col);
+      }
+      const dw rho_k = w[DENS][2];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        w[q][0] = w[q][1];
+        w[q][1] = w[q][2];
+        w[q][2] = w[q][3];
+        w[q][3] = from_f64(cur[q]);
+      }
+      dw Fn[4];
+      flux_z_split(w, sm.row[k + 1 - z0], hv12, k + 1 == a.nz, Fn);
+      dw dF[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) dF[q] = sub(Fp[q], Fn[q]);
+      dF[WMOM] = sub(dF[WMOM], mul(rho_k, gz12));
+      if (a.srcw) dF[WMOM] = add(dF[WMOM], mul(from_f64(a.srcw[(long long)k * a.nx + c]), d12));
+#pragma unroll
+      for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = update(iv[q], dF[q], a.c12);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) Fp[q] = Fn[q];
     }
-    const dw rho_k = w[DENS][2];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      w[q][0] = w[q][1];
-      w[q][1] = w[q][2];
-      w[q][2] = w[q][3];
-      w[q][3] = from_f64(cur[q]);
-    }
-    dw Fn[4];
-    flux_z_split(w, sRow[k + 1 - z0], hv12, k + 1 == a.nz, Fn);
-    dw dF[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) dF[q] = sub(Fp[q], Fn[q]);
-    dF[WMOM] = sub(dF[WMOM], mul(rho_k, gz12));
-    if (a.srcw) dF[WMOM] = add(dF[WMOM], mul(from_f64(a.srcw[(long long)k * a.nx + c]), d12));
-#pragma unroll
-    for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = update(iv[q], dF[q], a.c12);
-#pragma unroll
-    for (int q = 0; q < 4; ++q) Fp[q] = Fn[q];
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Single grid: x CTA (blockIdx.x, row) walks a run of chunks; z CTA is one tile.
+__global__ void __launch_bounds__(kXThreads) k_stage_x_split(SplitArgs a) {
+  __shared__ SmemX sm;
+  const int nchunks = (a.nx + kXCells - 1) / kXCells;
+  const int cbeg = blockIdx.x * a.chunks_per_block;
+  const int cend = min(cbeg + a.chunks_per_block, nchunks);
+  const bool halo = (a.flags & MW_FLAG_WRITE_HALO) && blockIdx.x == 0;
+  for (int k = blockIdx.y; k < a.nz; k += gridDim.y) x_rowrun(a, k, cbeg, cend, halo, sm);
+}
+
+__global__ void __launch_bounds__(kZThreads, 6) k_stage_z_split(SplitArgs a) {
+  __shared__ SmemZ sm;
+  z_tile(a, blockIdx.x, blockIdx.y * kZTile, kZTile, (a.flags & MW_FLAG_WRITE_HALO) && blockIdx.y == 0, sm);
+}
+
+// ---------------------------------------------------------------------------
+// Ensemble: one persistent launch per stage walks a work list over all
+// members (x: one item per member row; z: one item per member column-tile).
+__device__ SplitArgs member_args(const EnsStage& es, int e) {
+  const mw_ens_member m = es.members[e];
+  SplitArgs a;
+  a.nx = m.nx;
+  a.nz = m.nz;
+  a.pitch = m.nx + 2 * kHs;
+  a.plane = (long long)(m.nz + 2 * kHs) * a.pitch;
+  a.hyc = es.hyc + m.cell_off;
+  a.hytc = es.hytc + m.cell_off;
+  a.hyi = es.hyi + m.int_off;
+  a.hyti = es.hyti + m.int_off;
+  a.hypi = es.hypi + m.int_off;
+  a.srcw = nullptr;
+  a.init = es.init + m.state_off;
+  a.forcing = es.forcing + m.state_off;
+  a.out = es.out + m.state_off;
+  a.flags = es.flags;
+  a.chunks_per_block = 0;
+  const double d = es.direction == MW_DIR_X ? m.dx : m.dz;
+  const double dts = m.dt / (double)es.stage_div;  // dt/3, dt/2, dt/1 as evolve forms them
+  const double hv = -kHvBeta * d / (16 * m.dt);
+  a.hv12 = split_rn(12.0 * hv);
+  a.c12 = dts / (12.0 * d);
+  a.d12 = split_rn(12.0 * d);
+  a.gz12 = split_rn(12.0 * m.dz * kGrav);
+  return a;
+}
+
+__global__ void __launch_bounds__(kXThreads) k_ens_x_split(EnsStage es) {
+  __shared__ SmemX sm;
+  for (int it = blockIdx.x; it < es.n_items; it += gridDim.x) {
+    const int2 item = es.items[it];  // (member, row)
+    const SplitArgs a = member_args(es, item.x);
+    x_rowrun(a, item.y, 0, (a.nx + kXCells - 1) / kXCells, a.flags & MW_FLAG_WRITE_HALO, sm);
+  }
+}
+
+__global__ void __launch_bounds__(kZThreads, 6) k_ens_z_split(EnsStage es) {
+  __shared__ SmemZ sm;
+  for (int it = blockIdx.x; it < es.n_items; it += gridDim.x) {
+    const int2 item = es.items[it];  // (member, column block + ncb * tile)
+    const SplitArgs a = member_args(es, item.x);
+    const int ncb = (a.nx + kZThreads - 1) / kZThreads;
+    const int cb = item.y % ncb, tile = item.y / ncb;
+    z_tile(a, cb, tile * es.z_tile, es.z_tile, (a.flags & MW_FLAG_WRITE_HALO) && tile == 0, sm);
   }
 }
 
 }  // namespace
+
+int launch_ens_split(const EnsStage& es, int grid) {
+  if (es.n_items == 0) return MW_OK;
+  if (es.direction == MW_DIR_X)
+    k_ens_x_split<<<grid, kXThreads, 0, es.stream>>>(es);
+  else
+    k_ens_z_split<<<grid, kZThreads, 0, es.stream>>>(es);
+  return check_launch("ensemble split stage launch");
+}
+
+int ens_split_occupancy(int direction, int* blocks_per_sm) {
+  cudaError_t e = direction == MW_DIR_X
+                      ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_ens_x_split, kXThreads, 0)
+                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_ens_z_split, kZThreads, 0);
+  if (e != cudaSuccess) return fail(MW_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
+  return MW_OK;
+}
 
 int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
                        const double* hyi, const double* hyti, const double* hypi, const double* srcw,

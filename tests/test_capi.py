@@ -5,6 +5,8 @@ import ctypes
 import os
 import re
 
+import numpy as np
+
 import pytest
 import torch
 
@@ -125,3 +127,35 @@ def test_ic_table_matches_oracle_table():
         assert (s.background, s.u0, [tuple(b) for b in s.bubbles]) == (bg, u0, [tuple(b) for b in bub])
     with pytest.raises(NotImplementedError):
         ic_spec("injection", 2e4)
+
+
+def test_ensemble_plan_validation():
+    """Ensemble plans are built and checked on the host."""
+    L = _native.load()
+    M = _native.EnsMember
+    info = _native.EnsPlanInfo()
+    mem = (M * 2)(M(64, 32, 312.5, 312.5, 0.1, 0, 0, 0), M(100, 50, 200.0, 200.0, 0.1, 4 * 68 * 36, 36, 33))
+    assert L.mw_ensemble_plan_info(2, mem, 16, ctypes.byref(info)) == OK
+    assert info.n_x_items == 32 + 50
+    assert info.n_z_items == 1 * 2 + 1 * 4
+    assert info.bytes % 16 == 0 and info.z_items_off >= info.x_items_off + 8 * info.n_x_items
+    bad = (M * 2)(M(64, 32, 312.5, 312.5, 0.1, 0, 0, 0), M(100, 50, 200.0, 200.0, 0.1, 100, 36, 33))
+    assert L.mw_ensemble_plan_info(2, bad, 16, ctypes.byref(info)) == ALIAS
+    assert L.mw_ensemble_plan_info(2, mem, 65, ctypes.byref(info)) == INVALID
+    one = (M * 1)(M(1, 32, 1.0, 1.0, 0.1, 0, 0, 0))
+    assert L.mw_ensemble_plan_info(1, one, 16, ctypes.byref(info)) == SHAPE
+
+
+def test_thermal_ensemble_generator():
+    from pyminiweather_gb300.ensemble import thermal_ensemble
+    a, b = thermal_ensemble(256, seed=0), thermal_ensemble(256, seed=0)
+    assert [m[0]["nx"] for m in a] == [m[0]["nx"] for m in b]
+    nx = [m[0]["nx"] for m in a]
+    assert min(nx) >= 64 and max(nx) <= 1024 and all(n % 2 == 0 for n in nx)
+    assert all(m[0]["nz"] * 2 == m[0]["nx"] for m in a)
+    amps = [m[1][0][0] for m in a]
+    assert 1.0 <= min(amps) and max(amps) <= 5.0
+    # log-uniform: about half the members below the geometric mean 256
+    assert 0.35 < np.mean(np.array(nx) < 256) < 0.65
+    cells = sum(m[0]["nx"] * m[0]["nz"] for m in a)
+    assert 15e6 < cells < 35e6

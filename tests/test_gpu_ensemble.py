@@ -1,0 +1,118 @@
+"""Ensembles of uneven grids (the batching form): every member must evolve
+exactly as a single-grid run with the same parameters, through one persistent
+launch per direction-stage, eagerly or replayed from a CUDA graph."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from pyminiweather_gb300.data import initialize_fields
+from pyminiweather_gb300.ensemble import Ensemble, member_params, thermal_ensemble
+from pyminiweather_gb300.ics import init
+from pyminiweather_gb300.solve import evolve, reset_direction
+from tests.helpers import TOL_STEP, normwise, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def small_members(seed=1):
+    rng = np.random.default_rng(seed)
+    out = []
+    for nx, nz in ((64, 32), (100, 50), (130, 66), (256, 128), (37, 13), (300, 150)):
+        p = member_params(nx, nz)
+        out.append((p, [(rng.uniform(1, 5), rng.uniform(0.3, 0.7) * 2e4, rng.uniform(1500, 3000), 2000.0, 2000.0)]))
+    return out
+
+
+def single_run(p, bubbles, steps, dtype=torch.float64):
+    q = dict(p, f64_mode="split")
+    f = initialize_fields(q, dtype=dtype)
+    init(f, q, None, bubbles=bubbles)
+    reset_direction()
+    evolve(q, f, None, dt=q["dt"], nsteps=steps)
+    return f.state.to(torch.float64).cpu().numpy()
+
+
+# FP64 members run the same arithmetic as a single-grid run (rounding-level
+# agreement); FP32 members agree to FP32 rounding (the ensemble kernels inline
+# the same tile code with different constants folded, so FMA contraction may
+# differ).
+MEMBER_TOL = {torch.float64: 1e-12, torch.float32: 1e-5}
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_members_match_single_grid_runs(dtype):
+    mem = small_members()
+    ens = Ensemble(mem, dtype=dtype)
+    ens.step(10)
+    for e, (p, bub) in enumerate(mem):
+        got = ens.member_state(e).to(torch.float64).cpu().numpy()
+        ref = single_run(p, bub, 10, dtype)
+        err = max(normwise(got, ref, interior=False))
+        print("member %d %dx%d: max normwise vs single grid %.2e identical %s" % (
+            e, p["nx"], p["nz"], err, np.array_equal(got, ref)))
+        assert err <= MEMBER_TOL[dtype]
+
+
+def test_members_vs_oracle():
+    mem = small_members(seed=2)[:3]
+    ens = Ensemble(mem)
+    ens.step(100)
+    for e, (p, bub) in enumerate(mem):
+        o = O.OracleSim(O.make_params(p["nx"], p["nz"], "thermal"), bubbles=bub)
+        o.evolve(100)
+        err = normwise(ens.member_state(e).cpu().numpy(), o.state)
+        print("member %d vs oracle after 100 steps: %s" % (e, ["%.2e" % v for v in err]))
+        assert max(err) <= TOL_STEP
+
+
+def test_graph_replay_equals_eager_steps():
+    mem = small_members(seed=3)
+    a, b = Ensemble(mem), Ensemble(mem)
+    replay = a.graph()
+    for _ in range(3):
+        replay()
+    b.grid_x, b.grid_z = a.grid_x, a.grid_z
+    b.step(6)
+    torch.cuda.synchronize()
+    assert torch.equal(a.state, b.state) and torch.equal(a.state_tmp, b.state_tmp)
+    assert a.reverse == b.reverse == 0
+
+
+def test_autotune_does_not_change_results():
+    mem = small_members(seed=4)
+    a, b = Ensemble(mem), Ensemble(mem)
+    tuned = a.autotune(steps=1)
+    assert tuned["z_tile"] in (16, 32, 64) and tuned["grid_x"] > 0 and tuned["grid_z"] > 0
+    a.step(4)
+    b.step(4)
+    assert torch.equal(a.state, b.state)
+
+
+def test_uneven_thermal_ensemble_256():
+    """The batching configuration: 256 thermal members, nx log-uniform in
+    [64, 1024], 100 steps, FP64 and FP32; three members are re-run alone."""
+    mem = thermal_ensemble(256, seed=0)
+    e64 = Ensemble(mem, dtype=torch.float64)
+    e32 = Ensemble(mem, dtype=torch.float32)
+    m0 = [e64.member_stats(e)[0] for e in range(len(mem))]
+    for ens in (e64, e32):
+        ens.autotune(steps=1)
+        replay = ens.graph()
+        for _ in range(50):
+            replay()
+    torch.cuda.synchronize()
+    drift = max(abs(e64.member_stats(e)[0] - m0[e]) / m0[e] for e in range(len(mem)))
+    assert drift <= 1e-13
+    worst32 = 0.0
+    for e in range(len(mem)):
+        a = e32.member_state(e).to(torch.float64).cpu().numpy()
+        b = e64.member_state(e).cpu().numpy()
+        worst32 = max(worst32, max(rel_l2(a, b)[v] for v in (0, 3)))
+    print("256 members, %d cells: FP32 vs FP64 worst rel-L2 (dens, rhot) %.2e, FP64 mass drift %.1e" % (
+        e64.cells(), worst32, drift))
+    assert worst32 <= 1e-4
+    for e in (0, 100, 255):
+        p, bub = mem[e]
+        ref = single_run(p, bub, 100)
+        assert max(normwise(e64.member_state(e).cpu().numpy(), ref)) <= MEMBER_TOL[torch.float64]
