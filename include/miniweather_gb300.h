@@ -179,6 +179,25 @@ int mw_ensemble_step_f32(const void* plan_device, const mw_ens_plan_info* info, 
                          int* reverse, unsigned flags, int grid_x, int grid_z, void* stream);
 
 /* ---------------------------------------------------------------------------
+ * Adjoint of one direction-stage (no counterpart in the reference, which has
+ * no derivatives): for out = init + dt_stage * L(forcing) as mw_dirstage_f64
+ * computes it, given g_out = dJ/d(out) on the interior cells,
+ *   g_dst = g_base_a + g_base_b + (add_g_out ? g_out : 0)
+ *           + dt_stage * (dL/d forcing)^T g_out
+ * on the interior, 0 on the halo.  The transposed map includes the halo rules
+ * (a halo value's adjoint returns to the cell it was copied or scaled from),
+ * the hyperviscosity and the gravity term.  Arrays are (4, nz+4, nx+4) FP64;
+ * a base may be g_dst itself (accumulation); g_dst must not overlap g_out or
+ * forcing.  FP64 arithmetic.  workspace: mw_dirstage_vjp_workspace_bytes.
+ * ------------------------------------------------------------------------- */
+size_t mw_dirstage_vjp_workspace_bytes(int nx, int nz);
+int mw_dirstage_vjp_f64(int nx, int nz, double dx, double dz, double dt_full, const double* hy_dens_cell,
+                        const double* hy_dens_theta_cell, const double* hy_dens_int, const double* hy_dens_theta_int,
+                        const double* hy_pressure_int, const double* forcing, const double* g_out,
+                        const double* g_base_a, const double* g_base_b, int add_g_out, double* g_dst, double dt_stage,
+                        int direction, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---------------------------------------------------------------------------
  * Initial condition: replaces init (pyminiweather/ics/initial.py:11-105):
  * 3x3 Gauss-Legendre cell averages over all (nz+4)(nx+4) cells of the bubbles
  * (sample_ellipse_cosine, utils/utils.py:5-51), plus the hydrostatic

@@ -1,0 +1,276 @@
+// mw_adjoint.cu -- adjoint (vector-Jacobian product) of one direction-stage.
+//
+// Forward (pyminiweather/solve/step.py:21-82, interpolate.py:82-250):
+//   out = init + dt * L(forcing),  L = -(F(i+1) - F(i)) / d  [- rho' g on w in z],
+//   F(i) = f(A(i), D(i)),  A = sum_j c_j s(i-2+j),  D = sum_j e_j s(i-2+j),
+//   c = (-1, 7, 7, -1)/12, e = (-1, 3, -3, 1), s read through the halo rules
+//   (periodic in x, ics/bcs.py:35-39; wall in z, bcs.py:92-148).
+// Adjoint, given g = dJ/d(out) on the interior cells:
+//   dJ/d(init)    += g
+//   dJ/d(forcing) += dt * (dL/d forcing)^T g:
+//     Fbar(i) = (dt/d) (g(i) - g(i-1))      (g = 0 outside the interior)
+//     (Abar, Dbar)(i) = (df/dA, df/dD)^T Fbar(i)
+//     sbar(t) += c_j Abar(i) + e_j Dbar(i)  for the taps t = i-2+j, mapped
+//     back through the halo rules (a halo value's adjoint goes to the cell it
+//     was copied or scaled from), and sbar_rho(k) -= dt g_w(k) grav in z.
+// The flux Jacobian uses rho theta = A3 + (rho theta)_bg and p = C0 (rho theta)^gamma,
+// so dp/dA3 = gamma p / (rho theta); at the z walls w and d3[DENS] are held at
+// zero (interpolate.py:167-173), so those paths carry no adjoint.
+//
+// Two kernels per call: one thread per interface writes (Abar, Dbar) to a
+// caller-provided workspace; one thread per cell gathers its taps.
+#include "mw_common.cuh"
+
+namespace mw {
+namespace {
+
+struct VjpArgs {
+  int nx, nz, pitch;
+  long long plane;
+  double d;         // dx or dz
+  double hv;        // -hv_beta d / (16 dt_full)
+  double dt_stage;
+  const double *hyc, *hytc, *hyi, *hyti, *hypi;
+  const double* forcing;
+  const double* gout;
+  const double* base_a;
+  const double* base_b;
+  int add_gout;
+  double* gdst;
+  double* ws;       // 8 x n_interfaces: Abar[4], Dbar[4]
+  long long nif;    // interfaces per variable plane of ws
+};
+
+__device__ __forceinline__ int wrap_x(int j, int nx) { return j < 0 ? j + nx : (j >= nx ? j - nx : j); }
+
+__device__ __forceinline__ double zval(const VjpArgs& a, int q, int k, int col) {
+  if (k >= 0 && k < a.nz) return a.forcing[q * a.plane + (long long)(k + kHs) * a.pitch + col];
+  if (q == WMOM) return 0.0;
+  const int src = k < 0 ? kHs : a.nz + kHs - 1;
+  const double s = a.forcing[q * a.plane + (long long)src * a.pitch + col];
+  if (q == UMOM) return s / a.hyc[src] * a.hyc[k + kHs];
+  return s;
+}
+
+__device__ __forceinline__ double gval(const VjpArgs& a, int q, int k, int i) {
+  return a.gout[q * a.plane + (long long)(k + kHs) * a.pitch + i + kHs];
+}
+
+// tap weights of the interpolation (data/fields.py:94-97, convolution order
+// reversed) and of the third difference
+__constant__ double kC[4] = {-1.0 / 12, 7.0 / 12, 7.0 / 12, -1.0 / 12};
+__constant__ double kE[4] = {-1.0, 3.0, -3.0, 1.0};
+
+// Interface adjoints.  x: interface (k, i), i in [0, nx]; z: (k, c), k in [0, nz].
+template <int DIR>
+__global__ void k_vjp_iface(VjpArgs a) {
+  const long long n = a.nif;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+       idx += (long long)gridDim.x * blockDim.x) {
+    double s[4][4];
+    double Fb[4];
+    bool wall = false;
+    double hy_r, hy_rt;
+    if (DIR == MW_DIR_X) {
+      const int k = (int)(idx / (a.nx + 1)), i = (int)(idx % (a.nx + 1));
+      const long long row = (long long)(k + kHs) * a.pitch;
+      for (int j = 0; j < 4; ++j) {
+        const long long col = wrap_x(i - 2 + j, a.nx) + kHs;
+        for (int q = 0; q < 4; ++q) s[q][j] = a.forcing[q * a.plane + row + col];
+      }
+      for (int q = 0; q < 4; ++q) {
+        const double gr = i < a.nx ? gval(a, q, k, i) : 0.0;
+        const double gl = i > 0 ? gval(a, q, k, i - 1) : 0.0;
+        Fb[q] = a.dt_stage / a.d * (gr - gl);
+      }
+      hy_r = a.hyc[k + kHs];
+      hy_rt = a.hytc[k + kHs];
+    } else {
+      const int k = (int)(idx / a.nx), c = (int)(idx % a.nx);
+      for (int j = 0; j < 4; ++j)
+        for (int q = 0; q < 4; ++q) s[q][j] = zval(a, q, k - 2 + j, c + kHs);
+      for (int q = 0; q < 4; ++q) {
+        const double gr = k < a.nz ? gval(a, q, k, c) : 0.0;
+        const double gl = k > 0 ? gval(a, q, k - 1, c) : 0.0;
+        Fb[q] = a.dt_stage / a.d * (gr - gl);
+      }
+      hy_r = a.hyi[k];
+      hy_rt = a.hyti[k];
+      wall = (k == 0) || (k == a.nz);
+    }
+    double A[4];
+    for (int q = 0; q < 4; ++q) A[q] = ((s[q][0] * kC[0] + s[q][1] * kC[1]) + s[q][2] * kC[2]) + s[q][3] * kC[3];
+    const double rho = A[DENS] + hy_r;
+    const double rt = A[RHOT] + hy_rt;
+    const double u = A[UMOM] / rho, w = A[WMOM] / rho, th = rt / rho;
+    const double dpdA3 = kGamma * kC0 * pow(rt, kGamma) / rt;
+    double Ab[4], Db[4];
+    for (int q = 0; q < 4; ++q) Db[q] = -a.hv * Fb[q];
+    if (DIR == MW_DIR_X) {
+      Ab[DENS] = -(Fb[1] * u * u + Fb[2] * u * w + Fb[3] * u * th);
+      Ab[UMOM] = Fb[0] + 2.0 * Fb[1] * u + Fb[2] * w + Fb[3] * th;
+      Ab[WMOM] = Fb[2] * u;
+      Ab[RHOT] = Fb[1] * dpdA3 + Fb[3] * u;
+    } else if (!wall) {
+      Ab[DENS] = -(Fb[1] * w * u + Fb[2] * w * w + Fb[3] * w * th);
+      Ab[UMOM] = Fb[1] * w;
+      Ab[WMOM] = Fb[0] + Fb[1] * u + 2.0 * Fb[2] * w + Fb[3] * th;
+      Ab[RHOT] = Fb[2] * dpdA3 + Fb[3] * w;
+    } else {
+      Ab[DENS] = 0.0;
+      Ab[UMOM] = 0.0;
+      Ab[WMOM] = 0.0;
+      Ab[RHOT] = Fb[2] * dpdA3;
+      Db[DENS] = 0.0;
+    }
+    for (int q = 0; q < 4; ++q) {
+      a.ws[q * n + idx] = Ab[q];
+      a.ws[(4 + q) * n + idx] = Db[q];
+    }
+  }
+}
+
+// Cell gather: gdst = base_a + base_b + add_gout * gout + sbar (interior); halo cells of gdst = 0.
+template <int DIR>
+__global__ void k_vjp_gather(VjpArgs a) {
+  const long long ncell = (long long)a.plane;
+  const long long n = a.nif;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < ncell;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int kk = (int)(idx / a.pitch), ii = (int)(idx % a.pitch);
+    const int k = kk - kHs, i = ii - kHs;
+    if (k < 0 || k >= a.nz || i < 0 || i >= a.nx) {
+      for (int q = 0; q < 4; ++q) a.gdst[q * a.plane + idx] = 0.0;
+      continue;
+    }
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    if (DIR == MW_DIR_X) {
+      for (int j = 0; j < 4; ++j)
+        for (int m = -1; m <= 1; ++m) {
+          const int f = i + 2 - j + m * a.nx;  // interface whose tap j is cell i
+          if (f < 0 || f > a.nx) continue;
+          const long long o = (long long)k * (a.nx + 1) + f;
+          for (int q = 0; q < 4; ++q) acc[q] += kC[j] * a.ws[q * n + o] + kE[j] * a.ws[(4 + q) * n + o];
+        }
+    } else {
+      // taps t = f - 2 + j of interface f in [0, nz]; t maps to row k directly,
+      // or through the wall rule from halo rows -2,-1 (-> 0) and nz, nz+1 (-> nz-1)
+      for (int f = k - 1; f <= k + 2; ++f) {  // interfaces with an interior tap at row k
+        if (f < 0 || f > a.nz) continue;
+        const int j = k - f + 2;
+        const long long o = (long long)f * a.nx + i;
+        for (int q = 0; q < 4; ++q) acc[q] += kC[j] * a.ws[q * n + o] + kE[j] * a.ws[(4 + q) * n + o];
+      }
+      auto halo_taps = [&](int t, double wq[4]) {  // weight of halo row t on row k
+        const int src = t < 0 ? 0 : a.nz - 1;
+        wq[DENS] = wq[RHOT] = (k == src) ? 1.0 : 0.0;
+        wq[WMOM] = 0.0;
+        wq[UMOM] = (k == src) ? a.hyc[t + kHs] / a.hyc[src + kHs] : 0.0;
+      };
+      const int halo_rows[4] = {-2, -1, a.nz, a.nz + 1};
+      for (int h = 0; h < 4; ++h) {
+        const int t = halo_rows[h];
+        double wq[4];
+        halo_taps(t, wq);
+        if (wq[DENS] == 0.0 && wq[UMOM] == 0.0) continue;
+        for (int j = 0; j < 4; ++j) {
+          const int f = t + 2 - j;
+          if (f < 0 || f > a.nz) continue;
+          const long long o = (long long)f * a.nx + i;
+          for (int q = 0; q < 4; ++q)
+            acc[q] += wq[q] * (kC[j] * a.ws[q * n + o] + kE[j] * a.ws[(4 + q) * n + o]);
+        }
+      }
+      acc[DENS] -= a.dt_stage * kGrav * gval(a, WMOM, k, i);
+    }
+    for (int q = 0; q < 4; ++q) {
+      const long long o = q * a.plane + idx;
+      double v = acc[q];
+      if (a.add_gout) v += a.gout[o];
+      if (a.base_a) v += a.base_a[o];
+      if (a.base_b) v += a.base_b[o];
+      a.gdst[o] = v;
+    }
+  }
+}
+
+inline unsigned grid_for(long long n, int threads) {
+  long long b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  if (b > 65535LL * 32) b = 65535LL * 32;
+  return (unsigned)b;
+}
+
+long long n_interfaces(int nx, int nz, int dir) {
+  return dir == MW_DIR_X ? (long long)nz * (nx + 1) : (long long)(nz + 1) * nx;
+}
+
+}  // namespace
+}  // namespace mw
+
+using namespace mw;
+
+extern "C" size_t mw_dirstage_vjp_workspace_bytes(int nx, int nz) {
+  if (nx < 1 || nz < 1) return 0;
+  const long long n = std::max(n_interfaces(nx, nz, MW_DIR_X), n_interfaces(nx, nz, MW_DIR_Z));
+  return sizeof(double) * 8 * (size_t)n;
+}
+
+extern "C" int mw_dirstage_vjp_f64(int nx, int nz, double dx, double dz, double dt_full, const double* hyc,
+                                   const double* hytc, const double* hyi, const double* hyti, const double* hypi,
+                                   const double* forcing, const double* g_out, const double* g_base_a,
+                                   const double* g_base_b, int add_g_out, double* g_dst, double dt_stage,
+                                   int direction, void* workspace, size_t workspace_bytes, void* stream) {
+  int st = check_grid(nx, nz);
+  if (st) return st;
+  MW_REQUIRE(finite_pos(dx) && finite_pos(dz) && finite_pos(dt_full), MW_ERR_INVALID_ARG,
+             "dx, dz, dt_full must be finite and positive");
+  MW_REQUIRE(std::isfinite(dt_stage), MW_ERR_INVALID_ARG, "dt_stage must be finite");
+  MW_REQUIRE(direction == MW_DIR_X || direction == MW_DIR_Z, MW_ERR_INVALID_ARG, "direction must be 0 or 1");
+  MW_REQUIRE(hyc && hytc && hyi && hyti && hypi && forcing && g_out && g_dst && workspace, MW_ERR_INVALID_ARG,
+             "NULL pointer argument");
+  MW_REQUIRE(aligned(forcing) && aligned(g_out) && aligned(g_dst) && ((uintptr_t)workspace % 8) == 0, MW_ERR_ALIGN,
+             "misaligned pointer");
+  const size_t bytes = sizeof(double) * 4 * (size_t)make_geom(nx, nz).plane;
+  MW_REQUIRE(!ranges_overlap(g_dst, bytes, g_out, bytes), MW_ERR_ALIAS, "g_dst must not overlap g_out");
+  MW_REQUIRE(!ranges_overlap(g_dst, bytes, forcing, bytes), MW_ERR_ALIAS, "g_dst must not overlap forcing");
+  MW_REQUIRE((!g_base_a || g_base_a == g_dst || !ranges_overlap(g_dst, bytes, g_base_a, bytes)) &&
+                 (!g_base_b || g_base_b == g_dst || !ranges_overlap(g_dst, bytes, g_base_b, bytes)),
+             MW_ERR_ALIAS, "a base array must equal g_dst or not overlap it");
+  const size_t need = mw_dirstage_vjp_workspace_bytes(nx, nz);
+  MW_REQUIRE(workspace_bytes >= need, MW_ERR_WORKSPACE, "vjp workspace needs %zu bytes, got %zu", need,
+             workspace_bytes);
+  const Geom g = make_geom(nx, nz);
+  VjpArgs a;
+  a.nx = nx;
+  a.nz = nz;
+  a.pitch = g.pitch;
+  a.plane = g.plane;
+  a.d = direction == MW_DIR_X ? dx : dz;
+  a.hv = -kHvBeta * a.d / (16 * dt_full);
+  a.dt_stage = dt_stage;
+  a.hyc = hyc;
+  a.hytc = hytc;
+  a.hyi = hyi;
+  a.hyti = hyti;
+  a.hypi = hypi;
+  a.forcing = forcing;
+  a.gout = g_out;
+  a.base_a = g_base_a;
+  a.base_b = g_base_b;
+  a.add_gout = add_g_out;
+  a.gdst = g_dst;
+  a.ws = (double*)workspace;
+  a.nif = n_interfaces(nx, nz, direction);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (direction == MW_DIR_X) {
+    k_vjp_iface<MW_DIR_X><<<grid_for(a.nif, 128), 128, 0, s>>>(a);
+    if ((st = check_launch("vjp interface launch"))) return st;
+    k_vjp_gather<MW_DIR_X><<<grid_for(g.plane, 256), 256, 0, s>>>(a);
+  } else {
+    k_vjp_iface<MW_DIR_Z><<<grid_for(a.nif, 128), 128, 0, s>>>(a);
+    if ((st = check_launch("vjp interface launch"))) return st;
+    k_vjp_gather<MW_DIR_Z><<<grid_for(g.plane, 256), 256, 0, s>>>(a);
+  }
+  return check_launch("vjp gather launch");
+}

@@ -1,0 +1,125 @@
+"""The hand-written adjoint (differentiation form), checked against autograd
+through the pure-PyTorch copy of the step and against central finite
+differences."""
+import time
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import torch_step as TS
+from pyminiweather_gb300 import _native
+from pyminiweather_gb300.adjoint import RolloutContext, rollout, upper_half_rhot_misfit
+from pyminiweather_gb300.data import initialize_fields
+from pyminiweather_gb300.ics import init
+from pyminiweather_gb300.solve import evolve, reset_direction
+from tests.helpers import make_params
+
+pytestmark = pytest.mark.gpu
+
+
+def _fields(nx, nz, ic="thermal", amp=None):
+    p = make_params(nx, nz, ic)
+    f = initialize_fields(p)
+    bub = None if amp is None else [(amp, p["xlen"] / 2, 2000.0, 2000.0, 2000.0)]
+    init(f, p, None, bubbles=bub)
+    return p, f
+
+
+def _bg(f):
+    return [a for a in f.backgrounds()]
+
+
+@pytest.mark.parametrize("direction", [0, 1])
+def test_stage_vjp_matches_autograd(direction):
+    """One direction-stage: g_forcing = dt (dL/dforcing)^T g_out, against
+    torch autograd of the pure-PyTorch tendency."""
+    torch.manual_seed(0)
+    p, f = _fields(40, 24, "collision")
+    evolve(dict(p, f64_mode="native"), f, None, dt=p["dt"], nsteps=3)  # a developed state
+    s = f.state.clone()
+    g = torch.zeros_like(s)
+    g[:, 2:-2, 2:-2] = torch.randn(4, 24, 40, dtype=torch.float64, device=s.device)
+    dts = p["dt"] / 2
+    out = torch.empty_like(s)
+    ws = torch.empty(int(_native.load().mw_dirstage_vjp_workspace_bytes(40, 24)) // 8 + 1, dtype=torch.float64,
+                     device=s.device)
+    hb = [_native.ptr(a) for a in f.backgrounds()]
+    _native.call("mw_dirstage_vjp_f64", 40, 24, p["dx"], p["dz"], p["dt"], *hb, _native.ptr(s), _native.ptr(g),
+                 None, None, 0, _native.ptr(out), dts, direction, _native.ptr(ws), ws.numel() * 8,
+                 _native.stream_handle())
+    x = s[:, 2:-2, 2:-2].clone().requires_grad_(True)
+    L = TS.tendency_x(x, _bg(f), p["dx"], p["dt"]) if direction == 0 else TS.tendency_z(x, _bg(f), p["dz"], p["dt"])
+    (ref,) = torch.autograd.grad((dts * L * g[:, 2:-2, 2:-2]).sum(), x)
+    got = out[:, 2:-2, 2:-2]
+    for v in range(4):
+        err = float((got[v] - ref[v]).abs().max() / ref[v].abs().max().clamp_min(1e-300))
+        assert err <= 1e-12, (direction, v, err)
+    assert float(out[:, :2].abs().max()) == 0.0  # halo of the adjoint is zero
+
+
+def test_rollout_gradient_matches_autograd():
+    """Gradient of the upper-half (rho theta)' misfit after 12 steps w.r.t. all
+    four initial fields: hand-written adjoint (checkpoints every 5 steps)
+    against autograd through the pure-PyTorch step."""
+    nx, nz, steps = 48, 24, 12
+    p, f = _fields(nx, nz, amp=3.0)
+    _, ft = _fields(nx, nz, amp=3.5)
+    reset_direction()
+    evolve(dict(p, f64_mode="native"), ft, None, dt=p["dt"], nsteps=steps)
+    target = ft.state.clone()
+    x0 = f.state.clone().requires_grad_(True)
+    ctx = RolloutContext(params=dict(p, f64_mode="native"), fields=f, nsteps=steps, ckpt_every=5)
+    loss = upper_half_rhot_misfit(rollout(x0, ctx), target, nz)
+    (g,) = torch.autograd.grad(loss, x0)
+    xi = f.state[:, 2:-2, 2:-2].clone().requires_grad_(True)
+    s, _ = TS.evolve_interior(xi, _bg(f), p, steps)
+    d = s[3, nz // 2:, :] - target[3, 2 + nz // 2:2 + nz, 2:-2]
+    (gr,) = torch.autograd.grad((d * d).sum(), xi)
+    assert abs(float(loss) - float((d * d).sum())) <= 1e-10 * abs(float(loss))
+    for v in range(4):
+        err = float((g[v, 2:-2, 2:-2] - gr[v]).abs().max() / gr[v].abs().max())
+        print("field %d: adjoint vs autograd normwise %.2e" % (v, err))
+        assert err <= 1e-9
+    assert float(g[:, :2].abs().max()) == 0.0 and float(g[:, :, -2:].abs().max()) == 0.0
+
+
+def test_adjoint_vs_finite_differences_512x256():
+    """The differentiation configuration: 512 x 256 thermal, 200 steps,
+    checkpoints every 20; target from amplitude 3.5 K; 16 seeded directions,
+    central differences with eps = 1e-6."""
+    nx, nz, steps = 512, 256, 200
+    p, f = _fields(nx, nz, amp=3.0)
+    p["f64_mode"] = "native"  # FD differences of the forward need its full FP64 rounding
+    _, ft = _fields(nx, nz, amp=3.5)
+    reset_direction()
+    evolve(p, ft, None, dt=p["dt"], nsteps=steps)
+    target = ft.state.clone()
+    ctx = RolloutContext(params=p, fields=f, nsteps=steps, ckpt_every=20)
+    x0 = f.state.clone().requires_grad_(True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    loss = upper_half_rhot_misfit(rollout(x0, ctx), target, nz)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    (g,) = torch.autograd.grad(loss, x0)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    print("512x256, 200 steps: forward %.3f s, adjoint %.3f s (ratio %.2f)" % (t1 - t0, t2 - t1, (t2 - t1) / (t1 - t0)))
+
+    def L(x):
+        with torch.no_grad():
+            return float(upper_half_rhot_misfit(rollout(x, ctx), target, nz))
+
+    gen = torch.Generator(device="cpu").manual_seed(1234)
+    eps = 1e-6
+    worst = 0.0
+    for k in range(16):
+        v = torch.zeros_like(x0)
+        v[:, 2:-2, 2:-2] = torch.randn(4, nz, nx, generator=gen, dtype=torch.float64).to(x0.device)
+        fd = (L(x0.detach() + eps * v) - L(x0.detach() - eps * v)) / (2 * eps)
+        ad = float((g * v).sum())
+        rel = abs(fd - ad) / abs(ad)
+        worst = max(worst, rel)
+        print("direction %2d: adjoint %.10e  central FD %.10e  rel %.2e" % (k, ad, fd, rel))
+    assert worst <= 1e-6
