@@ -293,6 +293,38 @@ def ensemble_run(torch, steps, warmup, dtype):
     return out
 
 
+def adjoint_run(torch, mode):
+    """The differentiation form: 512 x 256 thermal, 200 steps, checkpoints every
+    20; forward (the rollout) and adjoint (checkpoint replay + reverse sweep)
+    timed with CUDA events."""
+    from pyminiweather_gb300.adjoint import RolloutContext, rollout, upper_half_rhot_misfit
+    from pyminiweather_gb300.data import initialize_fields
+    from pyminiweather_gb300.ics import init
+    p = dict(nx=512, nz=256, xlen=2e4, zlen=1e4, hs=2, s=4, ic_type="thermal", cfl=1.5, max_speed=450.0)
+    p["dx"], p["dz"] = p["xlen"] / 512, p["zlen"] / 256
+    p["dt"] = min(p["dx"], p["dz"]) * 1.5 / 450.0
+    p["f64_mode"] = mode
+    f = initialize_fields(p)
+    init(f, p)
+    target = f.state.clone() * 1.001
+    ctx = RolloutContext(params=p, fields=f, nsteps=200, ckpt_every=20)
+    res = []
+    for _ in range(2):  # the first pass warms up
+        x0 = f.state.clone().requires_grad_(True)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        ev[0].record()
+        loss = upper_half_rhot_misfit(rollout(x0, ctx), target, 256)
+        ev[1].record()
+        (g,) = torch.autograd.grad(loss, x0)
+        ev[2].record()
+        ev[2].synchronize()
+        res = [ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])]
+    del f, g
+    torch.cuda.empty_cache()
+    return {"grid": "512x256", "steps": 200, "ckpt_every": 20, "f64_mode": mode, "forward_ms": res[0],
+            "adjoint_ms": res[1], "ratio": res[1] / res[0]}
+
+
 def cpu_baseline(args, steps):
     from oracle import oracle as O
     threads = os.cpu_count() or 1
@@ -418,6 +450,8 @@ def run_gb300(args):
         # the batching form (ensemble of uneven grids), FP64 split and FP32
         line["ensemble"] = {"fp64": ensemble_run(torch, args.steps, args.warmup, torch.float64),
                             "fp32": ensemble_run(torch, args.steps, args.warmup, torch.float32)}
+        # the differentiation form: adjoint / forward cost
+        line["adjoint"] = {"split": adjoint_run(torch, "split"), "native": adjoint_run(torch, "native")}
         # end to end through the public API with host buffers
         init(fo, p)
         ms_e, nbytes = e2e_run(torch, p, fo, args.steps, 1)

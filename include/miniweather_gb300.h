@@ -197,6 +197,22 @@ int mw_dirstage_vjp_f64(int nx, int nz, double dx, double dz, double dt_full, co
                         const double* g_base_a, const double* g_base_b, int add_g_out, double* g_dst, double dt_stage,
                         int direction, void* workspace, size_t workspace_bytes, void* stream);
 
+/* One time step (as mw_step_f64 with nsteps = 1) that also keeps its six
+ * stage forcing states in `stages` (6 state arrays, contiguous): for the two
+ * directions in order, the direction's input S and its stage states s1, s2.
+ * No halo writes.  For the adjoint. */
+int mw_step_record_f64(int nx, int nz, double dx, double dz, double dt_full, double dt, const double* hy_dens_cell,
+                       const double* hy_dens_theta_cell, const double* hy_dens_int, const double* hy_dens_theta_int,
+                       const double* hy_pressure_int, const double* src_w, const double* state_in, double* stages,
+                       double* state_out, int reverse, int f64_mode, void* stream);
+/* Adjoint of one time step recorded by mw_step_record_f64: g_in = dJ/d(state_in)
+ * from g_out = dJ/d(state_out) (both (4, nz+4, nx+4), halo 0).  gbuf: 3 state
+ * arrays of work space (contiguous); g_in may equal g_out. */
+int mw_step_vjp_f64(int nx, int nz, double dx, double dz, double dt_full, double dt, const double* hy_dens_cell,
+                    const double* hy_dens_theta_cell, const double* hy_dens_int, const double* hy_dens_theta_int,
+                    const double* hy_pressure_int, const double* stages, const double* g_out, double* g_in,
+                    double* gbuf, int reverse, void* workspace, size_t workspace_bytes, void* stream);
+
 /* ---------------------------------------------------------------------------
  * Initial condition: replaces init (pyminiweather/ics/initial.py:11-105):
  * 3x3 Gauss-Legendre cell averages over all (nz+4)(nx+4) cells of the bubbles

@@ -41,67 +41,30 @@ class RolloutContext:
 
 
 class _Buffers:
-    """Work arrays for one grid (state-shaped FP64)."""
+    """Work arrays for one grid: the recorded stage states of a segment (six
+    per step), three adjoint work arrays and the VJP workspace."""
 
-    def __init__(self, f, n_stage_states):
-        z = lambda: torch.empty(f.shape, dtype=torch.float64, device=f.device)
-        self.f = f
-        self.stages = [z() for _ in range(n_stage_states)]
-        self.g = [z() for _ in range(4)]
+    def __init__(self, f, steps):
+        n = 4 * (f.nz + 4) * (f.nx + 4)
+        self.n = n
+        self.stages = torch.empty(6 * steps * n, dtype=torch.float64, device=f.device)
+        self.outs = torch.empty((steps + 1) * n, dtype=torch.float64, device=f.device)
+        self.gbuf = torch.empty(3 * n, dtype=torch.float64, device=f.device)
         need = int(_native.load().mw_dirstage_vjp_workspace_bytes(f.nx, f.nz))
         self.ws = torch.empty(need // 8 + 1, dtype=torch.float64, device=f.device)
 
 
-def _stage(p, f, init, forcing, out, dts, d):
+def _common(p, f, dt):
     hb = [_native.ptr(a) for a in f.backgrounds()]
-    _native.call("mw_dirstage_f64", f.nx, f.nz, float(p["dx"]), float(p["dz"]), float(p["dt"]), *hb,
-                 _native.ptr(f.src_w), _native.ptr(init), _native.ptr(forcing), _native.ptr(out), float(dts), d,
-                 f64_mode(p), 0, _native.stream_handle(f.device))
+    return [f.nx, f.nz, float(p["dx"]), float(p["dz"]), float(p["dt"]), float(dt), *hb]
 
 
-def _vjp(p, f, forcing, g_out, g_dst, dts, d, ws, base_a=None, base_b=None, add_g_out=False):
-    hb = [_native.ptr(a) for a in f.backgrounds()]
-    _native.call("mw_dirstage_vjp_f64", f.nx, f.nz, float(p["dx"]), float(p["dz"]), float(p["dt"]), *hb,
-                 _native.ptr(forcing), _native.ptr(g_out), _native.ptr(base_a), _native.ptr(base_b),
-                 int(add_g_out), _native.ptr(g_dst), float(dts), d, _native.ptr(ws), ws.numel() * 8,
-                 _native.stream_handle(f.device))
-
-
-def _directions(reverse):
-    return (_native.MW_DIR_X, _native.MW_DIR_Z) if reverse else (_native.MW_DIR_Z, _native.MW_DIR_X)
-
-
-def _forward_step(p, f, S, out, stage_states, reverse):
-    """One time step S -> out through six direction-stages, keeping the stage
-    forcing states in stage_states[0..5] (S, s1, s2 per direction)."""
-    dt = p["dt"]
-    cur = S
-    for n, d in enumerate(_directions(reverse)):
-        S_d, s1, s2 = stage_states[3 * n:3 * n + 3]
-        if S_d.data_ptr() != cur.data_ptr():
-            S_d.copy_(cur)
-        _stage(p, f, S_d, S_d, s1, dt / 3, d)
-        _stage(p, f, S_d, s1, s2, dt / 2, d)
-        dst = out if n == 1 else stage_states[3]
-        _stage(p, f, S_d, s2, dst, dt, d)
-        cur = dst
-
-
-def _backward_step(p, f, stage_states, g, reverse, buf):
-    """g: adjoint of the step's output; returns the adjoint of its input (one of buf.g)."""
-    dt = p["dt"]
-    gA, gB, gC, gD = buf.g
-    cur = g
-    for n, d in reversed(list(enumerate(_directions(reverse)))):
-        S_d, s1, s2 = stage_states[3 * n:3 * n + 3]
-        s2b = gA if cur.data_ptr() != gA.data_ptr() else gD
-        _vjp(p, f, s2, cur, s2b, dt, d, buf.ws)
-        s1b = gB
-        _vjp(p, f, s1, s2b, s1b, dt / 2, d, buf.ws)
-        outg = gC if cur.data_ptr() != gC.data_ptr() else gD
-        _vjp(p, f, S_d, s1b, outg, dt / 3, d, buf.ws, base_a=cur, base_b=s2b, add_g_out=True)
-        cur = outg
-    return cur
+def _segment_forward(p, f, cur, tmp, scratch, nsteps, reverse):
+    """nsteps steps of cur in place (mw_step_f64); returns the new direction flag."""
+    rv = ctypes.c_int(1 if reverse else 0)
+    _native.call("mw_step_f64", *_common(p, f, p["dt"]), _native.ptr(f.src_w), _native.ptr(cur), _native.ptr(tmp),
+                 _native.ptr(scratch), int(nsteps), ctypes.byref(rv), f64_mode(p), 0, _native.stream_handle(f.device))
+    return bool(rv.value)
 
 
 class Rollout(torch.autograd.Function):
@@ -112,16 +75,15 @@ class Rollout(torch.autograd.Function):
         p, f = ctx.params, ctx.fields
         _native.require_cuda(state0, "state0", dtype=torch.float64, shape=f.shape)
         cur = state0.detach().clone()
-        nxt = torch.empty_like(cur)
-        stages = [torch.empty_like(cur) for _ in range(6)]
+        tmp, scratch = torch.empty_like(cur), torch.empty_like(cur)
         ckpts = []
         rev = ctx.reverse
-        for k in range(ctx.nsteps):
-            if k % ctx.ckpt_every == 0:
-                ckpts.append((k, cur.clone(), rev))
-            _forward_step(p, f, cur, nxt, stages, rev)
-            cur, nxt = nxt, cur
-            rev = not rev
+        k = 0
+        while k < ctx.nsteps:
+            n = min(ctx.ckpt_every, ctx.nsteps - k)
+            ckpts.append((k, cur.clone(), rev))
+            rev = _segment_forward(p, f, cur, tmp, scratch, n, rev)
+            k += n
         autograd_ctx.ctx = ctx
         autograd_ctx.ckpts = ckpts
         return cur
@@ -130,26 +92,27 @@ class Rollout(torch.autograd.Function):
     def backward(autograd_ctx, g_final):
         ctx = autograd_ctx.ctx
         p, f = ctx.params, ctx.fields
-        E = ctx.ckpt_every
-        buf = _Buffers(f, 6 * E)
+        buf = _Buffers(f, ctx.ckpt_every)
+        N = buf.n
         g = g_final.detach().to(torch.float64).contiguous().clone()
-        out = torch.empty_like(g)
+        stream = _native.stream_handle(f.device)
+        common = _common(p, f, p["dt"])
         for k0, state, rev0 in reversed(autograd_ctx.ckpts):
-            n = min(E, ctx.nsteps - k0)
-            # replay the segment, keeping the six stage states of every step
-            cur = state
+            n = min(ctx.ckpt_every, ctx.nsteps - k0)
+            # replay the segment, recording the six stage states of every step
+            buf.outs[:N].copy_(state.reshape(-1))
             rev = rev0
             revs = []
             for j in range(n):
-                st = buf.stages[6 * j:6 * j + 6]
-                st[0].copy_(cur)
-                _forward_step(p, f, st[0], out, st, rev)
+                _native.call("mw_step_record_f64", *common, _native.ptr(f.src_w),
+                             _native.ptr(buf.outs[j * N:]), _native.ptr(buf.stages[6 * j * N:]),
+                             _native.ptr(buf.outs[(j + 1) * N:]), int(rev), f64_mode(p), stream)
                 revs.append(rev)
-                cur = out
                 rev = not rev
             for j in reversed(range(n)):
-                res = _backward_step(p, f, buf.stages[6 * j:6 * j + 6], g, revs[j], buf)
-                g.copy_(res)
+                _native.call("mw_step_vjp_f64", *common, _native.ptr(buf.stages[6 * j * N:]), _native.ptr(g),
+                             _native.ptr(g), _native.ptr(buf.gbuf), int(revs[j]), _native.ptr(buf.ws),
+                             buf.ws.numel() * 8, stream)
         g[:, :2, :].zero_()
         g[:, -2:, :].zero_()
         g[:, :, :2].zero_()

@@ -274,3 +274,42 @@ extern "C" int mw_dirstage_vjp_f64(int nx, int nz, double dx, double dz, double 
   }
   return check_launch("vjp gather launch");
 }
+
+// ---------------------------------------------------------------------------
+// Adjoint of one recorded time step (stages from mw_step_record_f64).  Per
+// direction, in reverse (RK3 of solve/step.py:112-141):
+//   s2bar = VJP(s2; g),  s1bar = VJP(s1; s2bar),  Sbar = g + s2bar + s1bar + VJP(S; s1bar).
+extern "C" int mw_step_vjp_f64(int nx, int nz, double dx, double dz, double dt_full, double dt, const double* hyc,
+                               const double* hytc, const double* hyi, const double* hyti, const double* hypi,
+                               const double* stages, const double* g_out, double* g_in, double* gbuf, int reverse,
+                               void* workspace, size_t workspace_bytes, void* stream) {
+  MW_REQUIRE(stages && g_out && g_in && gbuf, MW_ERR_INVALID_ARG, "NULL pointer argument");
+  MW_REQUIRE(finite_pos(dt), MW_ERR_INVALID_ARG, "dt must be finite and positive");
+  const size_t n = 4 * (size_t)make_geom(nx, nz).plane;
+  MW_REQUIRE(!ranges_overlap(gbuf, 3 * n * sizeof(double), g_in, n * sizeof(double)) &&
+                 !ranges_overlap(gbuf, 3 * n * sizeof(double), g_out, n * sizeof(double)),
+             MW_ERR_ALIAS, "gbuf must not overlap g_in or g_out");
+  double* gA = gbuf;
+  double* gB = gbuf + n;
+  double* gC = gbuf + 2 * n;
+  const int dirs[2] = {reverse ? MW_DIR_X : MW_DIR_Z, reverse ? MW_DIR_Z : MW_DIR_X};
+  const double* cur = g_out;
+  int st;
+  for (int d = 1; d >= 0; --d) {
+    const double* S = stages + (3 * d) * n;
+    const double* s1 = S + n;
+    const double* s2 = S + 2 * n;
+    double* out = d == 1 ? gC : g_in;
+    if ((st = mw_dirstage_vjp_f64(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, s2, cur, nullptr, nullptr, 0, gA,
+                                  dt, dirs[d], workspace, workspace_bytes, stream)))
+      return st;
+    if ((st = mw_dirstage_vjp_f64(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, s1, gA, nullptr, nullptr, 0, gB,
+                                  dt / 2, dirs[d], workspace, workspace_bytes, stream)))
+      return st;
+    if ((st = mw_dirstage_vjp_f64(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, S, gB, cur, gA, 1, out, dt / 3,
+                                  dirs[d], workspace, workspace_bytes, stream)))
+      return st;
+    cur = out;
+  }
+  return MW_OK;
+}

@@ -65,6 +65,16 @@ inline bool ranges_overlap(const void* a, size_t abytes, const void* b, size_t b
 
 int check_grid(int nx, int nz);
 
+// Rows per z CTA for a single-grid launch: the largest tile up to max_rows
+// that still gives about two CTAs per SM (152 SMs), at least 8 rows.
+inline int z_tile_rows(int nx, int nz, int cols_per_cta, int max_rows) {
+  const long long ncb = (nx + cols_per_cta - 1) / cols_per_cta;
+  long long t = (long long)nz * ncb / 304;
+  if (t > max_rows) t = max_rows;
+  if (t < 8) t = 8;
+  return (int)t;
+}
+
 }  // namespace mw
 
 #define MW_REQUIRE(cond, code, ...)            \

@@ -49,6 +49,7 @@ struct StageArgs {
   T* out;
   unsigned flags;
   int chunks_per_block;
+  int z_tile;
 };
 
 // ---- interpolation in the accumulation order of scipy.signal.convolve ----
@@ -404,8 +405,8 @@ __global__ void __launch_bounds__(kXThreads) k_stage_x(StageArgs<T> a) {
 template <typename T, int MODE>
 __global__ void __launch_bounds__(kZThreads) k_stage_z(StageArgs<T> a) {
   __shared__ SmemZT sm;
-  z_tile_t<T, MODE>(a, blockIdx.x, blockIdx.y * kZTile, kZTile, (a.flags & MW_FLAG_WRITE_HALO) && blockIdx.y == 0,
-                    sm);
+  z_tile_t<T, MODE>(a, blockIdx.x, blockIdx.y * a.z_tile, a.z_tile,
+                    (a.flags & MW_FLAG_WRITE_HALO) && blockIdx.y == 0, sm);
 }
 
 // ---------------------------------------------------------------------------
@@ -432,6 +433,7 @@ __device__ StageArgs<float> member_args_f32(const EnsStageT<float>& es, int e) {
   a.out = es.out + m.state_off;
   a.flags = es.flags;
   a.chunks_per_block = 0;
+  a.z_tile = es.z_tile;
   return a;
 }
 
@@ -522,11 +524,12 @@ static int launch_stage(int nx, int nz, double dx, double dz, double dt_full, co
   a.flags = flags;
   const int nchunks = (nx + kXCells - 1) / kXCells;
   a.chunks_per_block = (nchunks + kXBlocksPerRow - 1) / kXBlocksPerRow;
+  a.z_tile = z_tile_rows(nx, nz, kZThreads, kZTile);
   if (direction == MW_DIR_X) {
     dim3 grid((nchunks + a.chunks_per_block - 1) / a.chunks_per_block, (unsigned)min(nz, 65535));
     k_stage_x<T, MODE><<<grid, kXThreads, 0, stream>>>(a);
   } else {
-    dim3 grid((nx + kZThreads - 1) / kZThreads, (nz + kZTile - 1) / kZTile);
+    dim3 grid((nx + kZThreads - 1) / kZThreads, (nz + a.z_tile - 1) / a.z_tile);
     k_stage_z<T, MODE><<<grid, kZThreads, 0, stream>>>(a);
   }
   return check_launch(direction == MW_DIR_X ? "x direction-stage launch" : "z direction-stage launch");
@@ -717,4 +720,43 @@ extern "C" int mw_step_f64_noalloc(int nx, int nz, double dx, double dz, double 
                              return stage_f64(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, src_w, init,
                                               forcing, out, dts, dir, f64_mode, flags, s);
                            });
+}
+
+// ---------------------------------------------------------------------------
+// One time step that keeps its six stage forcing states (for the adjoint).
+extern "C" int mw_step_record_f64(int nx, int nz, double dx, double dz, double dt_full, double dt, const double* hyc,
+                                  const double* hytc, const double* hyi, const double* hyti, const double* hypi,
+                                  const double* src_w, const double* state_in, double* stages, double* state_out,
+                                  int reverse, int f64_mode, void* stream) {
+  MW_REQUIRE(state_in && stages && state_out, MW_ERR_INVALID_ARG, "NULL pointer argument");
+  const size_t n = 4 * (size_t)make_geom(nx, nz).plane;
+  int st = validate_stage<double>(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, stages, stages + n, state_out,
+                                  MW_DIR_X);
+  if (st) return st;
+  MW_REQUIRE(finite_pos(dt), MW_ERR_INVALID_ARG, "dt must be finite and positive");
+  MW_REQUIRE(f64_mode == MW_F64_NATIVE || f64_mode == MW_F64_SPLIT, MW_ERR_INVALID_ARG, "unknown f64_mode %d",
+             f64_mode);
+  MW_REQUIRE(!ranges_overlap(stages, 6 * n * sizeof(double), state_out, n * sizeof(double)) &&
+                 !ranges_overlap(stages, 6 * n * sizeof(double), state_in, n * sizeof(double)),
+             MW_ERR_ALIAS, "stages must not overlap state_in or state_out");
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaMemcpyAsync(stages, state_in, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  if (e != cudaSuccess) return fail(MW_ERR_CUDA, "stage copy: %s", cudaGetErrorString(e));
+  const int dirs[2] = {reverse ? MW_DIR_X : MW_DIR_Z, reverse ? MW_DIR_Z : MW_DIR_X};
+  for (int d = 0; d < 2; ++d) {
+    double* S = stages + (3 * d) * n;
+    double* s1 = S + n;
+    double* s2 = S + 2 * n;
+    double* out = d == 0 ? stages + 3 * n : state_out;
+    if ((st = stage_f64(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, src_w, S, S, s1, dt / 3, dirs[d], f64_mode,
+                        0, s)))
+      return st;
+    if ((st = stage_f64(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, src_w, S, s1, s2, dt / 2, dirs[d], f64_mode,
+                        0, s)))
+      return st;
+    if ((st = stage_f64(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, src_w, S, s2, out, dt, dirs[d], f64_mode, 0,
+                        s)))
+      return st;
+  }
+  return MW_OK;
 }

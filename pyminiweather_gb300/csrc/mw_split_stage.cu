@@ -80,6 +80,7 @@ struct SplitArgs {
   double* out;
   unsigned flags;
   int chunks_per_block;  // x: 255-cell chunks walked by one CTA
+  int z_tile;            // z: rows per CTA
   dwc hv12;              // 12 * hv
   double c12;            // dt_stage / (12 d): out = init + c12 * (F(i) - F(i+1))
   dwc d12;               // 12 d (source term: dt * src = c12 * 12 d * src)
@@ -373,7 +374,7 @@ __global__ void __launch_bounds__(kXThreads) k_stage_x_split(SplitArgs a) {
 
 __global__ void __launch_bounds__(kZThreads, 6) k_stage_z_split(SplitArgs a) {
   __shared__ SmemZ sm;
-  z_tile(a, blockIdx.x, blockIdx.y * kZTile, kZTile, (a.flags & MW_FLAG_WRITE_HALO) && blockIdx.y == 0, sm);
+  z_tile(a, blockIdx.x, blockIdx.y * a.z_tile, a.z_tile, (a.flags & MW_FLAG_WRITE_HALO) && blockIdx.y == 0, sm);
 }
 
 // ---------------------------------------------------------------------------
@@ -397,6 +398,7 @@ __device__ SplitArgs member_args(const EnsStage& es, int e) {
   a.out = es.out + m.state_off;
   a.flags = es.flags;
   a.chunks_per_block = 0;
+  a.z_tile = es.z_tile;
   const double d = es.direction == MW_DIR_X ? m.dx : m.dz;
   const double dts = m.dt / (double)es.stage_div;  // dt/3, dt/2, dt/1 as evolve forms them
   const double hv = -kHvBeta * d / (16 * m.dt);
@@ -474,11 +476,12 @@ int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, con
   a.gz12 = split_host(12.0 * dz * kGrav);
   const int nchunks = (nx + kXCells - 1) / kXCells;
   a.chunks_per_block = (nchunks + kXBlocksPerRow - 1) / kXBlocksPerRow;
+  a.z_tile = z_tile_rows(nx, nz, kZThreads, kZTile);
   if (direction == MW_DIR_X) {
     dim3 grid((nchunks + a.chunks_per_block - 1) / a.chunks_per_block, (unsigned)min(nz, 65535));
     k_stage_x_split<<<grid, kXThreads, 0, stream>>>(a);
   } else {
-    dim3 grid((nx + kZThreads - 1) / kZThreads, (nz + kZTile - 1) / kZTile);
+    dim3 grid((nx + kZThreads - 1) / kZThreads, (nz + a.z_tile - 1) / a.z_tile);
     k_stage_z_split<<<grid, kZThreads, 0, stream>>>(a);
   }
   return check_launch(direction == MW_DIR_X ? "x split direction-stage launch" : "z split direction-stage launch");

@@ -190,37 +190,55 @@ def test_fp32_form_error_and_mass():
     assert abs(m1 - m0) / m0 <= 1e-9
 
 
-@pytest.mark.parametrize("mode", ["split"])
-def test_fullsize_200_steps_vs_oracle(mode):
-    """The benchmark's stated criterion: 8192 x 4096 collision, 200 steps,
-    within 1e-10 per-variable normwise of the reference algorithm (the oracle,
-    pinned to the reference at small sizes).  Also mass conservation and the
-    mirror symmetry of the collision case about x = xlen/2."""
+def test_fullsize_200_steps_vs_oracle():
+    """The benchmark's stated criteria at 8192 x 4096 (collision), against the
+    oracle (pinned to the reference at small sizes):
+    - FP64 (split form) within 1e-10 per-variable normwise after 200 steps;
+      mass conserved; mirror symmetry about x = xlen/2 kept;
+    - FP32 perturbation fields: relative L2 of dens and rhot within 1e-4 at
+      steps 50, 100 and 200 (max error and mass drift reported)."""
     import os
-    nx, nz, steps = 8192, 4096, 200
+    nx, nz, marks = 8192, 4096, (50, 100, 200)
     p = make_params(nx, nz, "collision")
-    p["f64_mode"] = mode
-    f = initialize_fields(p)
-    init(f, p)
-    m0 = compute_stats(p, f)[0]
-    reset_direction()
-    evolve(p, f, None, dt=p["dt"], nsteps=steps)
-    m1 = compute_stats(p, f)[0]
-    got = host(f.state)
-    s = f.state[:, 2:-2, 2:-2]
-    scale = s.abs().amax(dim=(1, 2))
-    sign = torch.tensor([1.0, -1.0, 1.0, 1.0], dtype=s.dtype, device=s.device).view(4, 1, 1)
-    asym = ((s - sign * torch.flip(s, dims=[2])).abs().amax(dim=(1, 2)) / scale).tolist()
-    del f, s
-    torch.cuda.empty_cache()
+    p["f64_mode"] = "split"
+    got = {}
+    for dtype in (torch.float64, torch.float32):
+        f = initialize_fields(p, dtype=dtype)
+        init(f, p)
+        m0 = compute_stats(p, f)[0]
+        reset_direction()
+        done = 0
+        for c in marks:
+            evolve(p, f, None, dt=p["dt"], nsteps=c - done)
+            done = c
+            got[(dtype, c)] = host(f.state)
+        got[(dtype, "drift")] = (compute_stats(p, f)[0] - m0) / m0
+        if dtype == torch.float64:
+            s = f.state[:, 2:-2, 2:-2]
+            scale = s.abs().amax(dim=(1, 2))
+            sign = torch.tensor([1.0, -1.0, 1.0, 1.0], dtype=s.dtype, device=s.device).view(4, 1, 1)
+            got["asym"] = ((s - sign * torch.flip(s, dims=[2])).abs().amax(dim=(1, 2)) / scale).tolist()
+            del s
+        del f
+        torch.cuda.empty_cache()
     o = O.OracleSim(O.make_params(nx, nz, "collision"), threads=os.cpu_count())
-    o.evolve(steps)
-    err = normwise(got, o.state)
-    print("%s 8192x4096 collision 200 steps vs oracle: %s  mirror asymmetry %s  mass drift %.2e" % (
-        mode, ["%.2e" % e for e in err], ["%.1e" % a for a in asym], (m1 - m0) / m0))
-    assert max(err) <= TOL_STEP
-    assert max(asym) <= TOL_STEP
-    assert abs(m1 - m0) / m0 <= 1e-13
+    done = 0
+    for c in marks:
+        o.evolve(c - done)
+        done = c
+        e64 = normwise(got[(torch.float64, c)], o.state)
+        l2 = rel_l2(got[(torch.float32, c)], o.state)
+        mx = normwise(got[(torch.float32, c)], o.state)
+        print("8192x4096 collision step %d: FP64 split normwise %s | FP32 rel-L2 dens %.2e rhot %.2e, "
+              "max dens %.2e rhot %.2e" % (c, ["%.2e" % e for e in e64], l2[0], l2[3], mx[0], mx[3]))
+        assert l2[IDS.DENS] <= 1e-4 and l2[IDS.RHOT] <= 1e-4
+        if c == marks[-1]:
+            assert max(e64) <= TOL_STEP
+    print("mass drift FP64 %.2e FP32 %.2e; FP64 mirror asymmetry %s" % (
+        got[(torch.float64, "drift")], got[(torch.float32, "drift")], ["%.1e" % a for a in got["asym"]]))
+    assert max(got["asym"]) <= TOL_STEP
+    assert abs(got[(torch.float64, "drift")]) <= 1e-13
+    assert abs(got[(torch.float32, "drift")]) <= 1e-6
 
 
 def test_reference_interpolate_tests():  # tests/unit/test_interpolate.py:11-63
