@@ -1,0 +1,85 @@
+// mw_split2.cuh -- pairs of double-FP32 values in packed FP32 instructions.
+//
+// sm_100-class SMs execute FP32 add / multiply / FMA on register pairs
+// (f32x2): one issued instruction performs the same operation on two
+// independent values.  dw2 holds two independent double-words,
+// (h.x + l.x) and (h.y + l.y), and applies the algorithms of mw_split.cuh to
+// both at once.  The direction-stage kernels pair the state variables as
+// (DENS, UMOM) and (WMOM, RHOT), which halves the instruction count of the
+// per-variable work (interpolation, hyperviscosity, flux differences).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "mw_split.cuh"
+
+namespace mw {
+namespace split {
+
+struct dw2 {
+  float2 h, l;
+};
+
+__device__ __forceinline__ unsigned long long f2_bits(float2 a) {
+  return ((unsigned long long)__float_as_uint(a.y) << 32) | __float_as_uint(a.x);
+}
+__device__ __forceinline__ float2 f2_from(unsigned long long b) {
+  return make_float2(__uint_as_float((unsigned)b), __uint_as_float((unsigned)(b >> 32)));
+}
+
+__device__ __forceinline__ float2 f2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 f2mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b) {
+  unsigned long long d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+  return f2_from(d);
+}
+__device__ __forceinline__ float2 f2splat(float v) { return make_float2(v, v); }
+
+__device__ __forceinline__ dw2 two_sum2(float2 a, float2 b) {
+  const float2 s = f2add(a, b);
+  const float2 bb = f2sub(s, a);
+  const float2 e = f2add(f2sub(a, f2sub(s, bb)), f2sub(b, bb));
+  return {s, e};
+}
+// a - b exactly as s + e
+__device__ __forceinline__ dw2 two_diff2(float2 a, float2 b) {
+  const float2 s = f2sub(a, b);
+  const float2 bb = f2sub(s, a);  // -b as rounded
+  const float2 e = f2sub(f2sub(a, f2sub(s, bb)), f2add(b, bb));
+  return {s, e};
+}
+// requires |a| >= |b| (or a == 0) in each lane
+__device__ __forceinline__ dw2 fast_two_sum2(float2 a, float2 b) {
+  const float2 s = f2add(a, b);
+  return {s, f2sub(b, f2sub(s, a))};
+}
+
+__device__ __forceinline__ dw2 add2(dw2 x, dw2 y) {
+  const dw2 s = two_sum2(x.h, y.h);
+  return fast_two_sum2(s.h, f2add(s.l, f2add(x.l, y.l)));
+}
+__device__ __forceinline__ dw2 sub2(dw2 x, dw2 y) {
+  const dw2 s = two_diff2(x.h, y.h);
+  return fast_two_sum2(s.h, f2add(s.l, f2sub(x.l, y.l)));
+}
+// x * y; ny_h = -y.h (callers multiplying by a constant pass it precomputed)
+__device__ __forceinline__ dw2 mul2n(dw2 x, dw2 y, float2 ny_h) {
+  const float2 p = f2mul(x.h, y.h);
+  float2 e = f2fma(x.h, y.h, f2mul(x.h, ny_h));  // exact product error: x.h*y.h - p
+  e = f2fma(x.h, y.l, e);
+  e = f2fma(x.l, y.h, e);
+  return fast_two_sum2(p, e);
+}
+__device__ __forceinline__ dw2 mul2(dw2 x, dw2 y) {
+  return mul2n(x, y, f2sub(make_float2(0.f, 0.f), y.h));
+}
+
+__device__ __forceinline__ dw2 pack(dw a, dw b) { return {make_float2(a.h, b.h), make_float2(a.l, b.l)}; }
+__device__ __forceinline__ dw lo_of(dw2 p) { return {p.h.x, p.l.x}; }
+__device__ __forceinline__ dw hi_of(dw2 p) { return {p.h.y, p.l.y}; }
+__device__ __forceinline__ dw2 splat(dw a) { return {f2splat(a.h), f2splat(a.l)}; }
+
+}  // namespace split
+}  // namespace mw

@@ -23,6 +23,7 @@
 #include "mw_common.cuh"
 #include "mw_ensemble.cuh"
 #include "mw_split.cuh"
+#include "mw_split2.cuh"
 
 namespace mw {
 using namespace split;
@@ -54,8 +55,14 @@ __constant__ float c_pow_f[17] = {0.f,
 constexpr int kXThreads = 256;
 constexpr int kXCells = kXThreads - 1;
 constexpr int kXTile = kXThreads + 3;  // cells x0-2 .. x0+256
+#ifndef MW_ZSPLIT_MIN_BLOCKS
+#define MW_ZSPLIT_MIN_BLOCKS 5  // z CTAs per SM the register allocation must allow
+#endif
+#ifndef MW_ZSPLIT_TILE
+#define MW_ZSPLIT_TILE 64
+#endif
 constexpr int kZThreads = 128;
-constexpr int kZTile = 64;
+constexpr int kZTile = MW_ZSPLIT_TILE;
 constexpr int kZTileMax = 64;
 constexpr int kXBlocksPerRow = 2;  // x CTAs per row; each walks a run of chunks
 
@@ -115,58 +122,74 @@ __device__ __forceinline__ dw pgm1(dw d) {
 }
 
 // 12 * (4-point interpolation) = 7 (s1 + s2) - (s0 + s3) and the third
-// difference (s3 - s0) - 3 (s2 - s1).  The leading floats are combined with
-// error-free transformations (exact), the trailing floats and the rounding
-// errors are summed in FP32 (error about 2^-48 of the operands), and the pair
-// is renormalised once.
-__device__ __forceinline__ void interp_split(dw s0, dw s1, dw s2, dw s3, dw& A, dw& D) {
-  const dw a = two_sum(s1.h, s2.h);
-  const dw b = two_sum(s0.h, s3.h);
-  const dw a7 = two_prod(a.h, 7.0f);
-  const dw r = two_sum(a7.h, -b.h);
-  const float lo = (fmaf(7.0f, (s1.l + s2.l) + a.l, a7.l) - ((s0.l + s3.l) + b.l)) + r.l;
-  A = fast_two_sum(r.h, lo);
-  const dw p = two_sum(s3.h, -s0.h);
-  const dw q = two_sum(s2.h, -s1.h);
-  const dw q3 = two_prod(q.h, 3.0f);
-  const dw t = two_sum(p.h, -q3.h);
-  const float lo2 = (((s3.l - s0.l) + p.l) - fmaf(3.0f, (s2.l - s1.l) + q.l, q3.l)) + t.l;
-  D = fast_two_sum(t.h, lo2);
+// difference (s3 - s0) - 3 (s2 - s1), for a pair of variables at once.  The
+// leading floats are combined with error-free transformations (exact), the
+// trailing floats and the rounding errors are summed in FP32 (error about
+// 2^-48 of the operands), and each result is renormalised once.
+__device__ __forceinline__ void interp2(dw2 s0, dw2 s1, dw2 s2, dw2 s3, dw2& A, dw2& D) {
+  const float2 c7 = f2splat(7.0f), m7 = f2splat(-7.0f), c3 = f2splat(3.0f), m3 = f2splat(-3.0f);
+  const dw2 a = two_sum2(s1.h, s2.h);
+  const dw2 b = two_sum2(s0.h, s3.h);
+  const float2 a7 = f2mul(a.h, c7);
+  const float2 a7e = f2fma(a.h, c7, f2mul(a.h, m7));  // exact: 7 a.h - a7
+  const dw2 r = two_diff2(a7, b.h);
+  const float2 lo = f2add(f2sub(f2fma(c7, f2add(f2add(s1.l, s2.l), a.l), a7e), f2add(f2add(s0.l, s3.l), b.l)), r.l);
+  A = fast_two_sum2(r.h, lo);
+  const dw2 p = two_diff2(s3.h, s0.h);
+  const dw2 q = two_diff2(s2.h, s1.h);
+  const float2 q3 = f2mul(q.h, c3);
+  const float2 q3e = f2fma(q.h, c3, f2mul(q.h, m3));
+  const dw2 t = two_diff2(p.h, q3);
+  const float2 lo2 =
+      f2add(f2sub(f2add(f2sub(s3.l, s0.l), p.l), f2fma(c3, f2add(f2sub(s2.l, s1.l), q.l), q3e)), t.l);
+  D = fast_two_sum2(t.h, lo2);
 }
 
-// x flux times 12 (interpolate.py:105-129): with q = u = (rho u)'/rho,
-// F = ((rho u)', q (rho u)' + p', q (rho w)', q (rho theta)) - hv d3.
-__device__ __forceinline__ void flux_x_split(const dw s[4][4], const RowS& r, dw hv12, dw F[4]) {
-  dw A[4], D[4];
-#pragma unroll
-  for (int q = 0; q < 4; ++q) interp_split(s[q][0], s[q][1], s[q][2], s[q][3], A[q], D[q]);
-  const dw ri = rcp(add(A[DENS], r.R));
-  const dw u = mul(A[UMOM], ri);
-  const dw pp = mul(r.P12, pgm1(mul(A[RHOT], r.IRT)));
-  F[0] = sub(A[UMOM], mul(hv12, D[DENS]));
-  F[1] = sub(add(mul(u, A[UMOM]), pp), mul(hv12, D[UMOM]));
-  F[2] = sub(mul(u, A[WMOM]), mul(hv12, D[WMOM]));
-  F[3] = sub(mul(u, add(A[RHOT], r.RT)), mul(hv12, D[RHOT]));
+// Hyperviscosity constant in paired form: HV = 12 hv in both lanes, nHV its negated leading float.
+struct Hv2 {
+  dw2 v;
+  float2 nh;
+};
+__device__ __forceinline__ Hv2 make_hv2(dw hv12) { return {splat(hv12), f2splat(-hv12.h)}; }
+
+// x flux times 12 (interpolate.py:105-129) for the taps s[pair][j], pairs
+// (DENS, UMOM) and (WMOM, RHOT).  With u = (rho u)'/rho:
+// F = ((rho u)', u (rho u)' + p', u (rho w)', u (rho theta)) - hv d3.
+__device__ __forceinline__ void flux_x2(const dw2 s[2][4], const RowS& r, const Hv2& hv, dw2 F[2]) {
+  dw2 A[2], D[2];
+  interp2(s[0][0], s[0][1], s[0][2], s[0][3], A[0], D[0]);
+  interp2(s[1][0], s[1][1], s[1][2], s[1][3], A[1], D[1]);
+  const dw AD = lo_of(A[0]), AU = hi_of(A[0]), AW = lo_of(A[1]), AT = hi_of(A[1]);
+  const dw ri = rcp(add(AD, r.R));
+  const dw u = mul(AU, ri);
+  const dw pp = mul(r.P12, pgm1(mul(AT, r.IRT)));
+  const dw2 uu = mul2(splat(u), pack(AU, AW));
+  const dw X1 = add(lo_of(uu), pp);
+  const dw X3 = mul(u, add(AT, r.RT));
+  F[0] = sub2(pack(AU, X1), mul2n(D[0], hv.v, hv.nh));
+  F[1] = sub2(pack(hi_of(uu), X3), mul2n(D[1], hv.v, hv.nh));
 }
 
 // z flux times 12 (interpolate.py:153-186); w and d3[DENS] vanish at the walls.
-__device__ __forceinline__ void flux_z_split(const dw s[4][4], const RowS& r, dw hv12, bool wall, dw F[4]) {
-  dw A[4], D[4];
-#pragma unroll
-  for (int q = 0; q < 4; ++q) interp_split(s[q][0], s[q][1], s[q][2], s[q][3], A[q], D[q]);
-  const dw ri = rcp(add(A[DENS], r.R));
-  const dw pp = mul(r.P12, pgm1(mul(A[RHOT], r.IRT)));
-  dw rw = A[WMOM];
-  dw dd = D[DENS];
+__device__ __forceinline__ void flux_z2(const dw2 s[2][4], const RowS& r, const Hv2& hv, bool wall, dw2 F[2]) {
+  dw2 A[2], D[2];
+  interp2(s[0][0], s[0][1], s[0][2], s[0][3], A[0], D[0]);
+  interp2(s[1][0], s[1][1], s[1][2], s[1][3], A[1], D[1]);
+  const dw AD = lo_of(A[0]), AU = hi_of(A[0]), AT = hi_of(A[1]);
+  dw rw = lo_of(A[1]);
   if (wall) {
     rw = dw{0.f, 0.f};
-    dd = dw{0.f, 0.f};
+    D[0].h.x = 0.f;
+    D[0].l.x = 0.f;
   }
+  const dw ri = rcp(add(AD, r.R));
+  const dw pp = mul(r.P12, pgm1(mul(AT, r.IRT)));
   const dw w = mul(rw, ri);
-  F[0] = sub(rw, mul(hv12, dd));
-  F[1] = sub(mul(w, A[UMOM]), mul(hv12, D[UMOM]));
-  F[2] = sub(add(mul(w, rw), pp), mul(hv12, D[WMOM]));
-  F[3] = sub(mul(w, add(A[RHOT], r.RT)), mul(hv12, D[RHOT]));
+  const dw2 ww = mul2(splat(w), pack(AU, rw));
+  const dw X2 = add(hi_of(ww), pp);
+  const dw X3 = mul(w, add(AT, r.RT));
+  F[0] = sub2(pack(rw, lo_of(ww)), mul2n(D[0], hv.v, hv.nh));
+  F[1] = sub2(pack(X2, X3), mul2n(D[1], hv.v, hv.nh));
 }
 
 __device__ __forceinline__ RowS row_consts(double hy_r, double hy_rt, double P) {
@@ -210,23 +233,38 @@ __device__ __forceinline__ double update(double init, dw dF, double c12) { retur
 // call these; every thread of the CTA must call them (they contain barriers).
 
 struct SmemX {
-  dw sS[4][kXTile + 1];
-  dw sF[4][kXThreads];
+  dw2 sS[2][2][kXTile + 1];  // [buffer][pair][cell]
+  dw2 sF[2][2][kXThreads];   // [buffer][pair][interface]
   RowS row;
 };
 struct SmemZ {
   RowS row[kZTileMax + 1];
 };
 
-// x: row k, chunks [cbeg, cend) of 255 cells.  Per chunk: stage the 259
-// forcing values (split once) in shared memory, thread t evaluates the flux at
-// interface x0+t, thread t updates cell x0+t.  The next chunk's forcing values
-// and this chunk's init values are loaded before the flux evaluation so their
-// latency is covered by it.  The row constants (an FP64 pow) are formed once
-// per call.  halo: write the periodic halo of this row of the forcing array.
+__device__ __forceinline__ void pack4(const double v[4], dw2 out[2]) {
+  out[0] = pack(from_f64(v[DENS]), from_f64(v[UMOM]));
+  out[1] = pack(from_f64(v[WMOM]), from_f64(v[RHOT]));
+}
+
+// out = init + c12 (F(i) - F(i+1)) for the four variables (paired differences,
+// then per value one FP64 add merging the pair and one FP64 FMA).
+__device__ __forceinline__ void store_update(const SplitArgs& a, long long o, const double iv[4], dw2 dF[2]) {
+  const dw d[4] = {lo_of(dF[0]), hi_of(dF[0]), lo_of(dF[1]), hi_of(dF[1])};
+#pragma unroll
+  for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = update(iv[q], d[q], a.c12);
+}
+
+// x: row k, chunks [cbeg, cend) of 255 cells.  Per chunk: the 259 forcing
+// values, split once, are staged in shared memory as variable pairs; thread
+// t evaluates the flux at interface x0+t and, after one barrier, updates cell
+// x0+t.  Staging and fluxes are double-buffered, so one barrier per chunk
+// suffices; the next chunk's values and this chunk's init values are loaded
+// before the flux evaluation.  The row constants (an FP64 pow) are formed
+// once per call.  halo: write this row's periodic halo into forcing.
 __device__ __forceinline__ void x_rowrun(const SplitArgs& a, int k, int cbeg, int cend, bool halo, SmemX& sm) {
   const int t = threadIdx.x;
-  const dw hv12 = ld(a.hv12), d12 = ld(a.d12);
+  const Hv2 hv = make_hv2(ld(a.hv12));
+  const dw d12 = ld(a.d12);
   const long long row = (long long)(k + kHs) * a.pitch;
   auto load_stage = [&](int x0, double v0[4], double v1[4]) {
     const int c0 = x0 - 2 + t, c1 = c0 + kXThreads;
@@ -241,6 +279,17 @@ __device__ __forceinline__ void x_rowrun(const SplitArgs& a, int k, int cbeg, in
       for (int q = 0; q < 4; ++q) v1[q] = __ldg(a.forcing + q * a.plane + row + col);
     }
   };
+  auto store_stage = [&](int b, const double v0[4], const double v1[4]) {
+    dw2 p[2];
+    pack4(v0, p);
+    sm.sS[b][0][t] = p[0];
+    sm.sS[b][1][t] = p[1];
+    if (t < kXTile - kXThreads) {
+      pack4(v1, p);
+      sm.sS[b][0][t + kXThreads] = p[0];
+      sm.sS[b][1][t + kXThreads] = p[1];
+    }
+  };
   if (t == 0) {
     const double hrt = a.hytc[k + kHs];
     sm.row = row_consts(a.hyc[k + kHs], hrt, kC0 * pow(hrt, kGamma));
@@ -252,17 +301,15 @@ __device__ __forceinline__ void x_rowrun(const SplitArgs& a, int k, int cbeg, in
     for (int q = 0; q < 4; ++q) a.forcing[q * a.plane + row + dst[t]] = a.forcing[q * a.plane + row + src[t]];
   }
   double v0[4] = {0, 0, 0, 0}, v1[4] = {0, 0, 0, 0};
-  if (cbeg < cend) load_stage(cbeg * kXCells, v0, v1);
+  if (cbeg < cend) {
+    load_stage(cbeg * kXCells, v0, v1);
+    store_stage(0, v0, v1);
+  }
+  __syncthreads();
   for (int chunk = cbeg; chunk < cend; ++chunk) {
+    const int b = (chunk - cbeg) & 1;
     const int x0 = chunk * kXCells;
     const int i = x0 + t;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) sm.sS[q][t] = from_f64(v0[q]);
-    if (t < kXTile - kXThreads) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) sm.sS[q][t + kXThreads] = from_f64(v1[q]);
-    }
-    __syncthreads();
     const bool upd = t < kXCells && i < a.nx;
     const long long o = row + i + kHs;
     double iv[4];
@@ -270,35 +317,39 @@ __device__ __forceinline__ void x_rowrun(const SplitArgs& a, int k, int cbeg, in
 #pragma unroll
       for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
     }
-    if (chunk + 1 < cend) load_stage(x0 + kXCells, v0, v1);
+    const bool more = chunk + 1 < cend;
+    if (more) load_stage(x0 + kXCells, v0, v1);
     if (i <= a.nx) {
-      dw s[4][4];
+      dw2 s[2][4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q)
+      for (int pr = 0; pr < 2; ++pr)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) s[q][j] = sm.sS[q][t + j];
-      dw F[4];
-      flux_x_split(s, sm.row, hv12, F);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) sm.sF[q][t] = F[q];
+        for (int j = 0; j < 4; ++j) s[pr][j] = sm.sS[b][pr][t + j];
+      dw2 F[2];
+      flux_x2(s, sm.row, hv, F);
+      sm.sF[b][0][t] = F[0];
+      sm.sF[b][1][t] = F[1];
     }
+    if (more) store_stage(b ^ 1, v0, v1);
     __syncthreads();
     if (upd) {
-      dw dF[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) dF[q] = sub(sm.sF[q][t], sm.sF[q][t + 1]);
-      if (a.srcw) dF[WMOM] = add(dF[WMOM], mul(from_f64(a.srcw[(long long)k * a.nx + i]), d12));
-#pragma unroll
-      for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = update(iv[q], dF[q], a.c12);
+      dw2 dF[2] = {sub2(sm.sF[b][0][t], sm.sF[b][0][t + 1]), sub2(sm.sF[b][1][t], sm.sF[b][1][t + 1])};
+      if (a.srcw) {
+        const dw w = add(lo_of(dF[1]), mul(from_f64(a.srcw[(long long)k * a.nx + i]), d12));
+        dF[1].h.x = w.h;
+        dF[1].l.x = w.l;
+      }
+      store_update(a, o, iv, dF);
     }
   }
   __syncthreads();
 }
 
 // z: columns [cb*128, cb*128+128), rows [z0, z0+zt): one thread per column
-// marching the rows with a rolling window; the next row and the init values
-// are loaded one step ahead.  halo: write the wall halo rows of these columns
-// of the forcing array (cb == 0 also does the four x-halo columns).
+// marching the rows with a rolling window of variable pairs; the next row and
+// the init values are loaded one step ahead.  halo: write the wall halo rows
+// of these columns of the forcing array (cb == 0 also does the four x-halo
+// columns).
 __device__ __forceinline__ void z_tile(const SplitArgs& a, int cb, int z0, int zt, bool halo, SmemZ& sm) {
   const int z1 = min(z0 + zt, a.nz);
   for (int r = threadIdx.x; r <= z1 - z0; r += kZThreads) {
@@ -314,17 +365,24 @@ __device__ __forceinline__ void z_tile(const SplitArgs& a, int cb, int z0, int z
   if (c < a.nx) {
     const int col = c + kHs;
     if (halo) write_z_halo_column(a, col);
-    const dw hv12 = ld(a.hv12), d12 = ld(a.d12), gz12 = ld(a.gz12);
-    dw w[4][4];
+    const Hv2 hv = make_hv2(ld(a.hv12));
+    const dw d12 = ld(a.d12), gz12 = ld(a.gz12);
+    dw2 w[2][4];
 #pragma unroll
-    for (int j = 0; j < 4; ++j)
+    for (int j = 0; j < 4; ++j) {
+      double v[4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) w[q][j] = from_f64(zval64(a, q, z0 - 2 + j, col));
+      for (int q = 0; q < 4; ++q) v[q] = zval64(a, q, z0 - 2 + j, col);
+      dw2 p[2];
+      pack4(v, p);
+      w[0][j] = p[0];
+      w[1][j] = p[1];
+    }
     double nxt[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) nxt[q] = zval64(a, q, z0 + 2, col);
-    dw Fp[4];
-    flux_z_split(w, sm.row[0], hv12, z0 == 0, Fp);
+    dw2 Fp[2];
+    flux_z2(w, sm.row[0], hv, z0 == 0, Fp);
     for (int k = z0; k < z1; ++k) {
       const long long o = (long long)(k + kHs) * a.pitch + col;
       double iv[4];
@@ -337,25 +395,29 @@ __device__ __forceinline__ void z_tile(const SplitArgs& a, int cb, int z0, int z
 #pragma unroll
         for (int q = 0; q < 4; ++q) nxt[q] = zval64(a, q, k + 3, col);
       }
-      const dw rho_k = w[DENS][2];
+      const dw rho_k = lo_of(w[0][2]);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        w[q][0] = w[q][1];
-        w[q][1] = w[q][2];
-        w[q][2] = w[q][3];
-        w[q][3] = from_f64(cur[q]);
+      for (int pr = 0; pr < 2; ++pr) {
+        w[pr][0] = w[pr][1];
+        w[pr][1] = w[pr][2];
+        w[pr][2] = w[pr][3];
       }
-      dw Fn[4];
-      flux_z_split(w, sm.row[k + 1 - z0], hv12, k + 1 == a.nz, Fn);
-      dw dF[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) dF[q] = sub(Fp[q], Fn[q]);
-      dF[WMOM] = sub(dF[WMOM], mul(rho_k, gz12));
-      if (a.srcw) dF[WMOM] = add(dF[WMOM], mul(from_f64(a.srcw[(long long)k * a.nx + c]), d12));
-#pragma unroll
-      for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = update(iv[q], dF[q], a.c12);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) Fp[q] = Fn[q];
+      {
+        dw2 p[2];
+        pack4(cur, p);
+        w[0][3] = p[0];
+        w[1][3] = p[1];
+      }
+      dw2 Fn[2];
+      flux_z2(w, sm.row[k + 1 - z0], hv, k + 1 == a.nz, Fn);
+      dw2 dF[2] = {sub2(Fp[0], Fn[0]), sub2(Fp[1], Fn[1])};
+      dw dw_w = sub(lo_of(dF[1]), mul(rho_k, gz12));
+      if (a.srcw) dw_w = add(dw_w, mul(from_f64(a.srcw[(long long)k * a.nx + c]), d12));
+      dF[1].h.x = dw_w.h;
+      dF[1].l.x = dw_w.l;
+      store_update(a, o, iv, dF);
+      Fp[0] = Fn[0];
+      Fp[1] = Fn[1];
     }
   }
   __syncthreads();
@@ -372,7 +434,7 @@ __global__ void __launch_bounds__(kXThreads) k_stage_x_split(SplitArgs a) {
   for (int k = blockIdx.y; k < a.nz; k += gridDim.y) x_rowrun(a, k, cbeg, cend, halo, sm);
 }
 
-__global__ void __launch_bounds__(kZThreads, 6) k_stage_z_split(SplitArgs a) {
+__global__ void __launch_bounds__(kZThreads, MW_ZSPLIT_MIN_BLOCKS) k_stage_z_split(SplitArgs a) {
   __shared__ SmemZ sm;
   z_tile(a, blockIdx.x, blockIdx.y * a.z_tile, a.z_tile, (a.flags & MW_FLAG_WRITE_HALO) && blockIdx.y == 0, sm);
 }
@@ -418,7 +480,7 @@ __global__ void __launch_bounds__(kXThreads) k_ens_x_split(EnsStage es) {
   }
 }
 
-__global__ void __launch_bounds__(kZThreads, 6) k_ens_z_split(EnsStage es) {
+__global__ void __launch_bounds__(kZThreads, MW_ZSPLIT_MIN_BLOCKS) k_ens_z_split(EnsStage es) {
   __shared__ SmemZ sm;
   for (int it = blockIdx.x; it < es.n_items; it += gridDim.x) {
     const int2 item = es.items[it];  // (member, column block + ncb * tile)
