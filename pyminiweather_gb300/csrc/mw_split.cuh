@@ -141,6 +141,24 @@ __device__ __forceinline__ double f2d(float f) {
 // parts span at most 53 bits, which holds for normalised pairs).
 __device__ __forceinline__ double to_f64(dw x) { return f2d(x.h) + f2d(x.l); }
 
+// The float's sign, exponent field and significand placed in a double without
+// rebiasing the exponent: the double's value is exactly f * 2^-896 for every
+// normal float, and 0 for zero (subnormal floats become values below 2^-1022,
+// i.e. negligible).  Three integer operations; callers fold 2^896 into an FP64
+// constant.  Inf / NaN are not preserved (see to_f64_scaled).
+__device__ __forceinline__ double f2d_scaled(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned hi = ((u >> 3) & 0x0fffffffu) | (u & 0x80000000u);
+  return __longlong_as_double((long long)(((unsigned long long)hi << 32) | (u << 29)));
+}
+
+// (h + l) * 2^-896 as an FP64 value (one FP64 add); NaN when h is Inf or NaN.
+__device__ __forceinline__ double to_f64_scaled(dw x) {
+  const double v = f2d_scaled(x.h) + f2d_scaled(x.l);
+  return (__float_as_uint(x.h) & 0x7f800000u) == 0x7f800000u ? __longlong_as_double(0x7ff8000000000000LL) : v;
+}
+constexpr double kTwoPow896 = 5.28294531135665246352339629e+269;  // 2^896
+
 // FP64 -> FP32 rounded to nearest (ties away), by integer operations.
 __device__ __forceinline__ float d2f(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);

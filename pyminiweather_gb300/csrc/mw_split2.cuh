@@ -20,21 +20,12 @@ struct dw2 {
   float2 h, l;
 };
 
-__device__ __forceinline__ unsigned long long f2_bits(float2 a) {
-  return ((unsigned long long)__float_as_uint(a.y) << 32) | __float_as_uint(a.x);
-}
-__device__ __forceinline__ float2 f2_from(unsigned long long b) {
-  return make_float2(__uint_as_float((unsigned)b), __uint_as_float((unsigned)(b >> 32)));
-}
-
 __device__ __forceinline__ float2 f2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 f2mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 f2sub(float2 a, float2 b) {
-  unsigned long long d;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
-  return f2_from(d);
-}
+// a - b = RN(b * -1 + a): a packed FMA rounds once, exactly like a subtraction
+// (there is no packed subtract intrinsic).
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
 __device__ __forceinline__ float2 f2splat(float v) { return make_float2(v, v); }
 
 __device__ __forceinline__ dw2 two_sum2(float2 a, float2 b) {
@@ -73,7 +64,7 @@ __device__ __forceinline__ dw2 mul2n(dw2 x, dw2 y, float2 ny_h) {
   return fast_two_sum2(p, e);
 }
 __device__ __forceinline__ dw2 mul2(dw2 x, dw2 y) {
-  return mul2n(x, y, f2sub(make_float2(0.f, 0.f), y.h));
+  return mul2n(x, y, f2mul(y.h, make_float2(-1.f, -1.f)));
 }
 
 __device__ __forceinline__ dw2 pack(dw a, dw b) { return {make_float2(a.h, b.h), make_float2(a.l, b.l)}; }

@@ -20,6 +20,9 @@
 // double-FP32 (the FP32 rounding of a Horner partial sum y_k reaches the
 // result scaled by |delta|^(k-1)).  For |delta| <= 1/8, degree 16 with terms
 // 7..16 in FP32; beyond that, expm1(gamma log1p(delta)) in FP64.
+#include <algorithm>
+#include <atomic>
+
 #include "mw_common.cuh"
 #include "mw_ensemble.cuh"
 #include "mw_split.cuh"
@@ -58,13 +61,14 @@ constexpr int kXTile = kXThreads + 3;  // cells x0-2 .. x0+256
 #ifndef MW_ZSPLIT_MIN_BLOCKS
 #define MW_ZSPLIT_MIN_BLOCKS 5  // z CTAs per SM the register allocation must allow
 #endif
-#ifndef MW_ZSPLIT_TILE
-#define MW_ZSPLIT_TILE 64
-#endif
 constexpr int kZThreads = 128;
-constexpr int kZTile = MW_ZSPLIT_TILE;
-constexpr int kZTileMax = 64;
-constexpr int kXBlocksPerRow = 2;  // x CTAs per row; each walks a run of chunks
+constexpr int kZTileMax = 64;  // rows per shared-memory row-constant table
+constexpr int kZMinRows = 8;   // single grid: fewest rows per z CTA
+// Single-grid x: warps walk 31-cell segments independently (32 interfaces each).
+constexpr int kWCells = 31;
+constexpr int kWVals = kWCells + 4;  // staged cells x0-2 .. x0+32
+constexpr int kXWarps = kXThreads / 32;
+constexpr int kXRowsMax = 64;        // rows of one x CTA's range (row-constant table)
 
 struct RowS {
   dw R;    // 12 * background rho
@@ -86,10 +90,8 @@ struct SplitArgs {
   double* forcing;
   double* out;
   unsigned flags;
-  int chunks_per_block;  // x: 255-cell chunks walked by one CTA
-  int z_tile;            // z: rows per CTA
   dwc hv12;              // 12 * hv
-  double c12;            // dt_stage / (12 d): out = init + c12 * (F(i) - F(i+1))
+  double c12s;           // 2^896 dt_stage / (12 d): out = init + c12s * 2^-896 (F(i) - F(i+1))
   dwc d12;               // 12 d (source term: dt * src = c12 * 12 d * src)
   dwc gz12;              // 12 dz grav (z gravity term: dt g rho' = c12 * 12 dz g rho')
 };
@@ -224,9 +226,9 @@ __device__ __forceinline__ void write_z_halo_column(const SplitArgs& a, int col)
   }
 }
 
-// out = init + c12 (F(i) - F(i+1)): one FP64 add (merging the pair) and one
-// FP64 FMA per value.
-__device__ __forceinline__ double update(double init, dw dF, double c12) { return fma(c12, to_f64(dF), init); }
+// out = init + c12 (F(i) - F(i+1)): one FP64 add (merging the pair, scaled by
+// 2^-896) and one FP64 FMA per value; c12s = c12 * 2^896 undoes the scale.
+__device__ __forceinline__ double update(double init, dw dF, double c12s) { return fma(c12s, to_f64_scaled(dF), init); }
 
 // ---------------------------------------------------------------------------
 // Tiles.  Both the single-grid kernels and the persistent ensemble kernels
@@ -251,7 +253,7 @@ __device__ __forceinline__ void pack4(const double v[4], dw2 out[2]) {
 __device__ __forceinline__ void store_update(const SplitArgs& a, long long o, const double iv[4], dw2 dF[2]) {
   const dw d[4] = {lo_of(dF[0]), hi_of(dF[0]), lo_of(dF[1]), hi_of(dF[1])};
 #pragma unroll
-  for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = update(iv[q], d[q], a.c12);
+  for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = update(iv[q], d[q], a.c12s);
 }
 
 // x: row k, chunks [cbeg, cend) of 255 cells.  Per chunk: the 259 forcing
@@ -345,98 +347,217 @@ __device__ __forceinline__ void x_rowrun(const SplitArgs& a, int k, int cbeg, in
   __syncthreads();
 }
 
-// z: columns [cb*128, cb*128+128), rows [z0, z0+zt): one thread per column
-// marching the rows with a rolling window of variable pairs; the next row and
-// the init values are loaded one step ahead.  halo: write the wall halo rows
-// of these columns of the forcing array (cb == 0 also does the four x-halo
-// columns).
-__device__ __forceinline__ void z_tile(const SplitArgs& a, int cb, int z0, int zt, bool halo, SmemZ& sm) {
-  const int z1 = min(z0 + zt, a.nz);
-  for (int r = threadIdx.x; r <= z1 - z0; r += kZThreads) {
-    const int k = z0 + r;
+// x, single grid: the CTA owns the contiguous range [g0, g1) of the row-major
+// list of 31-cell segments (nseg per row) and splits it evenly over its eight
+// warps.  Each warp walks its segments with no CTA barrier: lane l stages cell
+// x0-2+l (lanes 0..2 also x0+30+l) in its own shared-memory slice, evaluates
+// the flux at interface x0+l, and lanes 0..30 update cells x0..x0+30 from the
+// fluxes of their own and the next lane's interface.  The next segment's
+// values are loaded one segment ahead.  The row constants (an FP64 pow per
+// row) are formed once per CTA for all rows of its range.
+struct SmemXW {
+  dw2 sS[kXWarps][2][kWVals + 1];  // [warp][pair][staged cell]
+  dw2 sF[kXWarps][2][32];          // [warp][pair][interface]
+  RowS row[kXRowsMax];
+};
+
+__device__ __forceinline__ RowS x_row_consts(const SplitArgs& a, int k) {
+  const double hrt = a.hytc[k + kHs];
+  return row_consts(a.hyc[k + kHs], hrt, kC0 * pow(hrt, kGamma));
+}
+
+__device__ __forceinline__ void x_warp_segments(const SplitArgs& a, int nseg, long long g0, long long g1, int row0,
+                                                bool halo, SmemXW& sm) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (g0 >= g1) return;
+  const Hv2 hv = make_hv2(ld(a.hv12));
+  const dw d12 = ld(a.d12);
+  int k = (int)(g0 / nseg), sg = (int)(g0 - (long long)k * nseg);
+  auto load = [&](int kk, int x0, double v0[4], double v1[4]) {
+    const long long row = (long long)(kk + kHs) * a.pitch;
+    const int c0 = x0 - 2 + lane, c1 = x0 + 30 + lane;
+    if (c0 <= a.nx + 1) {
+      const long long col = wrap_x(c0, a.nx) + kHs;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) v0[q] = __ldg(a.forcing + q * a.plane + row + col);
+    }
+    if (lane < 3 && c1 <= a.nx + 1) {
+      const long long col = wrap_x(c1, a.nx) + kHs;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) v1[q] = __ldg(a.forcing + q * a.plane + row + col);
+    }
+  };
+  double v0[4] = {0, 0, 0, 0}, v1[4] = {0, 0, 0, 0};
+  load(k, sg * kWCells, v0, v1);
+  for (long long g = g0; g < g1; ++g) {
+    const int x0 = sg * kWCells;
+    const long long row = (long long)(k + kHs) * a.pitch;
+    {
+      dw2 p[2];
+      pack4(v0, p);
+      sm.sS[w][0][lane] = p[0];
+      sm.sS[w][1][lane] = p[1];
+      if (lane < 3) {
+        pack4(v1, p);
+        sm.sS[w][0][32 + lane] = p[0];
+        sm.sS[w][1][32 + lane] = p[1];
+      }
+    }
+    if (halo && sg == 0 && lane < 4) {  // columns 0, 1 <- nx, nx+1; nx+2, nx+3 <- 2, 3
+      const int dst = lane < 2 ? lane : a.nx + lane, src = lane < 2 ? a.nx + lane : lane;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) a.forcing[q * a.plane + row + dst] = a.forcing[q * a.plane + row + src];
+    }
+    const int kc = k;
+    const int i = x0 + lane;
+    const bool upd = lane < kWCells && i < a.nx;
+    const long long o = row + i + kHs;
+    if (++sg == nseg) {
+      sg = 0;
+      ++k;
+    }
+    const bool more = g + 1 < g1;
+    if (more) load(k, sg * kWCells, v0, v1);
+    double iv[4];
+    if (upd) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
+    }
+    __syncwarp();
+    if (i <= a.nx) {
+      dw2 s[2][4];
+#pragma unroll
+      for (int pr = 0; pr < 2; ++pr)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) s[pr][j] = sm.sS[w][pr][lane + j];
+      dw2 F[2];
+      flux_x2(s, sm.row[kc - row0], hv, F);
+      sm.sF[w][0][lane] = F[0];
+      sm.sF[w][1][lane] = F[1];
+    }
+    __syncwarp();
+    if (upd) {
+      dw2 dF[2] = {sub2(sm.sF[w][0][lane], sm.sF[w][0][lane + 1]), sub2(sm.sF[w][1][lane], sm.sF[w][1][lane + 1])};
+      if (a.srcw) {
+        const dw ws = add(lo_of(dF[1]), mul(from_f64(a.srcw[(long long)kc * a.nx + i]), d12));
+        dF[1].h.x = ws.h;
+        dF[1].l.x = ws.l;
+      }
+      store_update(a, o, iv, dF);
+    }
+    __syncwarp();
+  }
+}
+
+// z: columns [cb*128, cb*128+128), rows [kbeg, kend), kend - kbeg <=
+// kZTileMax: one thread per column marching the rows with a rolling window of
+// variable pairs; the next row and the init values are loaded one step ahead;
+// the interface row constants are tabled in shared memory.  halo: write the
+// wall halo rows of these columns of the forcing array (cb == 0 also does the
+// four x-halo columns).
+__device__ __forceinline__ void z_march(const SplitArgs& a, int cb, int kbeg, int kend, bool halo, SmemZ& sm) {
+  __syncthreads();  // the previous table is no longer read
+  for (int r = threadIdx.x; r <= kend - kbeg; r += kZThreads) {
+    const int k = kbeg + r;
     sm.row[r] = row_consts(a.hyi[k], a.hyti[k], a.hypi[k]);
   }
   __syncthreads();
   const int c = cb * kZThreads + threadIdx.x;
-  if (halo && cb == 0 && threadIdx.x < 4) {
-    const int hcol[4] = {0, 1, a.nx + kHs, a.nx + kHs + 1};
-    write_z_halo_column(a, hcol[threadIdx.x]);
+  if (halo && cb == 0 && threadIdx.x < 4) write_z_halo_column(a, threadIdx.x < 2 ? threadIdx.x : a.nx + threadIdx.x);
+  if (c >= a.nx) return;
+  const int col = c + kHs;
+  if (halo) write_z_halo_column(a, col);
+  const Hv2 hv = make_hv2(ld(a.hv12));
+  const dw d12 = ld(a.d12), gz12 = ld(a.gz12);
+  dw2 w[2][4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    double v[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) v[q] = zval64(a, q, kbeg - 2 + j, col);
+    dw2 p[2];
+    pack4(v, p);
+    w[0][j] = p[0];
+    w[1][j] = p[1];
   }
-  if (c < a.nx) {
-    const int col = c + kHs;
-    if (halo) write_z_halo_column(a, col);
-    const Hv2 hv = make_hv2(ld(a.hv12));
-    const dw d12 = ld(a.d12), gz12 = ld(a.gz12);
-    dw2 w[2][4];
+  double nxt[4];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      double v[4];
+  for (int q = 0; q < 4; ++q) nxt[q] = zval64(a, q, kbeg + 2, col);
+  dw2 Fp[2];
+  flux_z2(w, sm.row[0], hv, kbeg == 0, Fp);
+  for (int k = kbeg; k < kend; ++k) {
+    const long long o = (long long)(k + kHs) * a.pitch + col;
+    double iv[4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) v[q] = zval64(a, q, z0 - 2 + j, col);
+    for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
+    double cur[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) cur[q] = nxt[q];
+    if (k + 1 < kend) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) nxt[q] = zval64(a, q, k + 3, col);
+    }
+    const dw rho_k = lo_of(w[0][2]);
+#pragma unroll
+    for (int pr = 0; pr < 2; ++pr) {
+      w[pr][0] = w[pr][1];
+      w[pr][1] = w[pr][2];
+      w[pr][2] = w[pr][3];
+    }
+    {
       dw2 p[2];
-      pack4(v, p);
-      w[0][j] = p[0];
-      w[1][j] = p[1];
+      pack4(cur, p);
+      w[0][3] = p[0];
+      w[1][3] = p[1];
     }
-    double nxt[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) nxt[q] = zval64(a, q, z0 + 2, col);
-    dw2 Fp[2];
-    flux_z2(w, sm.row[0], hv, z0 == 0, Fp);
-    for (int k = z0; k < z1; ++k) {
-      const long long o = (long long)(k + kHs) * a.pitch + col;
-      double iv[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
-      double cur[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) cur[q] = nxt[q];
-      if (k + 1 < z1) {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) nxt[q] = zval64(a, q, k + 3, col);
-      }
-      const dw rho_k = lo_of(w[0][2]);
-#pragma unroll
-      for (int pr = 0; pr < 2; ++pr) {
-        w[pr][0] = w[pr][1];
-        w[pr][1] = w[pr][2];
-        w[pr][2] = w[pr][3];
-      }
-      {
-        dw2 p[2];
-        pack4(cur, p);
-        w[0][3] = p[0];
-        w[1][3] = p[1];
-      }
-      dw2 Fn[2];
-      flux_z2(w, sm.row[k + 1 - z0], hv, k + 1 == a.nz, Fn);
-      dw2 dF[2] = {sub2(Fp[0], Fn[0]), sub2(Fp[1], Fn[1])};
-      dw dw_w = sub(lo_of(dF[1]), mul(rho_k, gz12));
-      if (a.srcw) dw_w = add(dw_w, mul(from_f64(a.srcw[(long long)k * a.nx + c]), d12));
-      dF[1].h.x = dw_w.h;
-      dF[1].l.x = dw_w.l;
-      store_update(a, o, iv, dF);
-      Fp[0] = Fn[0];
-      Fp[1] = Fn[1];
-    }
+    dw2 Fn[2];
+    flux_z2(w, sm.row[k + 1 - kbeg], hv, k + 1 == a.nz, Fn);
+    dw2 dF[2] = {sub2(Fp[0], Fn[0]), sub2(Fp[1], Fn[1])};
+    dw dw_w = sub(lo_of(dF[1]), mul(rho_k, gz12));
+    if (a.srcw) dw_w = add(dw_w, mul(from_f64(a.srcw[(long long)k * a.nx + c]), d12));
+    dF[1].h.x = dw_w.h;
+    dF[1].l.x = dw_w.l;
+    store_update(a, o, iv, dF);
+    Fp[0] = Fn[0];
+    Fp[1] = Fn[1];
   }
-  __syncthreads();
 }
 
 // ---------------------------------------------------------------------------
 // Single grid: x CTA (blockIdx.x, row) walks a run of chunks; z CTA is one tile.
-__global__ void __launch_bounds__(kXThreads) k_stage_x_split(SplitArgs a) {
-  __shared__ SmemX sm;
-  const int nchunks = (a.nx + kXCells - 1) / kXCells;
-  const int cbeg = blockIdx.x * a.chunks_per_block;
-  const int cend = min(cbeg + a.chunks_per_block, nchunks);
-  const bool halo = (a.flags & MW_FLAG_WRITE_HALO) && blockIdx.x == 0;
-  for (int k = blockIdx.y; k < a.nz; k += gridDim.y) x_rowrun(a, k, cbeg, cend, halo, sm);
+#ifndef MW_XSPLIT_SEGS_PER_WARP
+#define MW_XSPLIT_SEGS_PER_WARP 32  // segments per warp (0: one resident wave of CTAs)
+#endif
+#ifndef MW_XSPLIT_MIN_BLOCKS
+#define MW_XSPLIT_MIN_BLOCKS 3
+#endif
+__global__ void __launch_bounds__(kXThreads, MW_XSPLIT_MIN_BLOCKS) k_stage_x_split(SplitArgs a, int nseg, long long total) {
+  __shared__ SmemXW sm;
+  const long long g0 = total * blockIdx.x / gridDim.x, g1 = total * (blockIdx.x + 1) / gridDim.x;
+  if (g0 >= g1) return;
+  const int row0 = (int)(g0 / nseg), nrows = (int)((g1 - 1) / nseg) - row0 + 1;  // nrows <= kXRowsMax (host)
+  for (int r = threadIdx.x; r < nrows; r += kXThreads) sm.row[r] = x_row_consts(a, row0 + r);
+  __syncthreads();
+  const int w = threadIdx.x >> 5;
+  const long long n = g1 - g0;
+  x_warp_segments(a, nseg, g0 + n * w / kXWarps, g0 + n * (w + 1) / kXWarps, row0, a.flags & MW_FLAG_WRITE_HALO, sm);
 }
 
-__global__ void __launch_bounds__(kZThreads, MW_ZSPLIT_MIN_BLOCKS) k_stage_z_split(SplitArgs a) {
+// z, single grid: the CTA owns the contiguous range [u0, u1) of the
+// column-block-major list of (column block, row) units, at most kZTileMax
+// units, so it marches one or two column-block pieces.  The launch sizes the
+// grid to a whole number of resident waves of equal ranges.
+__global__ void __launch_bounds__(kZThreads, MW_ZSPLIT_MIN_BLOCKS) k_stage_z_split(SplitArgs a, int ncb) {
   __shared__ SmemZ sm;
-  z_tile(a, blockIdx.x, blockIdx.y * a.z_tile, a.z_tile, (a.flags & MW_FLAG_WRITE_HALO) && blockIdx.y == 0, sm);
+  const long long U = (long long)ncb * a.nz;
+  long long u = U * blockIdx.x / gridDim.x;
+  const long long u1 = U * (blockIdx.x + 1) / gridDim.x;
+  while (u < u1) {
+    const int cb = (int)(u / a.nz), k0 = (int)(u - (long long)cb * a.nz);
+    const int kend = (int)std::min<long long>(a.nz, k0 + (u1 - u));
+    z_march(a, cb, k0, kend, (a.flags & MW_FLAG_WRITE_HALO) && k0 == 0, sm);
+    u += kend - k0;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -459,13 +580,11 @@ __device__ SplitArgs member_args(const EnsStage& es, int e) {
   a.forcing = es.forcing + m.state_off;
   a.out = es.out + m.state_off;
   a.flags = es.flags;
-  a.chunks_per_block = 0;
-  a.z_tile = es.z_tile;
   const double d = es.direction == MW_DIR_X ? m.dx : m.dz;
   const double dts = m.dt / (double)es.stage_div;  // dt/3, dt/2, dt/1 as evolve forms them
   const double hv = -kHvBeta * d / (16 * m.dt);
   a.hv12 = split_rn(12.0 * hv);
-  a.c12 = dts / (12.0 * d);
+  a.c12s = dts / (12.0 * d) * kTwoPow896;  // exact: a power-of-two scale
   a.d12 = split_rn(12.0 * d);
   a.gz12 = split_rn(12.0 * m.dz * kGrav);
   return a;
@@ -487,7 +606,7 @@ __global__ void __launch_bounds__(kZThreads, MW_ZSPLIT_MIN_BLOCKS) k_ens_z_split
     const SplitArgs a = member_args(es, item.x);
     const int ncb = (a.nx + kZThreads - 1) / kZThreads;
     const int cb = item.y % ncb, tile = item.y / ncb;
-    z_tile(a, cb, tile * es.z_tile, es.z_tile, (a.flags & MW_FLAG_WRITE_HALO) && tile == 0, sm);
+    z_march(a, cb, tile * es.z_tile, min((tile + 1) * es.z_tile, a.nz), (a.flags & MW_FLAG_WRITE_HALO) && tile == 0, sm);
   }
 }
 
@@ -507,6 +626,24 @@ int ens_split_occupancy(int direction, int* blocks_per_sm) {
                       ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_ens_x_split, kXThreads, 0)
                       : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_ens_z_split, kZThreads, 0);
   if (e != cudaSuccess) return fail(MW_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
+  return MW_OK;
+}
+
+// CTAs of k_stage_x_split (which 0) / k_stage_z_split (which 1) resident on
+// the current device, cached per device.
+int resident_ctas(int which, int* out) {
+  static std::atomic<int> cache[2][64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return fail(MW_ERR_CUDA, "cudaGetDevice failed");
+  const bool cached = dev >= 0 && dev < 64;
+  if (cached && (*out = cache[which][dev].load(std::memory_order_relaxed)) > 0) return MW_OK;
+  int per_sm = 0, sms = 0;
+  cudaError_t e = which == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage_x_split, kXThreads, 0)
+                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage_z_split, kZThreads, 0);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return fail(MW_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
+  *out = std::max(1, per_sm) * sms;
+  if (cached) cache[which][dev].store(*out, std::memory_order_relaxed);
   return MW_OK;
 }
 
@@ -533,18 +670,34 @@ int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, con
   const double d = direction == MW_DIR_X ? dx : dz;
   const double hv = -kHvBeta * d / (16 * dt_full);
   a.hv12 = split_host(12.0 * hv);
-  a.c12 = dt_stage / (12.0 * d);
+  a.c12s = dt_stage / (12.0 * d) * kTwoPow896;  // exact: a power-of-two scale
+  MW_REQUIRE(std::isfinite(a.c12s), MW_ERR_INVALID_ARG,
+             "dt_stage / (12 d) = %g is above the split form's range (use the native FP64 mode)", dt_stage / (12.0 * d));
   a.d12 = split_host(12.0 * d);
   a.gz12 = split_host(12.0 * dz * kGrav);
-  const int nchunks = (nx + kXCells - 1) / kXCells;
-  a.chunks_per_block = (nchunks + kXBlocksPerRow - 1) / kXBlocksPerRow;
-  a.z_tile = z_tile_rows(nx, nz, kZThreads, kZTile);
   if (direction == MW_DIR_X) {
-    dim3 grid((nchunks + a.chunks_per_block - 1) / a.chunks_per_block, (unsigned)min(nz, 65535));
-    k_stage_x_split<<<grid, kXThreads, 0, stream>>>(a);
+    const int nseg = (nx + kWCells - 1) / kWCells;
+    const long long total = (long long)nseg * nz;
+    int resident = 0, st = resident_ctas(0, &resident);
+    if (st) return st;
+    // One resident wave (at least one segment per warp) for small grids;
+    // MW_XSPLIT_SEGS_PER_WARP segments per warp for large ones, so that the
+    // block scheduler evens out the warps' speeds; at most kXRowsMax rows per
+    // CTA range.
+    long long grid = std::min<long long>(resident, (total + kXWarps - 1) / kXWarps);
+    if (MW_XSPLIT_SEGS_PER_WARP > 0) grid = std::max<long long>(grid, total / (kXWarps * MW_XSPLIT_SEGS_PER_WARP));
+    grid = std::max<long long>(grid, (nz + kXRowsMax - 3) / (kXRowsMax - 2));
+    MW_REQUIRE(grid <= 0x7fffffffLL, MW_ERR_SHAPE, "grid too large for the x direction-stage launch");
+    k_stage_x_split<<<(unsigned)grid, kXThreads, 0, stream>>>(a, nseg, total);
   } else {
-    dim3 grid((nx + kZThreads - 1) / kZThreads, (nz + a.z_tile - 1) / a.z_tile);
-    k_stage_z_split<<<grid, kZThreads, 0, stream>>>(a);
+    const int ncb = (nx + kZThreads - 1) / kZThreads;
+    const long long units = (long long)ncb * nz;
+    int resident = 0, st = resident_ctas(1, &resident);
+    if (st) return st;
+    long long grid = resident * ((units + (long long)kZTileMax * resident - 1) / ((long long)kZTileMax * resident));
+    grid = std::max<long long>(1, std::min<long long>(grid, units / kZMinRows));
+    MW_REQUIRE(grid <= 0x7fffffffLL, MW_ERR_SHAPE, "grid too large for the z direction-stage launch");
+    k_stage_z_split<<<(unsigned)grid, kZThreads, 0, stream>>>(a, ncb);
   }
   return check_launch(direction == MW_DIR_X ? "x split direction-stage launch" : "z split direction-stage launch");
 }
