@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define MW_ABI_VERSION 1
+#define MW_ABI_VERSION 2
 
 enum mw_status {
   MW_OK = 0,
@@ -188,14 +188,17 @@ int mw_ensemble_step_f32(const void* plan_device, const mw_ens_plan_info* info, 
  * (a halo value's adjoint returns to the cell it was copied or scaled from),
  * the hyperviscosity and the gravity term.  Arrays are (4, nz+4, nx+4) FP64;
  * a base may be g_dst itself (accumulation); g_dst must not overlap g_out or
- * forcing.  FP64 arithmetic.  workspace: mw_dirstage_vjp_workspace_bytes.
+ * forcing.  f64_mode: MW_F64_NATIVE (FP64 arithmetic, two kernels) or
+ * MW_F64_SPLIT (double-FP32 interior arithmetic as the split forward, one
+ * kernel after a small background-table kernel).
+ * workspace: mw_dirstage_vjp_workspace_bytes.
  * ------------------------------------------------------------------------- */
 size_t mw_dirstage_vjp_workspace_bytes(int nx, int nz);
 int mw_dirstage_vjp_f64(int nx, int nz, double dx, double dz, double dt_full, const double* hy_dens_cell,
                         const double* hy_dens_theta_cell, const double* hy_dens_int, const double* hy_dens_theta_int,
                         const double* hy_pressure_int, const double* forcing, const double* g_out,
                         const double* g_base_a, const double* g_base_b, int add_g_out, double* g_dst, double dt_stage,
-                        int direction, void* workspace, size_t workspace_bytes, void* stream);
+                        int direction, int f64_mode, void* workspace, size_t workspace_bytes, void* stream);
 
 /* One time step (as mw_step_f64 with nsteps = 1) that also keeps its six
  * stage forcing states in `stages` (6 state arrays, contiguous): for the two
@@ -207,11 +210,12 @@ int mw_step_record_f64(int nx, int nz, double dx, double dz, double dt_full, dou
                        double* state_out, int reverse, int f64_mode, void* stream);
 /* Adjoint of one time step recorded by mw_step_record_f64: g_in = dJ/d(state_in)
  * from g_out = dJ/d(state_out) (both (4, nz+4, nx+4), halo 0).  gbuf: 3 state
- * arrays of work space (contiguous); g_in may equal g_out. */
+ * arrays of work space (contiguous); g_in may equal g_out.  f64_mode as for
+ * mw_dirstage_vjp_f64. */
 int mw_step_vjp_f64(int nx, int nz, double dx, double dz, double dt_full, double dt, const double* hy_dens_cell,
                     const double* hy_dens_theta_cell, const double* hy_dens_int, const double* hy_dens_theta_int,
                     const double* hy_pressure_int, const double* stages, const double* g_out, double* g_in,
-                    double* gbuf, int reverse, void* workspace, size_t workspace_bytes, void* stream);
+                    double* gbuf, int reverse, int f64_mode, void* workspace, size_t workspace_bytes, void* stream);
 
 /* ---------------------------------------------------------------------------
  * Initial condition: replaces init (pyminiweather/ics/initial.py:11-105):

@@ -42,9 +42,9 @@ _SIGNATURES = {
     "mw_ensemble_step_f32": [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _i, ctypes.POINTER(_i), _u, _i, _i, _P],
     "mw_ensemble_occupancy": [_i, _i, ctypes.POINTER(_i)],
     "mw_dirstage_vjp_workspace_bytes": [_i, _i],
-    "mw_dirstage_vjp_f64": [_i, _i, _d, _d, _d, _P, _P, _P, _P, _P, _P, _P, _P, _P, _i, _P, _d, _i, _P, _sz, _P],
+    "mw_dirstage_vjp_f64": [_i, _i, _d, _d, _d, _P, _P, _P, _P, _P, _P, _P, _P, _P, _i, _P, _d, _i, _i, _P, _sz, _P],
     "mw_step_record_f64": [_i, _i, _d, _d, _d, _d, _P, _P, _P, _P, _P, _P, _P, _P, _P, _i, _i, _P],
-    "mw_step_vjp_f64": [_i, _i, _d, _d, _d, _d, _P, _P, _P, _P, _P, _P, _P, _P, _P, _i, _P, _sz, _P],
+    "mw_step_vjp_f64": [_i, _i, _d, _d, _d, _d, _P, _P, _P, _P, _P, _P, _P, _P, _P, _i, _i, _P, _sz, _P],
     "mw_init_f64": [_i, _i, _d, _d, _i, _d, _i, _P, _P, _P, _P, _P, _P, _P, _P],
     "mw_init_f32": [_i, _i, _d, _d, _i, _d, _i, _P, _P, _P, _P, _P, _P, _P, _P],
     "mw_gravity_source_f64": [_i, _i, _d, _d, _P, _P, _P],

@@ -6,7 +6,8 @@ tensor) by ctx.nsteps steps and is differentiable: its backward pass replays
 the forward from checkpoints stored every ctx.ckpt_every steps, keeps the six
 stage states of each step of a segment, and runs the hand-written
 vector-Jacobian product of each direction-stage (mw_dirstage_vjp_f64) in
-reverse.  For one direction (RK3 of solve/step.py:112-141):
+reverse, in the arithmetic of the forward's f64_mode (FP64, or double-FP32
+for the split form).  For one direction (RK3 of solve/step.py:112-141):
 
     s1 = S + dt/3 L(S),  s2 = S + dt/2 L(s1),  S' = S + dt L(s2)
 
@@ -111,7 +112,7 @@ class Rollout(torch.autograd.Function):
                 rev = not rev
             for j in reversed(range(n)):
                 _native.call("mw_step_vjp_f64", *common, _native.ptr(buf.stages[6 * j * N:]), _native.ptr(g),
-                             _native.ptr(g), _native.ptr(buf.gbuf), int(revs[j]), _native.ptr(buf.ws),
+                             _native.ptr(g), _native.ptr(buf.gbuf), int(revs[j]), f64_mode(p), _native.ptr(buf.ws),
                              buf.ws.numel() * 8, stream)
         g[:, :2, :].zero_()
         g[:, -2:, :].zero_()

@@ -206,6 +206,15 @@ long long n_interfaces(int nx, int nz, int dir) {
 }
 
 }  // namespace
+
+// mw_adjoint_split.cu
+int launch_vjp_row_table(int nx, int nz, const double* hyc, const double* hytc, const double* hyi, const double* hyti,
+                         const double* hypi, void* workspace, cudaStream_t stream);
+int launch_vjp_split(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const void* table,
+                     const double* forcing, const double* g_out, const double* g_base_a, const double* g_base_b,
+                     int add_g_out, double* g_dst, double dt_stage, int direction, cudaStream_t stream);
+size_t vjp_split_table_bytes(int nz);
+
 }  // namespace mw
 
 using namespace mw;
@@ -213,14 +222,16 @@ using namespace mw;
 extern "C" size_t mw_dirstage_vjp_workspace_bytes(int nx, int nz) {
   if (nx < 1 || nz < 1) return 0;
   const long long n = std::max(n_interfaces(nx, nz, MW_DIR_X), n_interfaces(nx, nz, MW_DIR_Z));
-  return sizeof(double) * 8 * (size_t)n;
+  return std::max(sizeof(double) * 8 * (size_t)n, vjp_split_table_bytes(nz));
 }
 
-extern "C" int mw_dirstage_vjp_f64(int nx, int nz, double dx, double dz, double dt_full, const double* hyc,
-                                   const double* hytc, const double* hyi, const double* hyti, const double* hypi,
-                                   const double* forcing, const double* g_out, const double* g_base_a,
-                                   const double* g_base_b, int add_g_out, double* g_dst, double dt_stage,
-                                   int direction, void* workspace, size_t workspace_bytes, void* stream) {
+// Checks and launches one stage VJP; split mode expects the background table
+// (launch_vjp_row_table) in the workspace when table_ready, else writes it.
+static int vjp_stage(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
+                     const double* hyi, const double* hyti, const double* hypi, const double* forcing,
+                     const double* g_out, const double* g_base_a, const double* g_base_b, int add_g_out,
+                     double* g_dst, double dt_stage, int direction, int f64_mode, bool table_ready, void* workspace,
+                     size_t workspace_bytes, void* stream) {
   int st = check_grid(nx, nz);
   if (st) return st;
   MW_REQUIRE(finite_pos(dx) && finite_pos(dz) && finite_pos(dt_full), MW_ERR_INVALID_ARG,
@@ -237,9 +248,17 @@ extern "C" int mw_dirstage_vjp_f64(int nx, int nz, double dx, double dz, double 
   MW_REQUIRE((!g_base_a || g_base_a == g_dst || !ranges_overlap(g_dst, bytes, g_base_a, bytes)) &&
                  (!g_base_b || g_base_b == g_dst || !ranges_overlap(g_dst, bytes, g_base_b, bytes)),
              MW_ERR_ALIAS, "a base array must equal g_dst or not overlap it");
+  MW_REQUIRE(f64_mode == MW_F64_NATIVE || f64_mode == MW_F64_SPLIT, MW_ERR_INVALID_ARG,
+             "f64_mode must be MW_F64_NATIVE or MW_F64_SPLIT");
   const size_t need = mw_dirstage_vjp_workspace_bytes(nx, nz);
   MW_REQUIRE(workspace_bytes >= need, MW_ERR_WORKSPACE, "vjp workspace needs %zu bytes, got %zu", need,
              workspace_bytes);
+  if (f64_mode == MW_F64_SPLIT) {
+    if (!table_ready && (st = launch_vjp_row_table(nx, nz, hyc, hytc, hyi, hyti, hypi, workspace, (cudaStream_t)stream)))
+      return st;
+    return launch_vjp_split(nx, nz, dx, dz, dt_full, hyc, workspace, forcing, g_out, g_base_a, g_base_b, add_g_out,
+                            g_dst, dt_stage, direction, (cudaStream_t)stream);
+  }
   const Geom g = make_geom(nx, nz);
   VjpArgs a;
   a.nx = nx;
@@ -275,6 +294,16 @@ extern "C" int mw_dirstage_vjp_f64(int nx, int nz, double dx, double dz, double 
   return check_launch("vjp gather launch");
 }
 
+extern "C" int mw_dirstage_vjp_f64(int nx, int nz, double dx, double dz, double dt_full, const double* hyc,
+                                   const double* hytc, const double* hyi, const double* hyti, const double* hypi,
+                                   const double* forcing, const double* g_out, const double* g_base_a,
+                                   const double* g_base_b, int add_g_out, double* g_dst, double dt_stage,
+                                   int direction, int f64_mode, void* workspace, size_t workspace_bytes,
+                                   void* stream) {
+  return vjp_stage(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, forcing, g_out, g_base_a, g_base_b, add_g_out,
+                   g_dst, dt_stage, direction, f64_mode, false, workspace, workspace_bytes, stream);
+}
+
 // ---------------------------------------------------------------------------
 // Adjoint of one recorded time step (stages from mw_step_record_f64).  Per
 // direction, in reverse (RK3 of solve/step.py:112-141):
@@ -282,7 +311,7 @@ extern "C" int mw_dirstage_vjp_f64(int nx, int nz, double dx, double dz, double 
 extern "C" int mw_step_vjp_f64(int nx, int nz, double dx, double dz, double dt_full, double dt, const double* hyc,
                                const double* hytc, const double* hyi, const double* hyti, const double* hypi,
                                const double* stages, const double* g_out, double* g_in, double* gbuf, int reverse,
-                               void* workspace, size_t workspace_bytes, void* stream) {
+                               int f64_mode, void* workspace, size_t workspace_bytes, void* stream) {
   MW_REQUIRE(stages && g_out && g_in && gbuf, MW_ERR_INVALID_ARG, "NULL pointer argument");
   MW_REQUIRE(finite_pos(dt), MW_ERR_INVALID_ARG, "dt must be finite and positive");
   const size_t n = 4 * (size_t)make_geom(nx, nz).plane;
@@ -295,19 +324,21 @@ extern "C" int mw_step_vjp_f64(int nx, int nz, double dx, double dz, double dt_f
   const int dirs[2] = {reverse ? MW_DIR_X : MW_DIR_Z, reverse ? MW_DIR_Z : MW_DIR_X};
   const double* cur = g_out;
   int st;
+  bool ready = false;  // split mode: the background table is written by the first stage call
   for (int d = 1; d >= 0; --d) {
     const double* S = stages + (3 * d) * n;
     const double* s1 = S + n;
     const double* s2 = S + 2 * n;
     double* out = d == 1 ? gC : g_in;
-    if ((st = mw_dirstage_vjp_f64(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, s2, cur, nullptr, nullptr, 0, gA,
-                                  dt, dirs[d], workspace, workspace_bytes, stream)))
+    if ((st = vjp_stage(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, s2, cur, nullptr, nullptr, 0, gA, dt,
+                        dirs[d], f64_mode, ready, workspace, workspace_bytes, stream)))
       return st;
-    if ((st = mw_dirstage_vjp_f64(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, s1, gA, nullptr, nullptr, 0, gB,
-                                  dt / 2, dirs[d], workspace, workspace_bytes, stream)))
+    ready = true;
+    if ((st = vjp_stage(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, s1, gA, nullptr, nullptr, 0, gB, dt / 2,
+                        dirs[d], f64_mode, ready, workspace, workspace_bytes, stream)))
       return st;
-    if ((st = mw_dirstage_vjp_f64(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, S, gB, cur, gA, 1, out, dt / 3,
-                                  dirs[d], workspace, workspace_bytes, stream)))
+    if ((st = vjp_stage(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, S, gB, cur, gA, 1, out, dt / 3, dirs[d],
+                        f64_mode, ready, workspace, workspace_bytes, stream)))
       return st;
     cur = out;
   }

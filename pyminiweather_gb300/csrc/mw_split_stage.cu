@@ -6,20 +6,12 @@
 // interpolation, fluxes, pressure and flux divergence run on the FP32 pipe;
 // the stage update out = init + increment is one FP64 add per value.
 //
-// Quantities are carried scaled by 12 so that the 4-point interpolation
-// (-s0 + 7 s1 + 7 s2 - s3)/12 needs no division: A = 12 vals, and the
-// background terms, pressure and hyperviscosity coefficient are scaled to
-// match; the flux divergence is multiplied by dt / (12 d).
-//
-// Pressure: P_row ((1 + delta)^gamma - 1), delta = (rho theta)' / (rho theta)_bg,
-// with P_row = C0 (rho theta)_bg^gamma.  In z this is the reference's
-// p - hy_pressure_int (interpolate.py:163-165); in x the row constant cancels
-// in the flux difference.  (1 + delta)^gamma - 1 is the binomial series
-// sum_n C(gamma, n) delta^n.  For |delta| <= 1/64 (most cells) degree 8 leaves
-// a tail below 2^-56 relative; terms 4..8 are summed in FP32, 1..3 in
-// double-FP32 (the FP32 rounding of a Horner partial sum y_k reaches the
-// result scaled by |delta|^(k-1)).  For |delta| <= 1/8, degree 16 with terms
-// 7..16 in FP32; beyond that, expm1(gamma log1p(delta)) in FP64.
+// Quantities are carried scaled by 12 (mw_split_flux.cuh): A = 12 vals, and
+// the background terms, pressure and hyperviscosity coefficient are scaled to
+// match; the flux divergence is multiplied by dt / (12 d).  Pressure is
+// P_row ((1 + delta)^gamma - 1) with P_row = C0 (rho theta)_bg^gamma: in z the
+// reference's p - hy_pressure_int (interpolate.py:163-165); in x the row
+// constant cancels in the flux difference.
 #include <algorithm>
 #include <atomic>
 
@@ -27,33 +19,12 @@
 #include "mw_ensemble.cuh"
 #include "mw_split.cuh"
 #include "mw_split2.cuh"
+#include "mw_split_flux.cuh"
 
 namespace mw {
 using namespace split;
 
 namespace {
-
-constexpr double binom_gamma(int n) {
-  double c = kGamma;
-  for (int k = 1; k < n; ++k) c = c * (kGamma - k) / (k + 1);
-  return c;
-}
-constexpr float hi_of(double v) { return (float)v; }
-constexpr float lo_of(double v) { return (float)(v - (double)(float)v); }
-
-__constant__ float c_pow_h[7] = {0.f,
-                                 hi_of(binom_gamma(1)), hi_of(binom_gamma(2)), hi_of(binom_gamma(3)),
-                                 hi_of(binom_gamma(4)), hi_of(binom_gamma(5)), hi_of(binom_gamma(6))};
-__constant__ float c_pow_l[7] = {0.f,
-                                 lo_of(binom_gamma(1)), lo_of(binom_gamma(2)), lo_of(binom_gamma(3)),
-                                 lo_of(binom_gamma(4)), lo_of(binom_gamma(5)), lo_of(binom_gamma(6))};
-__constant__ float c_pow_f[17] = {0.f,
-                                  (float)binom_gamma(1), (float)binom_gamma(2), (float)binom_gamma(3),
-                                  (float)binom_gamma(4), (float)binom_gamma(5), (float)binom_gamma(6),
-                                  (float)binom_gamma(7), (float)binom_gamma(8), (float)binom_gamma(9),
-                                  (float)binom_gamma(10), (float)binom_gamma(11), (float)binom_gamma(12),
-                                  (float)binom_gamma(13), (float)binom_gamma(14), (float)binom_gamma(15),
-                                  (float)binom_gamma(16)};
 
 constexpr int kXThreads = 256;
 constexpr int kXCells = kXThreads - 1;
@@ -69,13 +40,6 @@ constexpr int kWCells = 31;
 constexpr int kWVals = kWCells + 4;  // staged cells x0-2 .. x0+32
 constexpr int kXWarps = kXThreads / 32;
 constexpr int kXRowsMax = 64;        // rows of one x CTA's range (row-constant table)
-
-struct RowS {
-  dw R;    // 12 * background rho
-  dw RT;   // 12 * background rho*theta
-  dw IRT;  // 1 / (12 * background rho*theta)
-  dw P12;  // 12 * background pressure
-};
 
 struct SplitArgs {
   int nx, nz, pitch;
@@ -95,115 +59,6 @@ struct SplitArgs {
   dwc d12;               // 12 d (source term: dt * src = c12 * 12 d * src)
   dwc gz12;              // 12 dz grav (z gravity term: dt g rho' = c12 * 12 dz g rho')
 };
-
-// (1 + d)^gamma - 1
-__device__ __forceinline__ dw pgm1(dw d) {
-  const float ad = fabsf(d.h);
-  const float df = d.h;
-  if (ad <= 0.015625f) {
-    float t = fmaf(c_pow_f[8], df, c_pow_f[7]);
-    t = fmaf(t, df, c_pow_f[6]);
-    t = fmaf(t, df, c_pow_f[5]);
-    t = fmaf(t, df, c_pow_f[4]);
-    dw y = add(mulf(d, t), dw{c_pow_h[3], c_pow_l[3]});
-    y = add(mul(y, d), dw{c_pow_h[2], c_pow_l[2]});
-    y = add(mul(y, d), dw{c_pow_h[1], c_pow_l[1]});
-    return mul(y, d);
-  }
-  if (ad <= 0.125f) {
-    float t = c_pow_f[16];
-#pragma unroll
-    for (int n = 15; n >= 7; --n) t = fmaf(t, df, c_pow_f[n]);
-    dw y = add(mulf(d, t), dw{c_pow_h[6], c_pow_l[6]});
-#pragma unroll
-    for (int n = 5; n >= 1; --n) y = add(mul(y, d), dw{c_pow_h[n], c_pow_l[n]});
-    return mul(y, d);
-  }
-  const double dd = to_f64(d);
-  return from_f64(expm1(kGamma * log1p(dd)));
-}
-
-// 12 * (4-point interpolation) = 7 (s1 + s2) - (s0 + s3) and the third
-// difference (s3 - s0) - 3 (s2 - s1), for a pair of variables at once.  The
-// leading floats are combined with error-free transformations (exact), the
-// trailing floats and the rounding errors are summed in FP32 (error about
-// 2^-48 of the operands), and each result is renormalised once.
-__device__ __forceinline__ void interp2(dw2 s0, dw2 s1, dw2 s2, dw2 s3, dw2& A, dw2& D) {
-  const float2 c7 = f2splat(7.0f), m7 = f2splat(-7.0f), c3 = f2splat(3.0f), m3 = f2splat(-3.0f);
-  const dw2 a = two_sum2(s1.h, s2.h);
-  const dw2 b = two_sum2(s0.h, s3.h);
-  const float2 a7 = f2mul(a.h, c7);
-  const float2 a7e = f2fma(a.h, c7, f2mul(a.h, m7));  // exact: 7 a.h - a7
-  const dw2 r = two_diff2(a7, b.h);
-  const float2 lo = f2add(f2sub(f2fma(c7, f2add(f2add(s1.l, s2.l), a.l), a7e), f2add(f2add(s0.l, s3.l), b.l)), r.l);
-  A = fast_two_sum2(r.h, lo);
-  const dw2 p = two_diff2(s3.h, s0.h);
-  const dw2 q = two_diff2(s2.h, s1.h);
-  const float2 q3 = f2mul(q.h, c3);
-  const float2 q3e = f2fma(q.h, c3, f2mul(q.h, m3));
-  const dw2 t = two_diff2(p.h, q3);
-  const float2 lo2 =
-      f2add(f2sub(f2add(f2sub(s3.l, s0.l), p.l), f2fma(c3, f2add(f2sub(s2.l, s1.l), q.l), q3e)), t.l);
-  D = fast_two_sum2(t.h, lo2);
-}
-
-// Hyperviscosity constant in paired form: HV = 12 hv in both lanes, nHV its negated leading float.
-struct Hv2 {
-  dw2 v;
-  float2 nh;
-};
-__device__ __forceinline__ Hv2 make_hv2(dw hv12) { return {splat(hv12), f2splat(-hv12.h)}; }
-
-// x flux times 12 (interpolate.py:105-129) for the taps s[pair][j], pairs
-// (DENS, UMOM) and (WMOM, RHOT).  With u = (rho u)'/rho:
-// F = ((rho u)', u (rho u)' + p', u (rho w)', u (rho theta)) - hv d3.
-__device__ __forceinline__ void flux_x2(const dw2 s[2][4], const RowS& r, const Hv2& hv, dw2 F[2]) {
-  dw2 A[2], D[2];
-  interp2(s[0][0], s[0][1], s[0][2], s[0][3], A[0], D[0]);
-  interp2(s[1][0], s[1][1], s[1][2], s[1][3], A[1], D[1]);
-  const dw AD = lo_of(A[0]), AU = hi_of(A[0]), AW = lo_of(A[1]), AT = hi_of(A[1]);
-  const dw ri = rcp(add(AD, r.R));
-  const dw u = mul(AU, ri);
-  const dw pp = mul(r.P12, pgm1(mul(AT, r.IRT)));
-  const dw2 uu = mul2(splat(u), pack(AU, AW));
-  const dw X1 = add(lo_of(uu), pp);
-  const dw X3 = mul(u, add(AT, r.RT));
-  F[0] = sub2(pack(AU, X1), mul2n(D[0], hv.v, hv.nh));
-  F[1] = sub2(pack(hi_of(uu), X3), mul2n(D[1], hv.v, hv.nh));
-}
-
-// z flux times 12 (interpolate.py:153-186); w and d3[DENS] vanish at the walls.
-__device__ __forceinline__ void flux_z2(const dw2 s[2][4], const RowS& r, const Hv2& hv, bool wall, dw2 F[2]) {
-  dw2 A[2], D[2];
-  interp2(s[0][0], s[0][1], s[0][2], s[0][3], A[0], D[0]);
-  interp2(s[1][0], s[1][1], s[1][2], s[1][3], A[1], D[1]);
-  const dw AD = lo_of(A[0]), AU = hi_of(A[0]), AT = hi_of(A[1]);
-  dw rw = lo_of(A[1]);
-  if (wall) {
-    rw = dw{0.f, 0.f};
-    D[0].h.x = 0.f;
-    D[0].l.x = 0.f;
-  }
-  const dw ri = rcp(add(AD, r.R));
-  const dw pp = mul(r.P12, pgm1(mul(AT, r.IRT)));
-  const dw w = mul(rw, ri);
-  const dw2 ww = mul2(splat(w), pack(AU, rw));
-  const dw X2 = add(hi_of(ww), pp);
-  const dw X3 = mul(w, add(AT, r.RT));
-  F[0] = sub2(pack(rw, lo_of(ww)), mul2n(D[0], hv.v, hv.nh));
-  F[1] = sub2(pack(X2, X3), mul2n(D[1], hv.v, hv.nh));
-}
-
-__device__ __forceinline__ RowS row_consts(double hy_r, double hy_rt, double P) {
-  RowS r;
-  r.R = from_f64(12.0 * hy_r);
-  r.RT = from_f64(12.0 * hy_rt);
-  r.IRT = from_f64(1.0 / (12.0 * hy_rt));
-  r.P12 = from_f64(12.0 * P);
-  return r;
-}
-
-__device__ __forceinline__ int wrap_x(int j, int nx) { return j < 0 ? j + nx : (j >= nx ? j - nx : j); }
 
 __device__ __forceinline__ double zval64(const SplitArgs& a, int q, int k, int col) {
   if (k >= 0 && k < a.nz) return a.forcing[q * a.plane + (long long)(k + kHs) * a.pitch + col];
@@ -242,11 +97,6 @@ struct SmemX {
 struct SmemZ {
   RowS row[kZTileMax + 1];
 };
-
-__device__ __forceinline__ void pack4(const double v[4], dw2 out[2]) {
-  out[0] = pack(from_f64(v[DENS]), from_f64(v[UMOM]));
-  out[1] = pack(from_f64(v[WMOM]), from_f64(v[RHOT]));
-}
 
 // out = init + c12 (F(i) - F(i+1)) for the four variables (paired differences,
 // then per value one FP64 add merging the pair and one FP64 FMA).

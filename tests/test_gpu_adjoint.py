@@ -30,10 +30,12 @@ def _bg(f):
     return [a for a in f.backgrounds()]
 
 
+@pytest.mark.parametrize("mode", [0, 1])
 @pytest.mark.parametrize("direction", [0, 1])
-def test_stage_vjp_matches_autograd(direction):
+def test_stage_vjp_matches_autograd(direction, mode):
     """One direction-stage: g_forcing = dt (dL/dforcing)^T g_out, against
-    torch autograd of the pure-PyTorch tendency."""
+    torch autograd of the pure-PyTorch tendency, in FP64 (mode 0) and
+    double-FP32 (mode 1) arithmetic."""
     torch.manual_seed(0)
     p, f = _fields(40, 24, "collision")
     evolve(dict(p, f64_mode="native"), f, None, dt=p["dt"], nsteps=3)  # a developed state
@@ -46,7 +48,7 @@ def test_stage_vjp_matches_autograd(direction):
                      device=s.device)
     hb = [_native.ptr(a) for a in f.backgrounds()]
     _native.call("mw_dirstage_vjp_f64", 40, 24, p["dx"], p["dz"], p["dt"], *hb, _native.ptr(s), _native.ptr(g),
-                 None, None, 0, _native.ptr(out), dts, direction, _native.ptr(ws), ws.numel() * 8,
+                 None, None, 0, _native.ptr(out), dts, direction, mode, _native.ptr(ws), ws.numel() * 8,
                  _native.stream_handle())
     x = s[:, 2:-2, 2:-2].clone().requires_grad_(True)
     L = TS.tendency_x(x, _bg(f), p["dx"], p["dt"]) if direction == 0 else TS.tendency_z(x, _bg(f), p["dz"], p["dt"])
@@ -54,14 +56,50 @@ def test_stage_vjp_matches_autograd(direction):
     got = out[:, 2:-2, 2:-2]
     for v in range(4):
         err = float((got[v] - ref[v]).abs().max() / ref[v].abs().max().clamp_min(1e-300))
-        assert err <= 1e-12, (direction, v, err)
-    assert float(out[:, :2].abs().max()) == 0.0  # halo of the adjoint is zero
+        assert err <= (1e-12 if mode == 0 else 1e-11), (direction, mode, v, err)
+    assert float(out[:, :2].abs().max()) == 0.0 and float(out[:, -2:].abs().max()) == 0.0  # halo rows
+    assert float(out[:, :, :2].abs().max()) == 0.0 and float(out[:, :, -2:].abs().max()) == 0.0  # halo columns
 
 
-def test_rollout_gradient_matches_autograd():
+@pytest.mark.parametrize("nx,nz", [(2, 1), (3, 2), (29, 5), (30, 31), (61, 58), (130, 3)])
+@pytest.mark.parametrize("direction", [0, 1])
+def test_stage_vjp_split_matches_native(nx, nz, direction):
+    """The double-FP32 stage adjoint against the FP64 one on ragged grids
+    (segment edges, one-row and two-column grids, both walls in one segment),
+    with bases and accumulation of g_out."""
+    p, f = _fields(nx, nz, "collision")
+    evolve(dict(p, f64_mode="native"), f, None, dt=p["dt"], nsteps=2)
+    s = f.state.clone()
+    gen = torch.Generator(device="cpu").manual_seed(nx * 100 + nz + direction)
+    g, ba, bb = (torch.zeros_like(s) for _ in range(3))
+    for a in (g, ba, bb):
+        a[:, 2:-2, 2:-2] = torch.randn(4, nz, nx, generator=gen, dtype=torch.float64).to(s.device)
+    ws = torch.empty(int(_native.load().mw_dirstage_vjp_workspace_bytes(nx, nz)) // 8 + 1, dtype=torch.float64,
+                     device=s.device)
+    hb = [_native.ptr(a) for a in f.backgrounds()]
+    outs = []
+    for mode in (0, 1):
+        out = torch.full_like(s, 7.0)
+        _native.call("mw_dirstage_vjp_f64", nx, nz, p["dx"], p["dz"], p["dt"], *hb, _native.ptr(s), _native.ptr(g),
+                     _native.ptr(ba), _native.ptr(bb), 1, _native.ptr(out), p["dt"] / 3, direction, mode,
+                     _native.ptr(ws), ws.numel() * 8, _native.stream_handle())
+        outs.append(out)
+    torch.cuda.synchronize()
+    ref, got = outs
+    inc_ref = ref[:, 2:-2, 2:-2] - (g + ba + bb)[:, 2:-2, 2:-2]
+    inc_got = got[:, 2:-2, 2:-2] - (g + ba + bb)[:, 2:-2, 2:-2]
+    for v in range(4):
+        err = float((inc_got[v] - inc_ref[v]).abs().max() / inc_ref[v].abs().max().clamp_min(1e-300))
+        assert err <= 1e-11, (nx, nz, direction, v, err)
+    assert torch.equal(got[:, :2], torch.zeros_like(got[:, :2])) and torch.equal(got[:, :, -2:], torch.zeros_like(got[:, :, -2:]))
+
+
+@pytest.mark.parametrize("mode", ["native", "split"])
+def test_rollout_gradient_matches_autograd(mode):
     """Gradient of the upper-half (rho theta)' misfit after 12 steps w.r.t. all
-    four initial fields: hand-written adjoint (checkpoints every 5 steps)
-    against autograd through the pure-PyTorch step."""
+    four initial fields: hand-written adjoint (checkpoints every 5 steps; FP64
+    or double-FP32 forward and adjoint) against autograd through the
+    pure-PyTorch step."""
     nx, nz, steps = 48, 24, 12
     p, f = _fields(nx, nz, amp=3.0)
     _, ft = _fields(nx, nz, amp=3.5)
@@ -69,14 +107,14 @@ def test_rollout_gradient_matches_autograd():
     evolve(dict(p, f64_mode="native"), ft, None, dt=p["dt"], nsteps=steps)
     target = ft.state.clone()
     x0 = f.state.clone().requires_grad_(True)
-    ctx = RolloutContext(params=dict(p, f64_mode="native"), fields=f, nsteps=steps, ckpt_every=5)
+    ctx = RolloutContext(params=dict(p, f64_mode=mode), fields=f, nsteps=steps, ckpt_every=5)
     loss = upper_half_rhot_misfit(rollout(x0, ctx), target, nz)
     (g,) = torch.autograd.grad(loss, x0)
     xi = f.state[:, 2:-2, 2:-2].clone().requires_grad_(True)
     s, _ = TS.evolve_interior(xi, _bg(f), p, steps)
     d = s[3, nz // 2:, :] - target[3, 2 + nz // 2:2 + nz, 2:-2]
     (gr,) = torch.autograd.grad((d * d).sum(), xi)
-    assert abs(float(loss) - float((d * d).sum())) <= 1e-10 * abs(float(loss))
+    assert abs(float(loss) - float((d * d).sum())) <= 1e-9 * abs(float(loss))
     for v in range(4):
         err = float((g[v, 2:-2, 2:-2] - gr[v]).abs().max() / gr[v].abs().max())
         print("field %d: adjoint vs autograd normwise %.2e" % (v, err))
