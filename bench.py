@@ -63,6 +63,21 @@ def dist_env():
     return world, rank, local
 
 
+def replica_max(torch, ms, dist, device):
+    """The slowest rank's time: every rank advances its own replica, so the job
+    ends when the last one does."""
+    if dist is None:
+        return ms
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(world, cells, steps, ms):
+    """Whole-job cell-steps/s: all ranks' cells over the slowest rank's time."""
+    return world * cells * steps / (ms * 1e-3)
+
+
 def load_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -240,9 +255,10 @@ def roofline(per, cells, bytes_per_value, peak, peak_kind, names, traffic_table)
                              "frac": round(algo / (tot[1 - d] / len(per[1 - d]) * 1e-3) / 1e9 / peak, 4)}}
 
 
-def e2e_run(torch, p, f, steps, warmup):
+def e2e_run(torch, p, f, steps, warmup, dist=None):
     """Public API with host buffers: per step, H2D of the state from pinned
-    memory, evolve(), D2H of the state into pinned memory."""
+    memory, evolve(), D2H of the state into pinned memory.  Under torchrun the
+    ranks start together and the caller takes the slowest rank's time."""
     from pyminiweather_gb300.solve import evolve, reset_direction
     h_in = torch.empty(f.state.shape, dtype=f.dtype, pin_memory=True)
     h_out = torch.empty(f.state.shape, dtype=f.dtype, pin_memory=True)
@@ -253,6 +269,8 @@ def e2e_run(torch, p, f, steps, warmup):
         evolve(p, f, None, dt=p["dt"])
         h_out.copy_(f.state, non_blocking=True)
     torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(steps):
@@ -409,12 +427,9 @@ def run_gb300(args):
     clocks.start()
     ms, per, launches = timed_run(torch, _native, p, f, args.steps, args.warmup, dist)
     clk = clocks.stop()
-    ms_t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if dist is not None:
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms = float(ms_t.item())
+    ms = replica_max(torch, ms, dist, "cuda")
     m1 = compute_stats(p, f)[0]
-    value = world * cells * args.steps / (ms * 1e-3)
+    value = job_value(world, cells, args.steps, ms)
     rl = roofline(per, cells, 8, peak, peak_kind, kernel_names(True, args.mode), traffic)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -425,14 +440,23 @@ def run_gb300(args):
             "mass_drift": (m1 - m0) / m0,
             "bytes_per_cell_step": STATE_VALUES_PER_CELL_STEP * 8}
 
-    if not args.no_extras:
+    if not args.no_extras and world > 1:
+        # several GPUs: the end-to-end leg only (the other forms are single-GPU figures)
+        init(f, p)
+        ms_e, nbytes = e2e_run(torch, p, f, args.steps, 1, dist)
+        ms_e = replica_max(torch, ms_e, dist, "cuda")
+        line["e2e"] = {"value": job_value(world, cells, args.steps, ms_e), "unit": UNIT,
+                       "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                       "ms_per_step": ms_e / args.steps, "api": "pyminiweather_gb300.solve.evolve",
+                       "f64_mode": args.mode}
+    elif not args.no_extras:
         # FP32 precision form on the same workload
         del f
         torch.cuda.empty_cache()
         f32 = initialize_fields(p, dtype=torch.float32)
         init(f32, p)
         ms32, per32, _ = timed_run(torch, _native, p, f32, args.steps, args.warmup, None)
-        v32 = world * cells * args.steps / (ms32 * 1e-3)
+        v32 = job_value(world, cells, args.steps, ms32)
         line["fp32"] = {"value": v32, "ms_per_step": ms32 / args.steps, "speedup_vs_fp64": v32 / value,
                         "roofline": roofline(per32, cells, 4, peak, peak_kind, kernel_names(False, "split"), traffic)}
         del f32
@@ -444,7 +468,7 @@ def run_gb300(args):
         init(fo, po)
         ks = max(1, min(args.steps, 3))
         mso, pero, _ = timed_run(torch, _native, po, fo, ks, 1, None)
-        line["fp64_" + other] = {"value": world * cells * ks / (mso * 1e-3), "ms_per_step": mso / ks,
+        line["fp64_" + other] = {"value": job_value(world, cells, ks, mso), "ms_per_step": mso / ks,
                                  "roofline": roofline(pero, cells, 8, peak, peak_kind, kernel_names(True, other),
                                                       traffic)}
         # the batching form (ensemble of uneven grids), FP64 split and FP32
@@ -455,14 +479,13 @@ def run_gb300(args):
         # end to end through the public API with host buffers
         init(fo, p)
         ms_e, nbytes = e2e_run(torch, p, fo, args.steps, 1)
-        line["e2e"] = {"value": world * cells * args.steps / (ms_e * 1e-3), "unit": UNIT,
+        line["e2e"] = {"value": job_value(world, cells, args.steps, ms_e), "unit": UNIT,
                        "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                        "ms_per_step": ms_e / args.steps, "api": "pyminiweather_gb300.solve.evolve",
                        "f64_mode": args.mode}
         del fo
         torch.cuda.empty_cache()
-        if rank == 0 and world == 1:
-            line["cpu_baseline"] = cpu_baseline(args, args.cpu_steps)
+        line["cpu_baseline"] = cpu_baseline(args, args.cpu_steps)
     if dist is not None:
         dist.barrier()
         dist.destroy_process_group()
