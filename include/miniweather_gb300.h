@@ -54,6 +54,9 @@ enum mw_f64_mode {
 /* Flags of the direction-stage and step entry points. */
 #define MW_FLAG_WRITE_HALO 1u /* write the halo cells into the forcing array
                                  as set_bc_x / set_bc_z do (ics/bcs.py:8-148) */
+#define MW_FLAG_INDEX64 2u    /* split form: use the 64-bit-index kernels even
+                                 when 32-bit indices suffice (for testing; arrays
+                                 of 2^31 or more values always use them) */
 
 /* Background profile of the initial condition. */
 enum mw_background {

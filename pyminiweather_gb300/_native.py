@@ -21,6 +21,7 @@ MW_OK = 0
 MW_DIR_X, MW_DIR_Z = 0, 1
 MW_F64_NATIVE, MW_F64_SPLIT = 0, 1
 MW_FLAG_WRITE_HALO = 1
+MW_FLAG_INDEX64 = 2
 MW_BG_CONST_THETA, MW_BG_BVFREQ = 0, 1
 MW_MAX_BUBBLES = 8
 

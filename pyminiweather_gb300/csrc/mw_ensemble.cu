@@ -34,6 +34,8 @@ int check_members(int n, const mw_ens_member* m, int z_tile) {
                "member %d: dx, dz, dt must be finite and positive", e);
     MW_REQUIRE(m[e].state_off >= 0 && m[e].cell_off >= 0 && m[e].int_off >= 0, MW_ERR_INVALID_ARG,
                "member %d: negative offset", e);
+    MW_REQUIRE(4 * make_geom(m[e].nx, m[e].nz).plane < (1LL << 31), MW_ERR_SHAPE,
+               "member %d: a member's state array must hold fewer than 2^31 values", e);
   }
   // members' state blocks must not overlap (each is written by its own items)
   std::vector<int> order(n);

@@ -112,12 +112,9 @@ __device__ __forceinline__ dw from_f64(double x) {
   const unsigned m23 = ((lo & 0x1fffffffu) + 32u) >> 6;
   float h = __uint_as_float(hb);
   float l = __uint_as_float(base + m23) - __uint_as_float(base);
-  if (ex < ((1023u - 100u) << 20)) {
-    h = 0.0f;
-    l = 0.0f;
-  }
-  if (ex > ((1023u + 127u) << 20)) {
-    h = __uint_as_float(0x7fc00000u);
+  // one unsigned range test; the rare out-of-range values take a branch
+  if (ex - ((1023u - 100u) << 20) > ((100u + 127u) << 20)) {
+    h = ex < ((1023u - 100u) << 20) ? 0.0f : __uint_as_float(0x7fc00000u);
     l = 0.0f;
   }
   return {h, l};
@@ -151,6 +148,9 @@ __device__ __forceinline__ double f2d_scaled(float f) {
   const unsigned hi = ((u >> 3) & 0x0fffffffu) | (u & 0x80000000u);
   return __longlong_as_double((long long)(((unsigned long long)hi << 32) | (u << 29)));
 }
+
+// (h + l) * 2^-896 as an FP64 value (one FP64 add), for finite h.
+__device__ __forceinline__ double to_f64_scaled_finite(dw x) { return f2d_scaled(x.h) + f2d_scaled(x.l); }
 
 // (h + l) * 2^-896 as an FP64 value (one FP64 add); NaN when h is Inf or NaN.
 __device__ __forceinline__ double to_f64_scaled(dw x) {

@@ -24,532 +24,29 @@
 namespace mw {
 using namespace split;
 
-namespace {
+namespace s32 {
+typedef int sidx;
+#include "mw_split_stage_impl.cuh"
+}  // namespace s32
 
-constexpr int kXThreads = 256;
-constexpr int kXCells = kXThreads - 1;
-constexpr int kXTile = kXThreads + 3;  // cells x0-2 .. x0+256
-#ifndef MW_ZSPLIT_MIN_BLOCKS
-#define MW_ZSPLIT_MIN_BLOCKS 5  // z CTAs per SM the register allocation must allow
-#endif
-constexpr int kZThreads = 128;
-constexpr int kZTileMax = 64;  // rows per shared-memory row-constant table
-constexpr int kZMinRows = 8;   // single grid: fewest rows per z CTA
-// Single-grid x: warps walk 31-cell segments independently (32 interfaces each).
-constexpr int kWCells = 31;
-constexpr int kWVals = kWCells + 4;  // staged cells x0-2 .. x0+32
-constexpr int kXWarps = kXThreads / 32;
-constexpr int kXRowsMax = 64;        // rows of one x CTA's range (row-constant table)
+namespace s64 {
+typedef long long sidx;
+#include "mw_split_stage_impl.cuh"
+}  // namespace s64
 
-struct SplitArgs {
-  int nx, nz, pitch;
-  long long plane;
-  const double* hyc;
-  const double* hytc;
-  const double* hyi;
-  const double* hyti;
-  const double* hypi;
-  const double* srcw;
-  const double* init;
-  double* forcing;
-  double* out;
-  unsigned flags;
-  dwc hv12;              // 12 * hv
-  double c12s;           // 2^896 dt_stage / (12 d): out = init + c12s * 2^-896 (F(i) - F(i+1))
-  dwc d12;               // 12 d (source term: dt * src = c12 * 12 d * src)
-  dwc gz12;              // 12 dz grav (z gravity term: dt g rho' = c12 * 12 dz g rho')
-};
-
-__device__ __forceinline__ double zval64(const SplitArgs& a, int q, int k, int col) {
-  if (k >= 0 && k < a.nz) return a.forcing[q * a.plane + (long long)(k + kHs) * a.pitch + col];
-  if (q == WMOM) return 0.0;
-  const int src = k < 0 ? kHs : a.nz + kHs - 1;
-  const double s = a.forcing[q * a.plane + (long long)src * a.pitch + col];
-  if (q == UMOM) return s / a.hyc[src] * a.hyc[k + kHs];
-  return s;
-}
-
-__device__ __forceinline__ void write_z_halo_column(const SplitArgs& a, int col) {
-  const int rows[4] = {-2, -1, a.nz, a.nz + 1};
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    double v[4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) v[r] = zval64(a, q, rows[r], col);
-#pragma unroll
-    for (int r = 0; r < 4; ++r) a.forcing[q * a.plane + (long long)(rows[r] + kHs) * a.pitch + col] = v[r];
-  }
-}
-
-// out = init + c12 (F(i) - F(i+1)): one FP64 add (merging the pair, scaled by
-// 2^-896) and one FP64 FMA per value; c12s = c12 * 2^896 undoes the scale.
-__device__ __forceinline__ double update(double init, dw dF, double c12s) { return fma(c12s, to_f64_scaled(dF), init); }
-
-// ---------------------------------------------------------------------------
-// Tiles.  Both the single-grid kernels and the persistent ensemble kernels
-// call these; every thread of the CTA must call them (they contain barriers).
-
-struct SmemX {
-  dw2 sS[2][2][kXTile + 1];  // [buffer][pair][cell]
-  dw2 sF[2][2][kXThreads];   // [buffer][pair][interface]
-  RowS row;
-};
-struct SmemZ {
-  RowS row[kZTileMax + 1];
-};
-
-// out = init + c12 (F(i) - F(i+1)) for the four variables (paired differences,
-// then per value one FP64 add merging the pair and one FP64 FMA).
-__device__ __forceinline__ void store_update(const SplitArgs& a, long long o, const double iv[4], dw2 dF[2]) {
-  const dw d[4] = {lo_of(dF[0]), hi_of(dF[0]), lo_of(dF[1]), hi_of(dF[1])};
-#pragma unroll
-  for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = update(iv[q], d[q], a.c12s);
-}
-
-// x: row k, chunks [cbeg, cend) of 255 cells.  Per chunk: the 259 forcing
-// values, split once, are staged in shared memory as variable pairs; thread
-// t evaluates the flux at interface x0+t and, after one barrier, updates cell
-// x0+t.  Staging and fluxes are double-buffered, so one barrier per chunk
-// suffices; the next chunk's values and this chunk's init values are loaded
-// before the flux evaluation.  The row constants (an FP64 pow) are formed
-// once per call.  halo: write this row's periodic halo into forcing.
-__device__ __forceinline__ void x_rowrun(const SplitArgs& a, int k, int cbeg, int cend, bool halo, SmemX& sm) {
-  const int t = threadIdx.x;
-  const Hv2 hv = make_hv2(ld(a.hv12));
-  const dw d12 = ld(a.d12);
-  const long long row = (long long)(k + kHs) * a.pitch;
-  auto load_stage = [&](int x0, double v0[4], double v1[4]) {
-    const int c0 = x0 - 2 + t, c1 = c0 + kXThreads;
-    if (c0 <= a.nx + 1) {
-      const long long col = wrap_x(c0, a.nx) + kHs;
-#pragma unroll
-      for (int q = 0; q < 4; ++q) v0[q] = __ldg(a.forcing + q * a.plane + row + col);
-    }
-    if (t < kXTile - kXThreads && c1 <= a.nx + 1) {
-      const long long col = wrap_x(c1, a.nx) + kHs;
-#pragma unroll
-      for (int q = 0; q < 4; ++q) v1[q] = __ldg(a.forcing + q * a.plane + row + col);
-    }
-  };
-  auto store_stage = [&](int b, const double v0[4], const double v1[4]) {
-    dw2 p[2];
-    pack4(v0, p);
-    sm.sS[b][0][t] = p[0];
-    sm.sS[b][1][t] = p[1];
-    if (t < kXTile - kXThreads) {
-      pack4(v1, p);
-      sm.sS[b][0][t + kXThreads] = p[0];
-      sm.sS[b][1][t + kXThreads] = p[1];
-    }
-  };
-  if (t == 0) {
-    const double hrt = a.hytc[k + kHs];
-    sm.row = row_consts(a.hyc[k + kHs], hrt, kC0 * pow(hrt, kGamma));
-  }
-  if (halo && t < 4) {
-    const int dst[4] = {0, 1, a.nx + kHs, a.nx + kHs + 1};
-    const int src[4] = {a.nx, a.nx + 1, kHs, kHs + 1};
-#pragma unroll
-    for (int q = 0; q < 4; ++q) a.forcing[q * a.plane + row + dst[t]] = a.forcing[q * a.plane + row + src[t]];
-  }
-  double v0[4] = {0, 0, 0, 0}, v1[4] = {0, 0, 0, 0};
-  if (cbeg < cend) {
-    load_stage(cbeg * kXCells, v0, v1);
-    store_stage(0, v0, v1);
-  }
-  __syncthreads();
-  for (int chunk = cbeg; chunk < cend; ++chunk) {
-    const int b = (chunk - cbeg) & 1;
-    const int x0 = chunk * kXCells;
-    const int i = x0 + t;
-    const bool upd = t < kXCells && i < a.nx;
-    const long long o = row + i + kHs;
-    double iv[4];
-    if (upd) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
-    }
-    const bool more = chunk + 1 < cend;
-    if (more) load_stage(x0 + kXCells, v0, v1);
-    if (i <= a.nx) {
-      dw2 s[2][4];
-#pragma unroll
-      for (int pr = 0; pr < 2; ++pr)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) s[pr][j] = sm.sS[b][pr][t + j];
-      dw2 F[2];
-      flux_x2(s, sm.row, hv, F);
-      sm.sF[b][0][t] = F[0];
-      sm.sF[b][1][t] = F[1];
-    }
-    if (more) store_stage(b ^ 1, v0, v1);
-    __syncthreads();
-    if (upd) {
-      dw2 dF[2] = {sub2(sm.sF[b][0][t], sm.sF[b][0][t + 1]), sub2(sm.sF[b][1][t], sm.sF[b][1][t + 1])};
-      if (a.srcw) {
-        const dw w = add(lo_of(dF[1]), mul(from_f64(a.srcw[(long long)k * a.nx + i]), d12));
-        dF[1].h.x = w.h;
-        dF[1].l.x = w.l;
-      }
-      store_update(a, o, iv, dF);
-    }
-  }
-  __syncthreads();
-}
-
-// x, single grid: the CTA owns the contiguous range [g0, g1) of the row-major
-// list of 31-cell segments (nseg per row) and splits it evenly over its eight
-// warps.  Each warp walks its segments with no CTA barrier: lane l stages cell
-// x0-2+l (lanes 0..2 also x0+30+l) in its own shared-memory slice, evaluates
-// the flux at interface x0+l, and lanes 0..30 update cells x0..x0+30 from the
-// fluxes of their own and the next lane's interface.  The next segment's
-// values are loaded one segment ahead.  The row constants (an FP64 pow per
-// row) are formed once per CTA for all rows of its range.
-struct SmemXW {
-  dw2 sS[kXWarps][2][kWVals + 1];  // [warp][pair][staged cell]
-  dw2 sF[kXWarps][2][32];          // [warp][pair][interface]
-  RowS row[kXRowsMax];
-};
-
-__device__ __forceinline__ RowS x_row_consts(const SplitArgs& a, int k) {
-  const double hrt = a.hytc[k + kHs];
-  return row_consts(a.hyc[k + kHs], hrt, kC0 * pow(hrt, kGamma));
-}
-
-__device__ __forceinline__ void x_warp_segments(const SplitArgs& a, int nseg, long long g0, long long g1, int row0,
-                                                bool halo, SmemXW& sm) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (g0 >= g1) return;
-  const Hv2 hv = make_hv2(ld(a.hv12));
-  const dw d12 = ld(a.d12);
-  int k = (int)(g0 / nseg), sg = (int)(g0 - (long long)k * nseg);
-  auto load = [&](int kk, int x0, double v0[4], double v1[4]) {
-    const long long row = (long long)(kk + kHs) * a.pitch;
-    const int c0 = x0 - 2 + lane, c1 = x0 + 30 + lane;
-    if (c0 <= a.nx + 1) {
-      const long long col = wrap_x(c0, a.nx) + kHs;
-#pragma unroll
-      for (int q = 0; q < 4; ++q) v0[q] = __ldg(a.forcing + q * a.plane + row + col);
-    }
-    if (lane < 3 && c1 <= a.nx + 1) {
-      const long long col = wrap_x(c1, a.nx) + kHs;
-#pragma unroll
-      for (int q = 0; q < 4; ++q) v1[q] = __ldg(a.forcing + q * a.plane + row + col);
-    }
-  };
-  double v0[4] = {0, 0, 0, 0}, v1[4] = {0, 0, 0, 0};
-  load(k, sg * kWCells, v0, v1);
-  for (long long g = g0; g < g1; ++g) {
-    const int x0 = sg * kWCells;
-    const long long row = (long long)(k + kHs) * a.pitch;
-    {
-      dw2 p[2];
-      pack4(v0, p);
-      sm.sS[w][0][lane] = p[0];
-      sm.sS[w][1][lane] = p[1];
-      if (lane < 3) {
-        pack4(v1, p);
-        sm.sS[w][0][32 + lane] = p[0];
-        sm.sS[w][1][32 + lane] = p[1];
-      }
-    }
-    if (halo && sg == 0 && lane < 4) {  // columns 0, 1 <- nx, nx+1; nx+2, nx+3 <- 2, 3
-      const int dst = lane < 2 ? lane : a.nx + lane, src = lane < 2 ? a.nx + lane : lane;
-#pragma unroll
-      for (int q = 0; q < 4; ++q) a.forcing[q * a.plane + row + dst] = a.forcing[q * a.plane + row + src];
-    }
-    const int kc = k;
-    const int i = x0 + lane;
-    const bool upd = lane < kWCells && i < a.nx;
-    const long long o = row + i + kHs;
-    if (++sg == nseg) {
-      sg = 0;
-      ++k;
-    }
-    const bool more = g + 1 < g1;
-    if (more) load(k, sg * kWCells, v0, v1);
-    double iv[4];
-    if (upd) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
-    }
-    __syncwarp();
-    if (i <= a.nx) {
-      dw2 s[2][4];
-#pragma unroll
-      for (int pr = 0; pr < 2; ++pr)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) s[pr][j] = sm.sS[w][pr][lane + j];
-      dw2 F[2];
-      flux_x2(s, sm.row[kc - row0], hv, F);
-      sm.sF[w][0][lane] = F[0];
-      sm.sF[w][1][lane] = F[1];
-    }
-    __syncwarp();
-    if (upd) {
-      dw2 dF[2] = {sub2(sm.sF[w][0][lane], sm.sF[w][0][lane + 1]), sub2(sm.sF[w][1][lane], sm.sF[w][1][lane + 1])};
-      if (a.srcw) {
-        const dw ws = add(lo_of(dF[1]), mul(from_f64(a.srcw[(long long)kc * a.nx + i]), d12));
-        dF[1].h.x = ws.h;
-        dF[1].l.x = ws.l;
-      }
-      store_update(a, o, iv, dF);
-    }
-    __syncwarp();
-  }
-}
-
-// z: columns [cb*128, cb*128+128), rows [kbeg, kend), kend - kbeg <=
-// kZTileMax: one thread per column marching the rows with a rolling window of
-// variable pairs; the next row and the init values are loaded one step ahead;
-// the interface row constants are tabled in shared memory.  halo: write the
-// wall halo rows of these columns of the forcing array (cb == 0 also does the
-// four x-halo columns).
-__device__ __forceinline__ void z_march(const SplitArgs& a, int cb, int kbeg, int kend, bool halo, SmemZ& sm) {
-  __syncthreads();  // the previous table is no longer read
-  for (int r = threadIdx.x; r <= kend - kbeg; r += kZThreads) {
-    const int k = kbeg + r;
-    sm.row[r] = row_consts(a.hyi[k], a.hyti[k], a.hypi[k]);
-  }
-  __syncthreads();
-  const int c = cb * kZThreads + threadIdx.x;
-  if (halo && cb == 0 && threadIdx.x < 4) write_z_halo_column(a, threadIdx.x < 2 ? threadIdx.x : a.nx + threadIdx.x);
-  if (c >= a.nx) return;
-  const int col = c + kHs;
-  if (halo) write_z_halo_column(a, col);
-  const Hv2 hv = make_hv2(ld(a.hv12));
-  const dw d12 = ld(a.d12), gz12 = ld(a.gz12);
-  dw2 w[2][4];
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    double v[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) v[q] = zval64(a, q, kbeg - 2 + j, col);
-    dw2 p[2];
-    pack4(v, p);
-    w[0][j] = p[0];
-    w[1][j] = p[1];
-  }
-  double nxt[4];
-#pragma unroll
-  for (int q = 0; q < 4; ++q) nxt[q] = zval64(a, q, kbeg + 2, col);
-  dw2 Fp[2];
-  flux_z2(w, sm.row[0], hv, kbeg == 0, Fp);
-  for (int k = kbeg; k < kend; ++k) {
-    const long long o = (long long)(k + kHs) * a.pitch + col;
-    double iv[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
-    double cur[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) cur[q] = nxt[q];
-    if (k + 1 < kend) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) nxt[q] = zval64(a, q, k + 3, col);
-    }
-    const dw rho_k = lo_of(w[0][2]);
-#pragma unroll
-    for (int pr = 0; pr < 2; ++pr) {
-      w[pr][0] = w[pr][1];
-      w[pr][1] = w[pr][2];
-      w[pr][2] = w[pr][3];
-    }
-    {
-      dw2 p[2];
-      pack4(cur, p);
-      w[0][3] = p[0];
-      w[1][3] = p[1];
-    }
-    dw2 Fn[2];
-    flux_z2(w, sm.row[k + 1 - kbeg], hv, k + 1 == a.nz, Fn);
-    dw2 dF[2] = {sub2(Fp[0], Fn[0]), sub2(Fp[1], Fn[1])};
-    dw dw_w = sub(lo_of(dF[1]), mul(rho_k, gz12));
-    if (a.srcw) dw_w = add(dw_w, mul(from_f64(a.srcw[(long long)k * a.nx + c]), d12));
-    dF[1].h.x = dw_w.h;
-    dF[1].l.x = dw_w.l;
-    store_update(a, o, iv, dF);
-    Fp[0] = Fn[0];
-    Fp[1] = Fn[1];
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Single grid: x CTA (blockIdx.x, row) walks a run of chunks; z CTA is one tile.
-#ifndef MW_XSPLIT_SEGS_PER_WARP
-#define MW_XSPLIT_SEGS_PER_WARP 32  // segments per warp (0: one resident wave of CTAs)
-#endif
-#ifndef MW_XSPLIT_MIN_BLOCKS
-#define MW_XSPLIT_MIN_BLOCKS 3
-#endif
-__global__ void __launch_bounds__(kXThreads, MW_XSPLIT_MIN_BLOCKS) k_stage_x_split(SplitArgs a, int nseg, long long total) {
-  __shared__ SmemXW sm;
-  const long long g0 = total * blockIdx.x / gridDim.x, g1 = total * (blockIdx.x + 1) / gridDim.x;
-  if (g0 >= g1) return;
-  const int row0 = (int)(g0 / nseg), nrows = (int)((g1 - 1) / nseg) - row0 + 1;  // nrows <= kXRowsMax (host)
-  for (int r = threadIdx.x; r < nrows; r += kXThreads) sm.row[r] = x_row_consts(a, row0 + r);
-  __syncthreads();
-  const int w = threadIdx.x >> 5;
-  const long long n = g1 - g0;
-  x_warp_segments(a, nseg, g0 + n * w / kXWarps, g0 + n * (w + 1) / kXWarps, row0, a.flags & MW_FLAG_WRITE_HALO, sm);
-}
-
-// z, single grid: the CTA owns the contiguous range [u0, u1) of the
-// column-block-major list of (column block, row) units, at most kZTileMax
-// units, so it marches one or two column-block pieces.  The launch sizes the
-// grid to a whole number of resident waves of equal ranges.
-__global__ void __launch_bounds__(kZThreads, MW_ZSPLIT_MIN_BLOCKS) k_stage_z_split(SplitArgs a, int ncb) {
-  __shared__ SmemZ sm;
-  const long long U = (long long)ncb * a.nz;
-  long long u = U * blockIdx.x / gridDim.x;
-  const long long u1 = U * (blockIdx.x + 1) / gridDim.x;
-  while (u < u1) {
-    const int cb = (int)(u / a.nz), k0 = (int)(u - (long long)cb * a.nz);
-    const int kend = (int)std::min<long long>(a.nz, k0 + (u1 - u));
-    z_march(a, cb, k0, kend, (a.flags & MW_FLAG_WRITE_HALO) && k0 == 0, sm);
-    u += kend - k0;
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Ensemble: one persistent launch per stage walks a work list over all
-// members (x: one item per member row; z: one item per member column-tile).
-__device__ SplitArgs member_args(const EnsStage& es, int e) {
-  const mw_ens_member m = es.members[e];
-  SplitArgs a;
-  a.nx = m.nx;
-  a.nz = m.nz;
-  a.pitch = m.nx + 2 * kHs;
-  a.plane = (long long)(m.nz + 2 * kHs) * a.pitch;
-  a.hyc = es.hyc + m.cell_off;
-  a.hytc = es.hytc + m.cell_off;
-  a.hyi = es.hyi + m.int_off;
-  a.hyti = es.hyti + m.int_off;
-  a.hypi = es.hypi + m.int_off;
-  a.srcw = nullptr;
-  a.init = es.init + m.state_off;
-  a.forcing = es.forcing + m.state_off;
-  a.out = es.out + m.state_off;
-  a.flags = es.flags;
-  const double d = es.direction == MW_DIR_X ? m.dx : m.dz;
-  const double dts = m.dt / (double)es.stage_div;  // dt/3, dt/2, dt/1 as evolve forms them
-  const double hv = -kHvBeta * d / (16 * m.dt);
-  a.hv12 = split_rn(12.0 * hv);
-  a.c12s = dts / (12.0 * d) * kTwoPow896;  // exact: a power-of-two scale
-  a.d12 = split_rn(12.0 * d);
-  a.gz12 = split_rn(12.0 * m.dz * kGrav);
-  return a;
-}
-
-__global__ void __launch_bounds__(kXThreads) k_ens_x_split(EnsStage es) {
-  __shared__ SmemX sm;
-  for (int it = blockIdx.x; it < es.n_items; it += gridDim.x) {
-    const int2 item = es.items[it];  // (member, row)
-    const SplitArgs a = member_args(es, item.x);
-    x_rowrun(a, item.y, 0, (a.nx + kXCells - 1) / kXCells, a.flags & MW_FLAG_WRITE_HALO, sm);
-  }
-}
-
-__global__ void __launch_bounds__(kZThreads, MW_ZSPLIT_MIN_BLOCKS) k_ens_z_split(EnsStage es) {
-  __shared__ SmemZ sm;
-  for (int it = blockIdx.x; it < es.n_items; it += gridDim.x) {
-    const int2 item = es.items[it];  // (member, column block + ncb * tile)
-    const SplitArgs a = member_args(es, item.x);
-    const int ncb = (a.nx + kZThreads - 1) / kZThreads;
-    const int cb = item.y % ncb, tile = item.y / ncb;
-    z_march(a, cb, tile * es.z_tile, min((tile + 1) * es.z_tile, a.nz), (a.flags & MW_FLAG_WRITE_HALO) && tile == 0, sm);
-  }
-}
-
-}  // namespace
-
-int launch_ens_split(const EnsStage& es, int grid) {
-  if (es.n_items == 0) return MW_OK;
-  if (es.direction == MW_DIR_X)
-    k_ens_x_split<<<grid, kXThreads, 0, es.stream>>>(es);
-  else
-    k_ens_z_split<<<grid, kZThreads, 0, es.stream>>>(es);
-  return check_launch("ensemble split stage launch");
-}
-
-int ens_split_occupancy(int direction, int* blocks_per_sm) {
-  cudaError_t e = direction == MW_DIR_X
-                      ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_ens_x_split, kXThreads, 0)
-                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_ens_z_split, kZThreads, 0);
-  if (e != cudaSuccess) return fail(MW_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
-  return MW_OK;
-}
-
-// CTAs of k_stage_x_split (which 0) / k_stage_z_split (which 1) resident on
-// the current device, cached per device.
-int resident_ctas(int which, int* out) {
-  static std::atomic<int> cache[2][64];
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return fail(MW_ERR_CUDA, "cudaGetDevice failed");
-  const bool cached = dev >= 0 && dev < 64;
-  if (cached && (*out = cache[which][dev].load(std::memory_order_relaxed)) > 0) return MW_OK;
-  int per_sm = 0, sms = 0;
-  cudaError_t e = which == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage_x_split, kXThreads, 0)
-                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage_z_split, kZThreads, 0);
-  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (e != cudaSuccess) return fail(MW_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
-  *out = std::max(1, per_sm) * sms;
-  if (cached) cache[which][dev].store(*out, std::memory_order_relaxed);
-  return MW_OK;
-}
-
+// Arrays whose four planes span fewer than 2^31 elements take the 32-bit-index kernels.
 int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
                        const double* hyi, const double* hyti, const double* hypi, const double* srcw,
                        const double* init, double* forcing, double* out, double dt_stage, int direction,
                        unsigned flags, cudaStream_t stream) {
-  const Geom g = make_geom(nx, nz);
-  SplitArgs a;
-  a.nx = nx;
-  a.nz = nz;
-  a.pitch = g.pitch;
-  a.plane = g.plane;
-  a.hyc = hyc;
-  a.hytc = hytc;
-  a.hyi = hyi;
-  a.hyti = hyti;
-  a.hypi = hypi;
-  a.srcw = srcw;
-  a.init = init;
-  a.forcing = forcing;
-  a.out = out;
-  a.flags = flags;
-  const double d = direction == MW_DIR_X ? dx : dz;
-  const double hv = -kHvBeta * d / (16 * dt_full);
-  a.hv12 = split_host(12.0 * hv);
-  a.c12s = dt_stage / (12.0 * d) * kTwoPow896;  // exact: a power-of-two scale
-  MW_REQUIRE(std::isfinite(a.c12s), MW_ERR_INVALID_ARG,
-             "dt_stage / (12 d) = %g is above the split form's range (use the native FP64 mode)", dt_stage / (12.0 * d));
-  a.d12 = split_host(12.0 * d);
-  a.gz12 = split_host(12.0 * dz * kGrav);
-  if (direction == MW_DIR_X) {
-    const int nseg = (nx + kWCells - 1) / kWCells;
-    const long long total = (long long)nseg * nz;
-    int resident = 0, st = resident_ctas(0, &resident);
-    if (st) return st;
-    // One resident wave (at least one segment per warp) for small grids;
-    // MW_XSPLIT_SEGS_PER_WARP segments per warp for large ones, so that the
-    // block scheduler evens out the warps' speeds; at most kXRowsMax rows per
-    // CTA range.
-    long long grid = std::min<long long>(resident, (total + kXWarps - 1) / kXWarps);
-    if (MW_XSPLIT_SEGS_PER_WARP > 0) grid = std::max<long long>(grid, total / (kXWarps * MW_XSPLIT_SEGS_PER_WARP));
-    grid = std::max<long long>(grid, (nz + kXRowsMax - 3) / (kXRowsMax - 2));
-    MW_REQUIRE(grid <= 0x7fffffffLL, MW_ERR_SHAPE, "grid too large for the x direction-stage launch");
-    k_stage_x_split<<<(unsigned)grid, kXThreads, 0, stream>>>(a, nseg, total);
-  } else {
-    const int ncb = (nx + kZThreads - 1) / kZThreads;
-    const long long units = (long long)ncb * nz;
-    int resident = 0, st = resident_ctas(1, &resident);
-    if (st) return st;
-    long long grid = resident * ((units + (long long)kZTileMax * resident - 1) / ((long long)kZTileMax * resident));
-    grid = std::max<long long>(1, std::min<long long>(grid, units / kZMinRows));
-    MW_REQUIRE(grid <= 0x7fffffffLL, MW_ERR_SHAPE, "grid too large for the z direction-stage launch");
-    k_stage_z_split<<<(unsigned)grid, kZThreads, 0, stream>>>(a, ncb);
-  }
-  return check_launch(direction == MW_DIR_X ? "x split direction-stage launch" : "z split direction-stage launch");
+  const bool small = 4 * make_geom(nx, nz).plane < (1LL << 31) && !(flags & MW_FLAG_INDEX64);
+  return (small ? s32::launch_stage_split : s64::launch_stage_split)(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti,
+                                                                     hypi, srcw, init, forcing, out, dt_stage,
+                                                                     direction, flags, stream);
 }
+
+// Ensemble members are planned with fewer than 2^31 elements per state array.
+int launch_ens_split(const EnsStage& es, int grid) { return s32::launch_ens_split(es, grid); }
+int ens_split_occupancy(int direction, int* blocks_per_sm) { return s32::ens_split_occupancy(direction, blocks_per_sm); }
 
 }  // namespace mw

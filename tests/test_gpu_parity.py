@@ -168,6 +168,47 @@ def test_vs_oracle_1024x512(mode):
         assert max(err) <= TOL_STEP
 
 
+@pytest.mark.parametrize("nx,nz", [(300, 150), (31, 7)])
+def test_split_index_widths_agree(nx, nz):
+    """The split kernels are compiled with 32-bit and 64-bit element indices
+    (arrays of 2^31 or more values take the latter); both give bit-identical
+    steps, halo included."""
+    outs = []
+    for flags in (_native.MW_FLAG_WRITE_HALO, _native.MW_FLAG_WRITE_HALO | _native.MW_FLAG_INDEX64):
+        p = make_params(nx, nz, "collision")
+        p["step_flags"] = flags
+        f = initialize_fields(p)
+        init(f, p, None)
+        reset_direction()
+        evolve(p, f, None, dt=p["dt"], nsteps=3)
+        outs.append((f.state.clone(), f.state_tmp.clone()))
+    assert torch.equal(outs[0][0], outs[1][0]) and torch.equal(outs[0][1], outs[1][1])
+
+
+@pytest.mark.parametrize("direction", [0, 1])
+def test_nonfinite_forcing_propagates_like_native(direction):
+    """A NaN or Inf in the forcing state reaches the same output cells as NaN in
+    the split form as in the FP64 form (the reference's arithmetic)."""
+    nx, nz = 64, 32
+    p = make_params(nx, nz, "collision")
+    f = initialize_fields(p)
+    init(f, p, None)
+    forcing = f.state.clone()
+    forcing[3, 2 + 10, 2 + 20] = float("nan")
+    forcing[1, 2 + 25, 2 + 40] = float("inf")
+    hb = [_native.ptr(a) for a in f.backgrounds()]
+    masks = []
+    for mode in (0, 1):
+        out = torch.zeros_like(f.state)
+        _native.call("mw_dirstage_f64", nx, nz, p["dx"], p["dz"], p["dt"], *hb, _native.ptr(f.src_w),
+                     _native.ptr(f.state), _native.ptr(forcing), _native.ptr(out), p["dt"] / 2, direction, mode, 0,
+                     _native.stream_handle())
+        masks.append(~torch.isfinite(out[:, 2:-2, 2:-2]))
+    torch.cuda.synchronize()
+    assert int(masks[0].sum()) > 0
+    assert torch.equal(masks[0].any(0), masks[1].any(0))
+
+
 def test_fp32_form_error_and_mass():
     """Precision form: FP32 perturbation fields, FP64 background / IC / reductions."""
     nx, nz = 512, 256
