@@ -54,6 +54,14 @@ __device__ __forceinline__ dw add(dw x, dw y) {
 
 __device__ __forceinline__ dw sub(dw x, dw y) { return add(x, neg(y)); }
 
+// c + x when the exponent of c.h is at least that of x.h (a series coefficient
+// plus a smaller Horner term): FastTwoSum replaces TwoSum for the leading parts.
+__device__ __forceinline__ dw add_big(dw c, dw x) {
+  const float s = c.h + x.h;
+  const float e = ((c.h - s) + x.h) + (c.l + x.l);
+  return fast_two_sum(s, e);
+}
+
 __device__ __forceinline__ dw mul(dw x, dw y) {
   float p = x.h * y.h;
   float e = fmaf(x.h, y.h, -p);

@@ -52,7 +52,9 @@ struct RowS {
 // terms 4..8 are summed in FP32, 1..3 in double-FP32 (the FP32 rounding of a
 // Horner partial sum y_k reaches the result scaled by |d|^(k-1)).  For
 // |d| <= 1/8, degree 16 with terms 7..16 in FP32; beyond that,
-// expm1(e log1p(d)) in FP64.
+// expm1(e log1p(d)) in FP64.  Each coefficient exceeds the Horner term added
+// to it (|C(e, n+1) d| < |C(e, n)| for these |d|), so the additions use
+// FastTwoSum.
 __device__ __forceinline__ dw pow_m1(const PowTab& T, double e, dw d) {
   const float ad = fabsf(d.h);
   const float df = d.h;
@@ -61,18 +63,18 @@ __device__ __forceinline__ dw pow_m1(const PowTab& T, double e, dw d) {
     t = fmaf(t, df, T.f[6]);
     t = fmaf(t, df, T.f[5]);
     t = fmaf(t, df, T.f[4]);
-    dw y = add(mulf(d, t), dw{T.h[3], T.l[3]});
-    y = add(mul(y, d), dw{T.h[2], T.l[2]});
-    y = add(mul(y, d), dw{T.h[1], T.l[1]});
+    dw y = add_big(dw{T.h[3], T.l[3]}, mulf(d, t));
+    y = add_big(dw{T.h[2], T.l[2]}, mul(y, d));
+    y = add_big(dw{T.h[1], T.l[1]}, mul(y, d));
     return mul(y, d);
   }
   if (ad <= 0.125f) {
     float t = T.f[16];
 #pragma unroll
     for (int n = 15; n >= 7; --n) t = fmaf(t, df, T.f[n]);
-    dw y = add(mulf(d, t), dw{T.h[6], T.l[6]});
+    dw y = add_big(dw{T.h[6], T.l[6]}, mulf(d, t));
 #pragma unroll
-    for (int n = 5; n >= 1; --n) y = add(mul(y, d), dw{T.h[n], T.l[n]});
+    for (int n = 5; n >= 1; --n) y = add_big(dw{T.h[n], T.l[n]}, mul(y, d));
     return mul(y, d);
   }
   const double dd = to_f64(d);
