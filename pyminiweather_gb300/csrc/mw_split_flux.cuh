@@ -58,27 +58,30 @@ struct RowS {
 __device__ __forceinline__ dw pow_m1(const PowTab& T, double e, dw d) {
   const float ad = fabsf(d.h);
   const float df = d.h;
-  if (ad <= 0.015625f) {
-    float t = fmaf(T.f[8], df, T.f[7]);
-    t = fmaf(t, df, T.f[6]);
-    t = fmaf(t, df, T.f[5]);
-    t = fmaf(t, df, T.f[4]);
-    dw y = add_big(dw{T.h[3], T.l[3]}, mulf(d, t));
-    y = add_big(dw{T.h[2], T.l[2]}, mul(y, d));
-    y = add_big(dw{T.h[1], T.l[1]}, mul(y, d));
-    return mul(y, d);
-  }
-  if (ad <= 0.125f) {
-    float t = T.f[16];
+  // degree 8, computed for every cell so that it schedules with the
+  // surrounding flux work; the rare larger |d| redo it below
+  float t = fmaf(T.f[8], df, T.f[7]);
+  t = fmaf(t, df, T.f[6]);
+  t = fmaf(t, df, T.f[5]);
+  t = fmaf(t, df, T.f[4]);
+  dw y = add_big(dw{T.h[3], T.l[3]}, mulf(d, t));
+  y = add_big(dw{T.h[2], T.l[2]}, mul(y, d));
+  y = add_big(dw{T.h[1], T.l[1]}, mul(y, d));
+  dw r = mul(y, d);
+  if (ad > 0.015625f) {
+    if (ad <= 0.125f) {
+      float t16 = T.f[16];
 #pragma unroll
-    for (int n = 15; n >= 7; --n) t = fmaf(t, df, T.f[n]);
-    dw y = add_big(dw{T.h[6], T.l[6]}, mulf(d, t));
+      for (int n = 15; n >= 7; --n) t16 = fmaf(t16, df, T.f[n]);
+      dw y16 = add_big(dw{T.h[6], T.l[6]}, mulf(d, t16));
 #pragma unroll
-    for (int n = 5; n >= 1; --n) y = add_big(dw{T.h[n], T.l[n]}, mul(y, d));
-    return mul(y, d);
+      for (int n = 5; n >= 1; --n) y16 = add_big(dw{T.h[n], T.l[n]}, mul(y16, d));
+      r = mul(y16, d);
+    } else {
+      r = from_f64(expm1(e * log1p(to_f64(d))));
+    }
   }
-  const double dd = to_f64(d);
-  return from_f64(expm1(e * log1p(dd)));
+  return r;
 }
 
 // (1 + d)^gamma - 1

@@ -84,13 +84,15 @@ struct SmemZ {
 __device__ __forceinline__ void store_update(const SplitArgs& a, sidx o, const double iv[4], dw2 dF[2]) {
   const dw d[4] = {lo_of(dF[0]), hi_of(dF[0]), lo_of(dF[1]), hi_of(dF[1])};
   const float2 z = f2add(f2sub(dF[0].h, dF[0].h), f2sub(dF[1].h, dF[1].h));
-  if (z.x + z.y == 0.0f) {
+  double v[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = fma(a.c12s, to_f64_scaled_finite(d[q]), iv[q]);
-  } else {
+  for (int q = 0; q < 4; ++q) v[q] = fma(a.c12s, to_f64_scaled_finite(d[q]), iv[q]);
+  if (!(z.x + z.y == 0.0f)) {
 #pragma unroll
-    for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = update(iv[q], d[q], a.c12s);
+    for (int q = 0; q < 4; ++q) v[q] = update(iv[q], d[q], a.c12s);
   }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = v[q];
 }
 
 // x: row k, chunks [cbeg, cend) of 255 cells.  Per chunk: the 259 forcing
@@ -210,21 +212,21 @@ __device__ __forceinline__ void x_warp_segments(const SplitArgs& a, int nseg, lo
   const Hv2 hv = make_hv2(ld(a.hv12));
   const dw d12 = ld(a.d12);
   int k = (int)(g0 / nseg), sg = (int)(g0 - (long long)k * nseg);
-  auto load = [&](int kk, int x0, double v0[4], double v1[4]) {
+  // The three cells beyond the 32 lanes' (x0+30 .. x0+32) are spread over
+  // lanes 0..11, one value each (variable lane & 3 of cell x0+30+(lane>>2)),
+  // so their conversion costs the warp one value's instructions, not four.
+  const int xq = lane & 3, xj = lane >> 2;
+  auto load = [&](int kk, int x0, double v0[4], double& v1) {
     const sidx row = (sidx)(kk + kHs) * a.pitch;
-    const int c0 = x0 - 2 + lane, c1 = x0 + 30 + lane;
+    const int c0 = x0 - 2 + lane, c1 = x0 + 30 + xj;
     if (c0 <= a.nx + 1) {
       const sidx col = wrap_x(c0, a.nx) + kHs;
 #pragma unroll
       for (int q = 0; q < 4; ++q) v0[q] = __ldg(a.forcing + q * a.plane + row + col);
     }
-    if (lane < 3 && c1 <= a.nx + 1) {
-      const sidx col = wrap_x(c1, a.nx) + kHs;
-#pragma unroll
-      for (int q = 0; q < 4; ++q) v1[q] = __ldg(a.forcing + q * a.plane + row + col);
-    }
+    if (lane < 12 && c1 <= a.nx + 1) v1 = __ldg(a.forcing + xq * a.plane + row + wrap_x(c1, a.nx) + kHs);
   };
-  double v0[4] = {0, 0, 0, 0}, v1[4] = {0, 0, 0, 0};
+  double v0[4] = {0, 0, 0, 0}, v1 = 0.0;
   load(k, sg * kWCells, v0, v1);
   for (long long g = g0; g < g1; ++g) {
     const int x0 = sg * kWCells;
@@ -234,10 +236,11 @@ __device__ __forceinline__ void x_warp_segments(const SplitArgs& a, int nseg, lo
       pack4(v0, p);
       sm.sS[w][0][lane] = p[0];
       sm.sS[w][1][lane] = p[1];
-      if (lane < 3) {
-        pack4(v1, p);
-        sm.sS[w][0][32 + lane] = p[0];
-        sm.sS[w][1][32 + lane] = p[1];
+      if (lane < 12) {
+        const dw d = from_f64(v1);
+        float* e = reinterpret_cast<float*>(&sm.sS[w][xq >> 1][32 + xj]);  // h.x, h.y, l.x, l.y
+        e[xq & 1] = d.h;
+        e[2 + (xq & 1)] = d.l;
       }
     }
     if (halo && sg == 0 && lane < 4) {  // columns 0, 1 <- nx, nx+1; nx+2, nx+3 <- 2, 3
