@@ -258,6 +258,14 @@ int mw_stats_f32(int nx, int nz, double dx, double dz, const double* hy_dens_cel
 int mw_solution_variables_f64(int nx, int nz, const double* hy_dens_cell, const double* hy_dens_theta_cell,
                               const double* state, double* out, void* stream);
 
+/* Text dump of the reference's driver (pyminiweather/__main__.py:220-233,
+ * np.savetxt(outfile, array.reshape(-1, last_dim), delimiter=",")): rows x cols
+ * HOST values, each "%.18e" as np.savetxt writes it ("nan", "inf", "-inf" for
+ * the special values), "," between values, "\n" after each row; the file is
+ * created (append = 0) or appended to.  threads <= 0: all hardware threads.
+ * Byte-identical to np.savetxt's output. */
+int mw_savetxt_f64(const double* values, long long rows, long long cols, const char* path, int append, int threads);
+
 /* ---------------------------------------------------------------------------
  * Unfused pieces of one direction-stage, for callers that use the reference's
  * fine-grained functions.  Intermediate shapes follow data/fields.py:67-78.
