@@ -50,7 +50,19 @@ struct StageArgs {
   unsigned flags;
   int chunks_per_block;
   int z_tile;
+  // FP32 form: the stage constants rounded once (FP64 arithmetic in the
+  // kernels would occupy the FP64 pipe per cell)
+  float hv_f;       // hv
+  float c_f;        // dt_stage / d
+  float dt_f;       // dt_stage
 };
+
+template <typename T>
+__host__ __device__ inline void set_f32_constants(StageArgs<T>& a, int direction) {
+  a.hv_f = float(a.hv);
+  a.c_f = float(a.dt_stage / (direction == MW_DIR_X ? a.dx : a.dz));
+  a.dt_f = float(a.dt_stage);
+}
 
 // ---- interpolation in the accumulation order of scipy.signal.convolve ----
 template <typename T>
@@ -278,7 +290,7 @@ __device__ __forceinline__ void x_rowrun_t(const StageArgs<T>& a, int k, int cbe
       if constexpr (MODE == MODE_NATIVE64) {
         flux_x_native(s, a.hyc[k + kHs], a.hytc[k + kHs], a.hv, F);
       } else {
-        flux_x_f32(s, sm.row, float(a.hv), F);
+        flux_x_f32(s, sm.row, a.hv_f, F);
       }
 #pragma unroll
       for (int q = 0; q < 4; ++q) sm.sF[q][t] = F[q];
@@ -293,7 +305,7 @@ __device__ __forceinline__ void x_rowrun_t(const StageArgs<T>& a, int k, int cbe
 #pragma unroll
         for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = iv[q] + a.dt_stage * tend[q];
       } else {
-        const float c = float(a.dt_stage / a.dx), dt = float(a.dt_stage);
+        const float c = a.c_f, dt = a.dt_f;
         float inc[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) inc[q] = (sm.sF[q][t] - sm.sF[q][t + 1]) * c;
@@ -338,7 +350,7 @@ __device__ __forceinline__ void z_tile_t(const StageArgs<T>& a, int cb, int z0, 
       if constexpr (MODE == MODE_NATIVE64) {
         flux_z_native(w, a.hyi[k], a.hyti[k], a.hypi[k], a.hv, wall, F);
       } else {
-        flux_z_f32(w, sm.row[k - z0], float(a.hv), wall, F);
+        flux_z_f32(w, sm.row[k - z0], a.hv_f, wall, F);
       }
     };
     T nxt[4];
@@ -374,7 +386,7 @@ __device__ __forceinline__ void z_tile_t(const StageArgs<T>& a, int cb, int z0, 
 #pragma unroll
         for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = iv[q] + a.dt_stage * tend[q];
       } else {
-        const float cz = float(a.dt_stage / a.dz), dt = float(a.dt_stage);
+        const float cz = a.c_f, dt = a.dt_f;
         float inc[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) inc[q] = (Fp[q] - Fn[q]) * cz;
@@ -434,6 +446,7 @@ __device__ StageArgs<float> member_args_f32(const EnsStageT<float>& es, int e) {
   a.flags = es.flags;
   a.chunks_per_block = 0;
   a.z_tile = es.z_tile;
+  set_f32_constants(a, es.direction);
   return a;
 }
 
@@ -525,6 +538,7 @@ static int launch_stage(int nx, int nz, double dx, double dz, double dt_full, co
   const int nchunks = (nx + kXCells - 1) / kXCells;
   a.chunks_per_block = (nchunks + kXBlocksPerRow - 1) / kXBlocksPerRow;
   a.z_tile = z_tile_rows(nx, nz, kZThreads, kZTile);
+  set_f32_constants(a, direction);
   if (direction == MW_DIR_X) {
     dim3 grid((nchunks + a.chunks_per_block - 1) / a.chunks_per_block, (unsigned)min(nz, 65535));
     k_stage_x<T, MODE><<<grid, kXThreads, 0, stream>>>(a);
