@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define MW_ABI_VERSION 2
+#define MW_ABI_VERSION 3
 
 enum mw_status {
   MW_OK = 0,
@@ -156,6 +156,8 @@ typedef struct mw_ens_member {
 typedef struct mw_ens_plan_info {
   int n_members, n_x_items, n_z_items, z_tile;
   size_t members_off, x_items_off, z_items_off, bytes; /* byte offsets / size of the device plan */
+  size_t xrows_off;    /* split form: per-row background constants, written by each step call */
+  long long n_xrows;   /* entries of that table: the length of the cell-centre backgrounds used */
 } mw_ens_plan_info;
 
 /* Size and layout of the work plan for these members (host array) with z
@@ -166,17 +168,18 @@ int mw_ensemble_plan_info(int n_members, const mw_ens_member* members, int z_til
 int mw_ensemble_plan(int n_members, const mw_ens_member* members, int z_tile, void* plan_device, size_t plan_bytes,
                      mw_ens_plan_info* info, void* stream);
 /* nsteps time steps of every member: 6 persistent launches per step, grid_x
- * and grid_z CTAs (0 = one full-occupancy wave).  The direction order follows
+ * and grid_z CTAs (0 = one full-occupancy wave); the FP64 call first writes
+ * the plan's row-constant table (one more launch per call).  The direction order follows
  * *reverse as in mw_step_f64 (all members alike).  FP64 storage supports
  * f64_mode MW_F64_SPLIT. */
-int mw_ensemble_step_f64(const void* plan_device, const mw_ens_plan_info* info, const double* hy_dens_cell,
+int mw_ensemble_step_f64(void* plan_device, const mw_ens_plan_info* info, const double* hy_dens_cell,
                          const double* hy_dens_theta_cell, const double* hy_dens_int, const double* hy_dens_theta_int,
                          const double* hy_pressure_int, double* state, double* state_tmp, double* scratch, int nsteps,
                          int* reverse, int f64_mode, unsigned flags, int grid_x, int grid_z, void* stream);
 /* Resident CTAs per SM of the persistent ensemble kernels (FP64 split or FP32
  * storage, x or z direction): a default grid is this times the SM count. */
 int mw_ensemble_occupancy(int f32_storage, int direction, int* blocks_per_sm);
-int mw_ensemble_step_f32(const void* plan_device, const mw_ens_plan_info* info, const double* hy_dens_cell,
+int mw_ensemble_step_f32(void* plan_device, const mw_ens_plan_info* info, const double* hy_dens_cell,
                          const double* hy_dens_theta_cell, const double* hy_dens_int, const double* hy_dens_theta_int,
                          const double* hy_pressure_int, float* state, float* state_tmp, float* scratch, int nsteps,
                          int* reverse, unsigned flags, int grid_x, int grid_z, void* stream);

@@ -79,7 +79,8 @@ class EnsPlanInfo(ctypes.Structure):
     """mw_ens_plan_info of include/miniweather_gb300.h."""
     _fields_ = [("n_members", ctypes.c_int), ("n_x_items", ctypes.c_int), ("n_z_items", ctypes.c_int),
                 ("z_tile", ctypes.c_int), ("members_off", ctypes.c_size_t), ("x_items_off", ctypes.c_size_t),
-                ("z_items_off", ctypes.c_size_t), ("bytes", ctypes.c_size_t)]
+                ("z_items_off", ctypes.c_size_t), ("bytes", ctypes.c_size_t), ("xrows_off", ctypes.c_size_t),
+                ("n_xrows", ctypes.c_longlong)]
 
 
 class MiniWeatherError(RuntimeError):

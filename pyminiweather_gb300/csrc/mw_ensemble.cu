@@ -9,6 +9,7 @@
 // are 128-column x z_tile-row tiles.  A persistent CTA takes items
 // blockIdx.x, blockIdx.x + gridDim.x, ...
 #include <algorithm>
+#include <type_traits>
 #include <cstring>
 #include <numeric>
 #include <vector>
@@ -51,8 +52,9 @@ int check_members(int n, const mw_ens_member* m, int z_tile) {
 }
 
 int layout(int n, const mw_ens_member* m, int z_tile, mw_ens_plan_info* info) {
-  long long nxi = 0, nzi = 0;
+  long long nxi = 0, nzi = 0, nrows = 0;
   for (int e = 0; e < n; ++e) {
+    nrows = std::max(nrows, m[e].cell_off + m[e].nz + 2LL * kHs);
     nxi += m[e].nz;
     nzi += (long long)((m[e].nx + kEnsZThreads - 1) / kEnsZThreads) * ((m[e].nz + z_tile - 1) / z_tile);
   }
@@ -64,7 +66,9 @@ int layout(int n, const mw_ens_member* m, int z_tile, mw_ens_plan_info* info) {
   info->members_off = 0;
   info->x_items_off = align16(sizeof(mw_ens_member) * (size_t)n);
   info->z_items_off = align16(info->x_items_off + sizeof(int2) * (size_t)nxi);
-  info->bytes = align16(info->z_items_off + sizeof(int2) * (size_t)nzi);
+  info->xrows_off = align16(info->z_items_off + sizeof(int2) * (size_t)nzi);
+  info->n_xrows = nrows;
+  info->bytes = align16(info->xrows_off + kEnsRowBytes * (size_t)nrows);
   return MW_OK;
 }
 
@@ -77,7 +81,7 @@ int num_sms(int* sms) {
 }
 
 template <typename T, typename Launch, typename Occ>
-int ens_step(const void* plan, const mw_ens_plan_info* info, const double* hyc, const double* hytc, const double* hyi,
+int ens_step(void* plan, const mw_ens_plan_info* info, const double* hyc, const double* hytc, const double* hyi,
              const double* hyti, const double* hypi, T* S, T* Tmp, T* A, int nsteps, int* reverse, unsigned flags,
              int grid_x, int grid_z, cudaStream_t stream, Launch launch, Occ occupancy) {
   MW_REQUIRE(plan && info, MW_ERR_INVALID_ARG, "plan and info must not be NULL");
@@ -114,6 +118,10 @@ int ens_step(const void* plan, const mw_ens_plan_info* info, const double* hyc, 
   es.stream = stream;
   const int2* xi = (const int2*)((const char*)plan + info->x_items_off);
   const int2* zi = (const int2*)((const char*)plan + info->z_items_off);
+  es.xrows = (const char*)plan + info->xrows_off;
+  if (std::is_same<T, double>::value && nsteps > 0 &&
+      (st = launch_ens_split_rowtable(hyc, hytc, info->n_xrows, (char*)plan + info->xrows_off, stream)))
+    return st;
   for (int n = 0; n < nsteps; ++n) {
     const int dirs[2] = {*reverse ? MW_DIR_X : MW_DIR_Z, *reverse ? MW_DIR_Z : MW_DIR_X};
     for (int d = 0; d < 2; ++d) {
@@ -177,7 +185,7 @@ extern "C" int mw_ensemble_plan(int n_members, const mw_ens_member* members, int
   return MW_OK;
 }
 
-extern "C" int mw_ensemble_step_f64(const void* plan_device, const mw_ens_plan_info* info, const double* hyc,
+extern "C" int mw_ensemble_step_f64(void* plan_device, const mw_ens_plan_info* info, const double* hyc,
                                     const double* hytc, const double* hyi, const double* hyti, const double* hypi,
                                     double* state, double* state_tmp, double* scratch, int nsteps, int* reverse,
                                     int f64_mode, unsigned flags, int grid_x, int grid_z, void* stream) {
@@ -189,7 +197,7 @@ extern "C" int mw_ensemble_step_f64(const void* plan_device, const mw_ens_plan_i
                           [](int d, int* b) { return ens_split_occupancy(d, b); });
 }
 
-extern "C" int mw_ensemble_step_f32(const void* plan_device, const mw_ens_plan_info* info, const double* hyc,
+extern "C" int mw_ensemble_step_f32(void* plan_device, const mw_ens_plan_info* info, const double* hyc,
                                     const double* hytc, const double* hyi, const double* hyti, const double* hypi,
                                     float* state, float* state_tmp, float* scratch, int nsteps, int* reverse,
                                     unsigned flags, int grid_x, int grid_z, void* stream) {

@@ -26,6 +26,7 @@ struct EnsStageT {
   const T* init;
   T* forcing;
   T* out;
+  const void* xrows;  // split form: row constants indexed like the cell-centre backgrounds
   cudaStream_t stream;
 };
 using EnsStage = EnsStageT<double>;
@@ -37,5 +38,9 @@ int launch_ens_f32(const EnsStageT<float>& es, int grid);
 int ens_f32_occupancy(int direction, int* blocks_per_sm);
 
 constexpr int kEnsZTileMax = 64;
+constexpr size_t kEnsRowBytes = 32;  // one row's background constants (four double-FP32 pairs)
+
+// Row-constant table of the split ensemble x kernels: entry j from hyc[j], hytc[j].
+int launch_ens_split_rowtable(const double* hyc, const double* hytc, long long n, void* table, cudaStream_t stream);
 
 }  // namespace mw

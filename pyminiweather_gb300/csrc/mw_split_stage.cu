@@ -45,6 +45,23 @@ int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, con
                                                                      direction, flags, stream);
 }
 
+static_assert(sizeof(RowS) == kEnsRowBytes, "row-constant table entry size");
+
+__global__ void k_ens_row_table(const double* hyc, const double* hytc, long long n, RowS* table) {
+  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x) {
+    const double hrt = hytc[j];
+    table[j] = row_consts(hyc[j], hrt, kC0 * pow(hrt, kGamma));
+  }
+}
+
+int launch_ens_split_rowtable(const double* hyc, const double* hytc, long long n, void* table, cudaStream_t stream) {
+  if (n <= 0) return MW_OK;
+  MW_REQUIRE(((uintptr_t)table % 16) == 0, MW_ERR_ALIGN, "row table misaligned");
+  const long long blocks = std::min<long long>((n + 127) / 128, 4096);
+  k_ens_row_table<<<(unsigned)blocks, 128, 0, stream>>>(hyc, hytc, n, (RowS*)table);
+  return check_launch("ensemble row-table launch");
+}
+
 // Ensemble members are planned with fewer than 2^31 elements per state array.
 int launch_ens_split(const EnsStage& es, int grid) { return s32::launch_ens_split(es, grid); }
 int ens_split_occupancy(int direction, int* blocks_per_sm) { return s32::ens_split_occupancy(direction, blocks_per_sm); }

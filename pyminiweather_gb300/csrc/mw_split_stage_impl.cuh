@@ -6,8 +6,6 @@
 namespace {
 
 constexpr int kXThreads = 256;
-constexpr int kXCells = kXThreads - 1;
-constexpr int kXTile = kXThreads + 3;  // cells x0-2 .. x0+256
 #ifndef MW_ZSPLIT_MIN_BLOCKS
 #define MW_ZSPLIT_MIN_BLOCKS 5  // z CTAs per SM the register allocation must allow
 #endif
@@ -68,11 +66,6 @@ __device__ __forceinline__ double update(double init, dw dF, double c12s) { retu
 // Tiles.  Both the single-grid kernels and the persistent ensemble kernels
 // call these; every thread of the CTA must call them (they contain barriers).
 
-struct SmemX {
-  dw2 sS[2][2][kXTile + 1];  // [buffer][pair][cell]
-  dw2 sF[2][2][kXThreads];   // [buffer][pair][interface]
-  RowS row;
-};
 struct SmemZ {
   RowS row[kZTileMax + 1];
 };
@@ -95,97 +88,6 @@ __device__ __forceinline__ void store_update(const SplitArgs& a, sidx o, const d
   for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = v[q];
 }
 
-// x: row k, chunks [cbeg, cend) of 255 cells.  Per chunk: the 259 forcing
-// values, split once, are staged in shared memory as variable pairs; thread
-// t evaluates the flux at interface x0+t and, after one barrier, updates cell
-// x0+t.  Staging and fluxes are double-buffered, so one barrier per chunk
-// suffices; the next chunk's values and this chunk's init values are loaded
-// before the flux evaluation.  The row constants (an FP64 pow) are formed
-// once per call.  halo: write this row's periodic halo into forcing.
-__device__ __forceinline__ void x_rowrun(const SplitArgs& a, int k, int cbeg, int cend, bool halo, SmemX& sm) {
-  const int t = threadIdx.x;
-  const Hv2 hv = make_hv2(ld(a.hv12));
-  const dw d12 = ld(a.d12);
-  const sidx row = (sidx)(k + kHs) * a.pitch;
-  auto load_stage = [&](int x0, double v0[4], double v1[4]) {
-    const int c0 = x0 - 2 + t, c1 = c0 + kXThreads;
-    if (c0 <= a.nx + 1) {
-      const sidx col = wrap_x(c0, a.nx) + kHs;
-#pragma unroll
-      for (int q = 0; q < 4; ++q) v0[q] = __ldg(a.forcing + q * a.plane + row + col);
-    }
-    if (t < kXTile - kXThreads && c1 <= a.nx + 1) {
-      const sidx col = wrap_x(c1, a.nx) + kHs;
-#pragma unroll
-      for (int q = 0; q < 4; ++q) v1[q] = __ldg(a.forcing + q * a.plane + row + col);
-    }
-  };
-  auto store_stage = [&](int b, const double v0[4], const double v1[4]) {
-    dw2 p[2];
-    pack4(v0, p);
-    sm.sS[b][0][t] = p[0];
-    sm.sS[b][1][t] = p[1];
-    if (t < kXTile - kXThreads) {
-      pack4(v1, p);
-      sm.sS[b][0][t + kXThreads] = p[0];
-      sm.sS[b][1][t + kXThreads] = p[1];
-    }
-  };
-  if (t == 0) {
-    const double hrt = a.hytc[k + kHs];
-    sm.row = row_consts(a.hyc[k + kHs], hrt, kC0 * pow(hrt, kGamma));
-  }
-  if (halo && t < 4) {
-    const int dst[4] = {0, 1, a.nx + kHs, a.nx + kHs + 1};
-    const int src[4] = {a.nx, a.nx + 1, kHs, kHs + 1};
-#pragma unroll
-    for (int q = 0; q < 4; ++q) a.forcing[q * a.plane + row + dst[t]] = a.forcing[q * a.plane + row + src[t]];
-  }
-  double v0[4] = {0, 0, 0, 0}, v1[4] = {0, 0, 0, 0};
-  if (cbeg < cend) {
-    load_stage(cbeg * kXCells, v0, v1);
-    store_stage(0, v0, v1);
-  }
-  __syncthreads();
-  for (int chunk = cbeg; chunk < cend; ++chunk) {
-    const int b = (chunk - cbeg) & 1;
-    const int x0 = chunk * kXCells;
-    const int i = x0 + t;
-    const bool upd = t < kXCells && i < a.nx;
-    const sidx o = row + i + kHs;
-    double iv[4];
-    if (upd) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
-    }
-    const bool more = chunk + 1 < cend;
-    if (more) load_stage(x0 + kXCells, v0, v1);
-    if (i <= a.nx) {
-      dw2 s[2][4];
-#pragma unroll
-      for (int pr = 0; pr < 2; ++pr)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) s[pr][j] = sm.sS[b][pr][t + j];
-      dw2 F[2];
-      flux_x2(s, sm.row, hv, F);
-      sm.sF[b][0][t] = F[0];
-      sm.sF[b][1][t] = F[1];
-    }
-    if (more) store_stage(b ^ 1, v0, v1);
-    __syncthreads();
-    if (upd) {
-      dw2 dF[2] = {sub2(sm.sF[b][0][t], sm.sF[b][0][t + 1]), sub2(sm.sF[b][1][t], sm.sF[b][1][t + 1])};
-      if (a.srcw) {
-        const dw w = add(lo_of(dF[1]), mul(from_f64(a.srcw[(sidx)k * a.nx + i]), d12));
-        dF[1].h.x = w.h;
-        dF[1].l.x = w.l;
-      }
-      store_update(a, o, iv, dF);
-    }
-  }
-  __syncthreads();
-}
-
 // x, single grid: the CTA owns the contiguous range [g0, g1) of the row-major
 // list of 31-cell segments (nseg per row) and splits it evenly over its eight
 // warps.  Each warp walks its segments with no CTA barrier: lane l stages cell
@@ -205,8 +107,10 @@ __device__ __forceinline__ RowS x_row_consts(const SplitArgs& a, int k) {
   return row_consts(a.hyc[k + kHs], hrt, kC0 * pow(hrt, kGamma));
 }
 
-__device__ __forceinline__ void x_warp_segments(const SplitArgs& a, int nseg, long long g0, long long g1, int row0,
-                                                bool halo, SmemXW& sm) {
+// row_at(k): the row constants of row k.
+template <typename RowAt>
+__device__ __forceinline__ void x_warp_segments(const SplitArgs& a, int nseg, long long g0, long long g1,
+                                                RowAt row_at, bool halo, SmemXW& sm) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if (g0 >= g1) return;
   const Hv2 hv = make_hv2(ld(a.hv12));
@@ -271,7 +175,7 @@ __device__ __forceinline__ void x_warp_segments(const SplitArgs& a, int nseg, lo
 #pragma unroll
         for (int j = 0; j < 4; ++j) s[pr][j] = sm.sS[w][pr][lane + j];
       dw2 F[2];
-      flux_x2(s, sm.row[kc - row0], hv, F);
+      flux_x2(s, row_at(kc), hv, F);
       sm.sF[w][0][lane] = F[0];
       sm.sF[w][1][lane] = F[1];
     }
@@ -380,7 +284,8 @@ __global__ void __launch_bounds__(kXThreads, MW_XSPLIT_MIN_BLOCKS) k_stage_x_spl
   __syncthreads();
   const int w = threadIdx.x >> 5;
   const long long n = g1 - g0;
-  x_warp_segments(a, nseg, g0 + n * w / kXWarps, g0 + n * (w + 1) / kXWarps, row0, a.flags & MW_FLAG_WRITE_HALO, sm);
+  x_warp_segments(a, nseg, g0 + n * w / kXWarps, g0 + n * (w + 1) / kXWarps,
+                  [&](int k) { return sm.row[k - row0]; }, a.flags & MW_FLAG_WRITE_HALO, sm);
 }
 
 // z, single grid: the CTA owns the contiguous range [u0, u1) of the
@@ -430,12 +335,19 @@ __device__ SplitArgs member_args(const EnsStage& es, int e) {
   return a;
 }
 
-__global__ void __launch_bounds__(kXThreads) k_ens_x_split(EnsStage es) {
-  __shared__ SmemX sm;
-  for (int it = blockIdx.x; it < es.n_items; it += gridDim.x) {
+// x items are rows (member, row), one per warp: the warp walks the row's
+// 31-cell segments as the single-grid kernel does, with the row constants read
+// from the plan's table (written once per step call, no FP64 pow per row).
+__global__ void __launch_bounds__(kXThreads, MW_XSPLIT_MIN_BLOCKS) k_ens_x_split(EnsStage es) {
+  __shared__ SmemXW sm;
+  const int nw = gridDim.x * kXWarps;
+  for (int it = blockIdx.x * kXWarps + (threadIdx.x >> 5); it < es.n_items; it += nw) {
     const int2 item = es.items[it];  // (member, row)
     const SplitArgs a = member_args(es, item.x);
-    x_rowrun(a, item.y, 0, (a.nx + kXCells - 1) / kXCells, a.flags & MW_FLAG_WRITE_HALO, sm);
+    const int nseg = (a.nx + kWCells - 1) / kWCells;
+    const RowS r = reinterpret_cast<const RowS*>(es.xrows)[es.members[item.x].cell_off + item.y + kHs];
+    x_warp_segments(a, nseg, (long long)item.y * nseg, (long long)(item.y + 1) * nseg,
+                    [&](int) { return r; }, a.flags & MW_FLAG_WRITE_HALO, sm);
   }
 }
 

@@ -35,7 +35,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_status_strings_and_version():
     L = _native.load()
-    assert L.mw_abi_version() == 2
+    assert L.mw_abi_version() == 3
     for code in range(8):
         assert L.mw_status_string(code)
     assert L.mw_status_string(99) == b"unknown status"
