@@ -450,12 +450,57 @@ __device__ StageArgs<float> member_args_f32(const EnsStageT<float>& es, int e) {
   return a;
 }
 
+// x items are rows (member, row), one per warp: lane l evaluates the flux at
+// interface x0+l of a 31-cell segment from its four taps (L1-resident loads)
+// and takes the flux of interface x0+l+1 from lane l+1 by a shuffle, so rows
+// of 64..1024 cells keep most lanes busy.
+constexpr int kF32WCells = 31;
+
+__device__ __forceinline__ void x_row_warp_f32(const StageArgs<float>& a, int k, bool halo) {
+  const int lane = threadIdx.x & 31;
+  const RowF r = rowf_x(a.hyc[k + kHs], a.hytc[k + kHs]);
+  const long long row = (long long)(k + kHs) * a.pitch;
+  if (halo && lane < 4) {  // columns 0, 1 <- nx, nx+1; nx+2, nx+3 <- 2, 3
+    const int dst = lane < 2 ? lane : a.nx + lane, src = lane < 2 ? a.nx + lane : lane;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) a.forcing[q * a.plane + row + dst] = a.forcing[q * a.plane + row + src];
+  }
+  for (int x0 = 0; x0 < a.nx; x0 += kF32WCells) {
+    const int i = x0 + lane;
+    const bool upd = lane < kF32WCells && i < a.nx;
+    const long long o = row + i + kHs;
+    float iv[4];
+    if (upd) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
+    }
+    float F[4] = {0.f, 0.f, 0.f, 0.f};
+    if (i <= a.nx) {
+      float s4[4][4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const long long col = wrap_x(i - 2 + j, a.nx) + kHs;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) s4[q][j] = __ldg(a.forcing + q * a.plane + row + col);
+      }
+      flux_x_f32(s4, r, a.hv_f, F);
+    }
+    float Fn[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) Fn[q] = __shfl_down_sync(0xffffffffu, F[q], 1);
+    if (upd) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = iv[q] + (F[q] - Fn[q]) * a.c_f;
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kXThreads) k_ens_x_f32(EnsStageT<float> es) {
-  __shared__ SmemXT<float> sm;
-  for (int it = blockIdx.x; it < es.n_items; it += gridDim.x) {
-    const int2 item = es.items[it];
+  const int nw = gridDim.x * (kXThreads / 32);
+  for (int it = blockIdx.x * (kXThreads / 32) + (threadIdx.x >> 5); it < es.n_items; it += nw) {
+    const int2 item = es.items[it];  // (member, row)
     const StageArgs<float> a = member_args_f32(es, item.x);
-    x_rowrun_t<float, MODE_F32>(a, item.y, 0, (a.nx + kXCells - 1) / kXCells, a.flags & MW_FLAG_WRITE_HALO, sm);
+    x_row_warp_f32(a, item.y, a.flags & MW_FLAG_WRITE_HALO);
   }
 }
 
