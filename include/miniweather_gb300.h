@@ -110,6 +110,21 @@ int mw_step_f64(int nx, int nz, double dx, double dz, double dt_full, double dt,
                 const double* hy_pressure_int, const double* src_w, double* state, double* state_tmp,
                 double* scratch, int nsteps, int* reverse, int f64_mode, unsigned flags, void* stream);
 
+/* One time step of a state held in HOST memory (no counterpart in the
+ * reference, whose arrays are host arrays to begin with): h_in (4, nz+4, nx+4)
+ * is copied into state, the step runs as mw_step_f64 with nsteps = 1, and the
+ * resulting state is copied into h_out (which may equal h_in).  Enqueued on
+ * `stream`; h_out is complete once the stream is.  In the split form the
+ * copies overlap the computation by nbands row bands (<= 16, at least 16 rows
+ * each); the results are those of copy-in, mw_step_f64, copy-out bit for bit.
+ * h_in / h_out should be page-locked for the copies to run asynchronously.
+ * Calls on one device share internal copy streams and are serialised. */
+int mw_step_f64_host(int nx, int nz, double dx, double dz, double dt_full, double dt, const double* hy_dens_cell,
+                     const double* hy_dens_theta_cell, const double* hy_dens_int, const double* hy_dens_theta_int,
+                     const double* hy_pressure_int, const double* src_w, const double* h_in, double* h_out,
+                     double* state, double* state_tmp, double* scratch, int* reverse, int f64_mode, unsigned flags,
+                     int nbands, void* stream);
+
 int mw_step_f32(int nx, int nz, double dx, double dz, double dt_full, double dt, const double* hy_dens_cell,
                 const double* hy_dens_theta_cell, const double* hy_dens_int, const double* hy_dens_theta_int,
                 const double* hy_pressure_int, const double* src_w, float* state, float* state_tmp, float* scratch,

@@ -34,6 +34,8 @@ _SIGNATURES = {
     "mw_dirstage_f64": [_i, _i, _d, _d, _d, _P, _P, _P, _P, _P, _P, _P, _P, _P, _d, _i, _i, _u, _P],
     "mw_dirstage_f32": [_i, _i, _d, _d, _d, _P, _P, _P, _P, _P, _P, _P, _P, _P, _d, _i, _u, _P],
     "mw_step_f64": [_i, _i, _d, _d, _d, _d, _P, _P, _P, _P, _P, _P, _P, _P, _P, _i, ctypes.POINTER(_i), _i, _u, _P],
+    "mw_step_f64_host": [_i, _i, _d, _d, _d, _d, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, ctypes.POINTER(_i), _i,
+                         _u, _i, _P],
     "mw_step_f32": [_i, _i, _d, _d, _d, _d, _P, _P, _P, _P, _P, _P, _P, _P, _P, _i, ctypes.POINTER(_i), _u, _P],
     "mw_step_f64_noalloc": [_i, _i, _d, _d, _d, _d, _P, _P, _P, _P, _P, _P, _P, _P, _i, ctypes.POINTER(_i), _i, _u,
                             _P],

@@ -598,7 +598,7 @@ static int launch_stage(int nx, int nz, double dx, double dz, double dt_full, co
 int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
                        const double* hyi, const double* hyti, const double* hypi, const double* srcw,
                        const double* init, double* forcing, double* out, double dt_stage, int direction,
-                       unsigned flags, cudaStream_t stream);
+                       unsigned flags, int r0, int r1, cudaStream_t stream);
 
 static int stage_f64(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
                      const double* hyi, const double* hyti, const double* hypi, const double* srcw,
@@ -606,7 +606,7 @@ static int stage_f64(int nx, int nz, double dx, double dz, double dt_full, const
                      unsigned flags, cudaStream_t stream) {
   if (mode == MW_F64_SPLIT)
     return launch_stage_split(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, srcw, init, forcing, out,
-                              dt_stage, direction, flags, stream);
+                              dt_stage, direction, flags, 0, nz, stream);
   return launch_stage<double, MODE_NATIVE64>(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, srcw, init, forcing,
                                              out, dt_stage, direction, flags, stream);
 }

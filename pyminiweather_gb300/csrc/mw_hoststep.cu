@@ -1,0 +1,178 @@
+// mw_hoststep.cu -- one time step of a state held in host memory: copy in,
+// step, copy out, with the copies overlapped with the computation by row
+// bands (the end-to-end use of the step by a caller whose arrays live on the
+// host).
+//
+// The x direction only couples cells of the same row, so its three stages can
+// run on a band of rows as soon as that band has arrived, and the band can
+// leave as soon as its last x stage is done.  A z stage needs two rows of the
+// neighbouring bands, so it runs over a band once those have arrived (first
+// stage) or over the whole grid.  For the order x then z: bands stream in
+// under the x stages, z stages 1-2 run over the grid, z stage 3 runs band by
+// band and each band streams out behind it.  For z then x: z stage 1 runs
+// band by band behind the copies in, z stages 2-3 over the grid, and the x
+// stages band by band ahead of the copies out.  All kernels run in order on
+// the caller's stream, so every read sees the same data as in mw_step_f64;
+// the copies run on two side streams ordered against it by events.
+#include <algorithm>
+#include <mutex>
+
+#include "mw_common.cuh"
+
+namespace mw {
+
+int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
+                       const double* hyi, const double* hyti, const double* hypi, const double* srcw,
+                       const double* init, double* forcing, double* out, double dt_stage, int direction,
+                       unsigned flags, int r0, int r1, cudaStream_t stream);
+
+namespace {
+
+constexpr int kMaxBands = 16;
+
+struct CopyRes {
+  bool ready = false;
+  cudaStream_t h2d = nullptr, d2h = nullptr;
+  cudaEvent_t start = nullptr, done = nullptr, in[kMaxBands] = {}, out[kMaxBands] = {};
+};
+CopyRes g_res[64];
+std::mutex g_mu;  // held while a call enqueues its work: calls share the streams and events of a device
+
+int resources(CopyRes** r) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return fail(MW_ERR_CUDA, "no usable device");
+  CopyRes& c = g_res[dev];
+  if (!c.ready) {
+    cudaError_t e = cudaStreamCreateWithFlags(&c.h2d, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c.d2h, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c.start, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c.done, cudaEventDisableTiming);
+    for (int b = 0; b < kMaxBands && e == cudaSuccess; ++b) {
+      e = cudaEventCreateWithFlags(&c.in[b], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c.out[b], cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) return fail(MW_ERR_CUDA, "copy streams / events: %s", cudaGetErrorString(e));
+    c.ready = true;
+  }
+  *r = &c;
+  return MW_OK;
+}
+
+// The array rows a band moves between host and device: its interior rows, plus
+// the wall halo rows for the first and last band.
+void band_rows(int nz, int nb, int b, int* r0, int* r1, int* a0, int* a1) {
+  const int per = (nz + nb - 1) / nb;
+  *r0 = std::min(nz, b * per);
+  *r1 = std::min(nz, *r0 + per);
+  *a0 = b == 0 ? 0 : *r0 + kHs;
+  *a1 = b == nb - 1 ? nz + 2 * kHs : *r1 + kHs;
+}
+
+cudaError_t copy_band(double* dst, const double* src, const Geom& g, int a0, int a1, cudaMemcpyKind kind,
+                      cudaStream_t s) {
+  cudaError_t e = cudaSuccess;
+  for (int q = 0; q < 4 && e == cudaSuccess; ++q) {
+    const long long off = q * g.plane + (long long)a0 * g.pitch;
+    e = cudaMemcpyAsync(dst + off, src + off, sizeof(double) * (size_t)(a1 - a0) * g.pitch, kind, s);
+  }
+  return e;
+}
+
+}  // namespace
+}  // namespace mw
+
+using namespace mw;
+
+extern "C" int mw_step_f64(int nx, int nz, double dx, double dz, double dt_full, double dt, const double* hyc,
+                           const double* hytc, const double* hyi, const double* hyti, const double* hypi,
+                           const double* src_w, double* state, double* state_tmp, double* scratch, int nsteps,
+                           int* reverse, int f64_mode, unsigned flags, void* stream);
+
+extern "C" int mw_step_f64_host(int nx, int nz, double dx, double dz, double dt_full, double dt, const double* hyc,
+                                const double* hytc, const double* hyi, const double* hyti, const double* hypi,
+                                const double* src_w, const double* h_in, double* h_out, double* state,
+                                double* state_tmp, double* scratch, int* reverse, int f64_mode, unsigned flags,
+                                int nbands, void* stream) {
+  // argument checks of the step itself (nothing runs for nsteps = 0)
+  int st = mw_step_f64(nx, nz, dx, dz, dt_full, dt, hyc, hytc, hyi, hyti, hypi, src_w, state, state_tmp, scratch, 0,
+                       reverse, f64_mode, flags, stream);
+  if (st) return st;
+  MW_REQUIRE(h_in && h_out, MW_ERR_INVALID_ARG, "host state arrays must not be NULL");
+  const Geom g = make_geom(nx, nz);
+  const size_t bytes = sizeof(double) * 4 * (size_t)g.plane;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nb = std::max(1, std::min({nbands, kMaxBands, nz / 16}));
+  if (f64_mode != MW_F64_SPLIT || nb == 1) {  // no bands: copy in, step, copy out
+    cudaError_t e = cudaMemcpyAsync(state, h_in, bytes, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return fail(MW_ERR_CUDA, "copy in: %s", cudaGetErrorString(e));
+    if ((st = mw_step_f64(nx, nz, dx, dz, dt_full, dt, hyc, hytc, hyi, hyti, hypi, src_w, state, state_tmp, scratch, 1,
+                          reverse, f64_mode, flags, stream)))
+      return st;
+    e = cudaMemcpyAsync(h_out, state, bytes, cudaMemcpyDeviceToHost, s);
+    return e == cudaSuccess ? MW_OK : fail(MW_ERR_CUDA, "copy out: %s", cudaGetErrorString(e));
+  }
+  std::lock_guard<std::mutex> lock(g_mu);
+  CopyRes* c = nullptr;
+  if ((st = resources(&c))) return st;
+  double *S = state, *Tmp = state_tmp, *A = scratch;
+  auto stage = [&](const double* init, double* forcing, double* out, double dts, int dir, int r0, int r1) {
+    return launch_stage_split(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, src_w, init, forcing, out, dts,
+                              dir, flags, r0, r1, s);
+  };
+  auto x_band = [&](int r0, int r1) {
+    int e;
+    if ((e = stage(S, S, A, dt / 3, MW_DIR_X, r0, r1))) return e;
+    if ((e = stage(S, A, Tmp, dt / 2, MW_DIR_X, r0, r1))) return e;
+    return stage(S, Tmp, S, dt, MW_DIR_X, r0, r1);
+  };
+  cudaError_t e = cudaEventRecord(c->start, s);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(c->h2d, c->start, 0);
+  for (int b = 0; b < nb && e == cudaSuccess; ++b) {
+    int r0, r1, a0, a1;
+    band_rows(nz, nb, b, &r0, &r1, &a0, &a1);
+    e = copy_band(S, h_in, g, a0, a1, cudaMemcpyHostToDevice, c->h2d);
+    if (e == cudaSuccess) e = cudaEventRecord(c->in[b], c->h2d);
+  }
+  if (e != cudaSuccess) return fail(MW_ERR_CUDA, "copy in: %s", cudaGetErrorString(e));
+  auto band_out = [&](int b) {
+    int r0, r1, a0, a1;
+    band_rows(nz, nb, b, &r0, &r1, &a0, &a1);
+    cudaError_t ee = cudaEventRecord(c->out[b], s);
+    if (ee == cudaSuccess) ee = cudaStreamWaitEvent(c->d2h, c->out[b], 0);
+    if (ee == cudaSuccess) ee = copy_band(h_out, S, g, a0, a1, cudaMemcpyDeviceToHost, c->d2h);
+    return ee == cudaSuccess ? MW_OK : fail(MW_ERR_CUDA, "copy out: %s", cudaGetErrorString(ee));
+  };
+  if (*reverse) {  // x then z
+    for (int b = 0; b < nb; ++b) {
+      int r0, r1, a0, a1;
+      band_rows(nz, nb, b, &r0, &r1, &a0, &a1);
+      if ((e = cudaStreamWaitEvent(s, c->in[b], 0)) != cudaSuccess) return fail(MW_ERR_CUDA, "wait: %s", cudaGetErrorString(e));
+      if ((st = x_band(r0, r1))) return st;
+    }
+    if ((st = stage(S, S, A, dt / 3, MW_DIR_Z, 0, nz)) || (st = stage(S, A, Tmp, dt / 2, MW_DIR_Z, 0, nz))) return st;
+    for (int b = 0; b < nb; ++b) {
+      int r0, r1, a0, a1;
+      band_rows(nz, nb, b, &r0, &r1, &a0, &a1);
+      if ((st = stage(S, Tmp, S, dt, MW_DIR_Z, r0, r1)) || (st = band_out(b))) return st;
+    }
+  } else {  // z then x
+    for (int b = 0; b < nb; ++b) {
+      int r0, r1, a0, a1;
+      band_rows(nz, nb, b, &r0, &r1, &a0, &a1);
+      if ((e = cudaStreamWaitEvent(s, c->in[std::min(b + 1, nb - 1)], 0)) != cudaSuccess)
+        return fail(MW_ERR_CUDA, "wait: %s", cudaGetErrorString(e));
+      if ((st = stage(S, S, A, dt / 3, MW_DIR_Z, r0, r1))) return st;
+    }
+    if ((st = stage(S, A, Tmp, dt / 2, MW_DIR_Z, 0, nz)) || (st = stage(S, Tmp, S, dt, MW_DIR_Z, 0, nz))) return st;
+    for (int b = 0; b < nb; ++b) {
+      int r0, r1, a0, a1;
+      band_rows(nz, nb, b, &r0, &r1, &a0, &a1);
+      if ((st = x_band(r0, r1)) || (st = band_out(b))) return st;
+    }
+  }
+  e = cudaEventRecord(c->done, c->d2h);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c->done, 0);
+  if (e != cudaSuccess) return fail(MW_ERR_CUDA, "join: %s", cudaGetErrorString(e));
+  *reverse = *reverse ? 0 : 1;
+  return MW_OK;
+}

@@ -34,15 +34,16 @@ typedef long long sidx;
 #include "mw_split_stage_impl.cuh"
 }  // namespace s64
 
-// Arrays whose four planes span fewer than 2^31 elements take the 32-bit-index kernels.
+// Arrays whose four planes span fewer than 2^31 elements take the 32-bit-index
+// kernels.  Output rows [r0, r1) (the whole grid: 0, nz).
 int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
                        const double* hyi, const double* hyti, const double* hypi, const double* srcw,
                        const double* init, double* forcing, double* out, double dt_stage, int direction,
-                       unsigned flags, cudaStream_t stream) {
+                       unsigned flags, int r0, int r1, cudaStream_t stream) {
   const bool small = 4 * make_geom(nx, nz).plane < (1LL << 31) && !(flags & MW_FLAG_INDEX64);
   return (small ? s32::launch_stage_split : s64::launch_stage_split)(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti,
                                                                      hypi, srcw, init, forcing, out, dt_stage,
-                                                                     direction, flags, stream);
+                                                                     direction, flags, r0, r1, stream);
 }
 
 static_assert(sizeof(RowS) == kEnsRowBytes, "row-constant table entry size");

@@ -46,15 +46,19 @@ __device__ __forceinline__ double zval64(const SplitArgs& a, int q, int k, int c
   return s;
 }
 
-__device__ __forceinline__ void write_z_halo_column(const SplitArgs& a, int col) {
-  const int rows[4] = {-2, -1, a.nz, a.nz + 1};
+// Wall halo rows of one column of the forcing array: -2, -1 (bottom) from
+// row 0 and nz, nz+1 (top) from row nz-1.
+__device__ __forceinline__ void write_z_halo_column(const SplitArgs& a, int col, bool bottom, bool top) {
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    double v[4];
+  for (int h = 0; h < 2; ++h) {
+    if (!(h == 0 ? bottom : top)) continue;
+    const int r0 = h == 0 ? -2 : a.nz;
 #pragma unroll
-    for (int r = 0; r < 4; ++r) v[r] = zval64(a, q, rows[r], col);
-#pragma unroll
-    for (int r = 0; r < 4; ++r) a.forcing[q * (sidx)a.plane + (sidx)(rows[r] + kHs) * a.pitch + col] = v[r];
+    for (int q = 0; q < 4; ++q) {
+      const double v0 = zval64(a, q, r0, col), v1 = zval64(a, q, r0 + 1, col);
+      a.forcing[q * (sidx)a.plane + (sidx)(r0 + kHs) * a.pitch + col] = v0;
+      a.forcing[q * (sidx)a.plane + (sidx)(r0 + 1 + kHs) * a.pitch + col] = v1;
+    }
   }
 }
 
@@ -196,10 +200,11 @@ __device__ __forceinline__ void x_warp_segments(const SplitArgs& a, int nseg, lo
 // z: columns [cb*128, cb*128+128), rows [kbeg, kend), kend - kbeg <=
 // kZTileMax: one thread per column marching the rows with a rolling window of
 // variable pairs; the next row and the init values are loaded one step ahead;
-// the interface row constants are tabled in shared memory.  halo: write the
-// wall halo rows of these columns of the forcing array (cb == 0 also does the
-// four x-halo columns).
-__device__ __forceinline__ void z_march(const SplitArgs& a, int cb, int kbeg, int kend, bool halo, SmemZ& sm) {
+// the interface row constants are tabled in shared memory.  hbot / htop:
+// write the bottom / top wall halo rows of these columns of the forcing array
+// (cb == 0 also does the four x-halo columns).
+__device__ __forceinline__ void z_march(const SplitArgs& a, int cb, int kbeg, int kend, bool hbot, bool htop,
+                                        SmemZ& sm) {
   __syncthreads();  // the previous table is no longer read
   for (int r = threadIdx.x; r <= kend - kbeg; r += kZThreads) {
     const int k = kbeg + r;
@@ -207,10 +212,11 @@ __device__ __forceinline__ void z_march(const SplitArgs& a, int cb, int kbeg, in
   }
   __syncthreads();
   const int c = cb * kZThreads + threadIdx.x;
-  if (halo && cb == 0 && threadIdx.x < 4) write_z_halo_column(a, threadIdx.x < 2 ? threadIdx.x : a.nx + threadIdx.x);
+  if ((hbot || htop) && cb == 0 && threadIdx.x < 4)
+    write_z_halo_column(a, threadIdx.x < 2 ? threadIdx.x : a.nx + threadIdx.x, hbot, htop);
   if (c >= a.nx) return;
   const int col = c + kHs;
-  if (halo) write_z_halo_column(a, col);
+  if (hbot || htop) write_z_halo_column(a, col, hbot, htop);
   const Hv2 hv = make_hv2(ld(a.hv12));
   const dw d12 = ld(a.d12), gz12 = ld(a.gz12);
   dw2 w[2][4];
@@ -275,9 +281,11 @@ __device__ __forceinline__ void z_march(const SplitArgs& a, int cb, int kbeg, in
 #ifndef MW_XSPLIT_MIN_BLOCKS
 #define MW_XSPLIT_MIN_BLOCKS 3
 #endif
-__global__ void __launch_bounds__(kXThreads, MW_XSPLIT_MIN_BLOCKS) k_stage_x_split(SplitArgs a, int nseg, long long total) {
+// Segments [gbase, gbase + total) (rows gbase / nseg onwards).
+__global__ void __launch_bounds__(kXThreads, MW_XSPLIT_MIN_BLOCKS) k_stage_x_split(SplitArgs a, int nseg, long long total,
+                                                                                   long long gbase) {
   __shared__ SmemXW sm;
-  const long long g0 = total * blockIdx.x / gridDim.x, g1 = total * (blockIdx.x + 1) / gridDim.x;
+  const long long g0 = gbase + total * blockIdx.x / gridDim.x, g1 = gbase + total * (blockIdx.x + 1) / gridDim.x;
   if (g0 >= g1) return;
   const int row0 = (int)(g0 / nseg), nrows = (int)((g1 - 1) / nseg) - row0 + 1;  // nrows <= kXRowsMax (host)
   for (int r = threadIdx.x; r < nrows; r += kXThreads) sm.row[r] = x_row_consts(a, row0 + r);
@@ -292,15 +300,18 @@ __global__ void __launch_bounds__(kXThreads, MW_XSPLIT_MIN_BLOCKS) k_stage_x_spl
 // column-block-major list of (column block, row) units, at most kZTileMax
 // units, so it marches one or two column-block pieces.  The launch sizes the
 // grid to a whole number of resident waves of equal ranges.
-__global__ void __launch_bounds__(kZThreads, MW_ZSPLIT_MIN_BLOCKS) k_stage_z_split(SplitArgs a, int ncb) {
+// Rows [r0, r1) of every column block.
+__global__ void __launch_bounds__(kZThreads, MW_ZSPLIT_MIN_BLOCKS) k_stage_z_split(SplitArgs a, int ncb, int r0, int r1) {
   __shared__ SmemZ sm;
-  const long long U = (long long)ncb * a.nz;
+  const int rows = r1 - r0;
+  const long long U = (long long)ncb * rows;
   long long u = U * blockIdx.x / gridDim.x;
   const long long u1 = U * (blockIdx.x + 1) / gridDim.x;
+  const bool halo = a.flags & MW_FLAG_WRITE_HALO;
   while (u < u1) {
-    const int cb = (int)(u / a.nz), k0 = (int)(u - (long long)cb * a.nz);
-    const int kend = (int)std::min<long long>(a.nz, k0 + (u1 - u));
-    z_march(a, cb, k0, kend, (a.flags & MW_FLAG_WRITE_HALO) && k0 == 0, sm);
+    const int cb = (int)(u / rows), k0 = r0 + (int)(u - (long long)cb * rows);
+    const int kend = (int)std::min<long long>(r1, k0 + (u1 - u));
+    z_march(a, cb, k0, kend, halo && k0 == 0, halo && kend == a.nz, sm);
     u += kend - k0;
   }
 }
@@ -358,7 +369,9 @@ __global__ void __launch_bounds__(kZThreads, MW_ZSPLIT_MIN_BLOCKS) k_ens_z_split
     const SplitArgs a = member_args(es, item.x);
     const int ncb = (a.nx + kZThreads - 1) / kZThreads;
     const int cb = item.y % ncb, tile = item.y / ncb;
-    z_march(a, cb, tile * es.z_tile, min((tile + 1) * es.z_tile, a.nz), (a.flags & MW_FLAG_WRITE_HALO) && tile == 0, sm);
+    const int k0 = tile * es.z_tile, kend = min(k0 + es.z_tile, a.nz);
+    const bool halo = a.flags & MW_FLAG_WRITE_HALO;
+    z_march(a, cb, k0, kend, halo && k0 == 0, halo && kend == a.nz, sm);
   }
 }
 
@@ -402,8 +415,10 @@ int resident_ctas(int which, int* out) {
 int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
                        const double* hyi, const double* hyti, const double* hypi, const double* srcw,
                        const double* init, double* forcing, double* out, double dt_stage, int direction,
-                       unsigned flags, cudaStream_t stream) {
+                       unsigned flags, int r0, int r1, cudaStream_t stream) {
   const Geom g = make_geom(nx, nz);
+  MW_REQUIRE(0 <= r0 && r0 < r1 && r1 <= nz, MW_ERR_INVALID_ARG, "row range [%d, %d) outside [0, %d)", r0, r1, nz);
+  const int rows = r1 - r0;
   SplitArgs a;
   a.nx = nx;
   a.nz = nz;
@@ -429,7 +444,7 @@ int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, con
   a.gz12 = split_host(12.0 * dz * kGrav);
   if (direction == MW_DIR_X) {
     const int nseg = (nx + kWCells - 1) / kWCells;
-    const long long total = (long long)nseg * nz;
+    const long long total = (long long)nseg * rows;
     int resident = 0, st = resident_ctas(0, &resident);
     if (st) return st;
     // One resident wave (at least one segment per warp) for small grids;
@@ -438,18 +453,18 @@ int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, con
     // CTA range.
     long long grid = std::min<long long>(resident, (total + kXWarps - 1) / kXWarps);
     if (MW_XSPLIT_SEGS_PER_WARP > 0) grid = std::max<long long>(grid, total / (kXWarps * MW_XSPLIT_SEGS_PER_WARP));
-    grid = std::max<long long>(grid, (nz + kXRowsMax - 3) / (kXRowsMax - 2));
+    grid = std::max<long long>(grid, (rows + kXRowsMax - 3) / (kXRowsMax - 2));
     MW_REQUIRE(grid <= 0x7fffffffLL, MW_ERR_SHAPE, "grid too large for the x direction-stage launch");
-    k_stage_x_split<<<(unsigned)grid, kXThreads, 0, stream>>>(a, nseg, total);
+    k_stage_x_split<<<(unsigned)grid, kXThreads, 0, stream>>>(a, nseg, total, (long long)r0 * nseg);
   } else {
     const int ncb = (nx + kZThreads - 1) / kZThreads;
-    const long long units = (long long)ncb * nz;
+    const long long units = (long long)ncb * rows;
     int resident = 0, st = resident_ctas(1, &resident);
     if (st) return st;
     long long grid = resident * ((units + (long long)kZTileMax * resident - 1) / ((long long)kZTileMax * resident));
     grid = std::max<long long>(1, std::min<long long>(grid, units / kZMinRows));
     MW_REQUIRE(grid <= 0x7fffffffLL, MW_ERR_SHAPE, "grid too large for the z direction-stage launch");
-    k_stage_z_split<<<(unsigned)grid, kZThreads, 0, stream>>>(a, ncb);
+    k_stage_z_split<<<(unsigned)grid, kZThreads, 0, stream>>>(a, ncb, r0, r1);
   }
   return check_launch(direction == MW_DIR_X ? "x split direction-stage launch" : "z split direction-stage launch");
 }

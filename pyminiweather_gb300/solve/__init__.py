@@ -7,4 +7,4 @@ from .interpolate import (  # noqa: F401
     interpolate_z,
 )
 from .source import add_source_terms  # noqa: F401
-from .step import discrete_step, evolve, reset_direction  # noqa: F401
+from .step import discrete_step, evolve, evolve_host, reset_direction  # noqa: F401

@@ -104,3 +104,37 @@ def evolve(params: Dict, fields, mesh=None, dt: float = 1e-4, nsteps: int = 1) -
     else:
         _native.call("mw_step_f32", *args, flags, _native.stream_handle(fields.device))
     reverse_direction = bool(rv.value)
+
+
+def evolve_host(params: Dict, fields, h_in: torch.Tensor, h_out: torch.Tensor, dt: float = 1e-4,
+                nbands: int = 16) -> None:
+    """One time step of a state held in host memory: h_in (a CPU tensor of the
+    state's shape, ideally pinned) is copied into fields.state, the step runs as
+    evolve() would run it, and the new state is copied into h_out (may be
+    h_in).  The FP64 split form overlaps the copies with the step by row bands
+    (mw_step_f64_host); other forms copy, step and copy.  Returns once the work
+    is enqueued on the current stream; synchronise before reading h_out."""
+    global reverse_direction
+    for name, h in (("h_in", h_in), ("h_out", h_out)):
+        if not isinstance(h, torch.Tensor) or h.device.type != "cpu" or tuple(h.shape) != tuple(fields.shape) \
+                or h.dtype != fields.dtype or not h.is_contiguous():
+            raise ValueError("%s must be a contiguous CPU tensor of shape %s and dtype %s"
+                             % (name, tuple(fields.shape), fields.dtype))
+    if fields.dtype != torch.float64:
+        fields.state.copy_(h_in, non_blocking=True)
+        evolve(params, fields, None, dt=dt)
+        h_out.copy_(fields.state, non_blocking=True)
+        return
+    _check_state(fields, fields.state, "fields.state")
+    _check_state(fields, fields.state_tmp, "fields.state_tmp")
+    _check_state(fields, fields.scratch, "fields.scratch")
+    rv = ctypes.c_int(1 if reverse_direction else 0)
+    hb = [_native.ptr(a) for a in fields.backgrounds()]
+    flags = params.get("step_flags", _native.MW_FLAG_WRITE_HALO)
+    _native.call("mw_step_f64_host", fields.nx, fields.nz, float(params["dx"]), float(params["dz"]),
+                 float(params["dt"]), float(dt), *hb, _native.ptr(fields.src_w), ctypes.c_void_p(h_in.data_ptr()),
+                 ctypes.c_void_p(h_out.data_ptr()), _native.ptr(fields.state), _native.ptr(fields.state_tmp),
+                 _native.ptr(fields.scratch), ctypes.byref(rv), f64_mode(params), flags, int(nbands),
+                 _native.stream_handle(fields.device))
+    reverse_direction = bool(rv.value)
+

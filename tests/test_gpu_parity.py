@@ -312,3 +312,55 @@ def test_errors_surface_as_exceptions():
     with pytest.raises(NotImplementedError):
         evolve(dict(p, ic_type="injection"), f, None, dt=p["dt"])
     torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("nx,nz,nbands,flags", [(512, 256, 8, 1), (300, 150, 16, 1), (300, 150, 4, 0), (64, 40, 8, 1),
+                                                (100, 20, 8, 1)])
+def test_host_step_matches_copy_step_copy(nx, nz, nbands, flags):
+    """evolve_host (copies overlapped with the step by row bands) against copy-in,
+    evolve, copy-out: bit-identical states and host results for both direction
+    orders, halo writes on and off, and h_out aliasing h_in."""
+    import pyminiweather_gb300.solve.step as S
+    from pyminiweather_gb300.solve import evolve_host
+    p = make_params(nx, nz, "collision")
+    p["step_flags"] = flags
+    ref = initialize_fields(p)
+    init(ref, p, None)
+    evolve(dict(p, f64_mode="split"), ref, None, dt=p["dt"], nsteps=1)  # a developed state with nonzero halos
+    h0 = ref.state.cpu().pin_memory()
+    got = initialize_fields(p)
+    init(got, p, None)
+    reset_direction()
+    h_in, h_out = h0.clone().pin_memory(), torch.empty_like(h0).pin_memory()
+    ref.state.copy_(h0)
+    for step in range(3):  # both direction orders
+        src = h_in if step == 0 else h_out  # later steps read and write the same host array
+        rd = S.reverse_direction
+        ref.state.copy_(src)  # the reference sequence: copy in, step, copy out
+        S.reverse_direction = rd
+        evolve(p, ref, None, dt=p["dt"])
+        h_ref = ref.state.cpu()
+        S.reverse_direction = rd
+        evolve_host(p, got, src, h_out, dt=p["dt"], nbands=nbands)
+        torch.cuda.synchronize()
+        assert torch.equal(h_out, h_ref), step
+        assert torch.equal(got.state, ref.state) and torch.equal(got.state_tmp, ref.state_tmp), step
+
+
+def test_host_step_fp32_and_native_forms():
+    from pyminiweather_gb300.solve import evolve_host
+    for dtype, mode in ((torch.float32, "split"), (torch.float64, "native")):
+        p = make_params(64, 32, "thermal")
+        p["f64_mode"] = mode
+        a = initialize_fields(p, dtype=dtype)
+        init(a, p, None)
+        b = initialize_fields(p, dtype=dtype)
+        init(b, p, None)
+        h = a.state.cpu().pin_memory()
+        out = torch.empty_like(h).pin_memory()
+        reset_direction()
+        evolve(p, a, None, dt=p["dt"])
+        reset_direction()
+        evolve_host(p, b, h, out, dt=p["dt"])
+        torch.cuda.synchronize()
+        assert torch.equal(out, a.state.cpu())
