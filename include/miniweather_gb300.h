@@ -57,6 +57,10 @@ enum mw_f64_mode {
 #define MW_FLAG_INDEX64 2u    /* split form: use the 64-bit-index kernels even
                                  when 32-bit indices suffice (for testing; arrays
                                  of 2^31 or more values always use them) */
+#define MW_FLAG_CHECK_FINITE 4u /* mw_step_f64 / _f32: after the steps, count the
+                                 non-finite interior values of the state and
+                                 return MW_ERR_NONFINITE if there are any
+                                 (synchronises the stream to read the count) */
 
 /* Background profile of the initial condition. */
 enum mw_background {
@@ -265,6 +269,11 @@ int mw_gravity_source_f64(int nx, int nz, double xlen, double zlen, const double
  * in a fixed order (deterministic).  workspace must hold
  * mw_stats_workspace_bytes(nx, nz) bytes.
  * ------------------------------------------------------------------------- */
+/* Count the non-finite (NaN, +-Inf) interior values of a (4, nz+4, nx+4)
+ * state into *count (a device counter, added to, not reset); no host sync. */
+int mw_count_nonfinite_f64(int nx, int nz, const double* state, unsigned long long* count, void* stream);
+int mw_count_nonfinite_f32(int nx, int nz, const float* state, unsigned long long* count, void* stream);
+
 size_t mw_stats_workspace_bytes(int nx, int nz);
 int mw_stats_f64(int nx, int nz, double dx, double dz, const double* hy_dens_cell, const double* hy_dens_theta_cell,
                  const double* state, void* workspace, size_t workspace_bytes, double* out2, void* stream);

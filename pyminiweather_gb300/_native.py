@@ -22,6 +22,7 @@ MW_DIR_X, MW_DIR_Z = 0, 1
 MW_F64_NATIVE, MW_F64_SPLIT = 0, 1
 MW_FLAG_WRITE_HALO = 1
 MW_FLAG_INDEX64 = 2
+MW_FLAG_CHECK_FINITE = 4
 MW_BG_CONST_THETA, MW_BG_BVFREQ = 0, 1
 MW_MAX_BUBBLES = 8
 
@@ -55,6 +56,8 @@ _SIGNATURES = {
     "mw_stats_f64": [_i, _i, _d, _d, _P, _P, _P, _P, _sz, _P, _P],
     "mw_stats_f32": [_i, _i, _d, _d, _P, _P, _P, _P, _sz, _P, _P],
     "mw_solution_variables_f64": [_i, _i, _P, _P, _P, _P, _P],
+    "mw_count_nonfinite_f64": [_i, _i, _P, _P, _P],
+    "mw_count_nonfinite_f32": [_i, _i, _P, _P, _P],
     "mw_savetxt_f64": [_P, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_char_p, _i, _i],
     "mw_set_bc_f64": [_i, _i, _P, _P, _i, _P],
     "mw_interpolate_f64": [_i, _i, _P, _P, _P, _i, _P],

@@ -6,6 +6,8 @@
 // operation with explicitly rounded intrinsics (__dadd_rn, __dmul_rn, ...),
 // so that no multiply-add is contracted and results round exactly as NumPy's
 // do, pow and cos aside.
+#include <algorithm>
+
 #include "mw_common.cuh"
 #include "mw_split.cuh"
 
@@ -609,3 +611,64 @@ extern "C" int mw_add_source_f64(int nx, int nz, const double* src_w, double* te
   k_add_source<<<grid_for((long long)nx * nz, 256), 256, 0, (cudaStream_t)stream>>>(nx, nz, src_w, tend);
   return check_launch("add_source launch");
 }
+
+// ---------------------------------------------------------------------------
+// Non-finite values of the interior (failure detection after a step).
+namespace mw {
+namespace {
+template <typename T>
+__global__ void k_count_nonfinite(int nx, int nz, const T* s, unsigned long long* count) {
+  const int pitch = nx + 2 * kHs;
+  const long long plane = (long long)(nz + 2 * kHs) * pitch;
+  const long long n = 4LL * nz * nx;
+  unsigned c = 0;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const long long q = e / ((long long)nz * nx), r = e - q * nz * nx;
+    const int k = (int)(r / nx), i = (int)(r - (long long)k * nx);
+    const T v = s[q * plane + (long long)(k + kHs) * pitch + i + kHs];
+    c += !isfinite(v);
+  }
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, (unsigned long long)c);
+}
+
+template <typename T>
+int count_nonfinite(int nx, int nz, const T* state, unsigned long long* count, cudaStream_t stream) {
+  int st = check_grid(nx, nz);
+  if (st) return st;
+  MW_REQUIRE(state && count, MW_ERR_INVALID_ARG, "NULL pointer argument");
+  const long long n = 4LL * nz * nx;
+  const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 8);
+  k_count_nonfinite<T><<<(unsigned)blocks, 256, 0, stream>>>(nx, nz, state, count);
+  return check_launch("non-finite count launch");
+}
+}  // namespace
+
+// The MW_FLAG_CHECK_FINITE tail of the step entry points (blocking).
+template <typename T>
+int check_finite_blocking(int nx, int nz, const T* state, cudaStream_t stream) {
+  unsigned long long* d = nullptr;
+  unsigned long long h = 0;
+  cudaError_t e = cudaMallocAsync((void**)&d, sizeof(*d), stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d, 0, sizeof(*d), stream);
+  if (e != cudaSuccess) return fail(MW_ERR_CUDA, "non-finite check: %s", cudaGetErrorString(e));
+  int st = count_nonfinite(nx, nz, state, d, stream);
+  e = cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, stream);
+  cudaError_t e2 = cudaFreeAsync(d, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  if (st) return st;
+  if (e != cudaSuccess || e2 != cudaSuccess) return fail(MW_ERR_CUDA, "non-finite check: %s", cudaGetErrorString(e));
+  if (h) return fail(MW_ERR_NONFINITE, "%llu non-finite interior values in the state after the step", h);
+  return MW_OK;
+}
+template int check_finite_blocking<double>(int, int, const double*, cudaStream_t);
+template int check_finite_blocking<float>(int, int, const float*, cudaStream_t);
+}  // namespace mw
+
+extern "C" int mw_count_nonfinite_f64(int nx, int nz, const double* state, unsigned long long* count, void* stream) {
+  return mw::count_nonfinite(nx, nz, state, count, (cudaStream_t)stream);
+}
+extern "C" int mw_count_nonfinite_f32(int nx, int nz, const float* state, unsigned long long* count, void* stream) {
+  return mw::count_nonfinite(nx, nz, state, count, (cudaStream_t)stream);
+}
+

@@ -594,6 +594,10 @@ static int launch_stage(int nx, int nz, double dx, double dz, double dt_full, co
   return check_launch(direction == MW_DIR_X ? "x direction-stage launch" : "z direction-stage launch");
 }
 
+// MW_FLAG_CHECK_FINITE: count non-finite interior values, blocking (mw_aux.cu).
+template <typename T>
+int check_finite_blocking(int nx, int nz, const T* state, cudaStream_t stream);
+
 // Split-arithmetic launches live in mw_split_stage.cu.
 int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
                        const double* hyi, const double* hyti, const double* hypi, const double* srcw,
@@ -682,11 +686,13 @@ extern "C" int mw_step_f64(int nx, int nz, double dx, double dz, double dt_full,
   MW_REQUIRE(f64_mode == MW_F64_NATIVE || f64_mode == MW_F64_SPLIT, MW_ERR_INVALID_ARG, "unknown f64_mode %d",
              f64_mode);
   cudaStream_t s = (cudaStream_t)stream;
-  return run_steps<double>(dt, state, state_tmp, scratch, nsteps, reverse,
-                           [&](const double* init, double* forcing, double* out, double dts, int dir) {
-                             return stage_f64(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, src_w, init, forcing,
-                                              out, dts, dir, f64_mode, flags, s);
-                           });
+  st = run_steps<double>(dt, state, state_tmp, scratch, nsteps, reverse,
+                         [&](const double* init, double* forcing, double* out, double dts, int dir) {
+                           return stage_f64(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, src_w, init, forcing,
+                                            out, dts, dir, f64_mode, flags, s);
+                         });
+  if (st == MW_OK && nsteps > 0 && (flags & MW_FLAG_CHECK_FINITE)) st = check_finite_blocking(nx, nz, (const double*)state, s);
+  return st;
 }
 
 extern "C" int mw_step_f32(int nx, int nz, double dx, double dz, double dt_full, double dt, const double* hyc,
@@ -699,11 +705,13 @@ extern "C" int mw_step_f32(int nx, int nz, double dx, double dz, double dt_full,
   MW_REQUIRE(finite_pos(dt), MW_ERR_INVALID_ARG, "dt must be finite and positive");
   if (st) return st;
   cudaStream_t s = (cudaStream_t)stream;
-  return run_steps<float>(dt, state, state_tmp, scratch, nsteps, reverse,
-                          [&](const float* init, float* forcing, float* out, double dts, int dir) {
-                            return launch_stage<float, MODE_F32>(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi,
-                                                                 src_w, init, forcing, out, dts, dir, flags, s);
-                          });
+  st = run_steps<float>(dt, state, state_tmp, scratch, nsteps, reverse,
+                        [&](const float* init, float* forcing, float* out, double dts, int dir) {
+                          return launch_stage<float, MODE_F32>(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi,
+                                                               src_w, init, forcing, out, dts, dir, flags, s);
+                        });
+  if (st == MW_OK && nsteps > 0 && (flags & MW_FLAG_CHECK_FINITE)) st = check_finite_blocking(nx, nz, (const float*)state, s);
+  return st;
 }
 
 // ---------------------------------------------------------------------------

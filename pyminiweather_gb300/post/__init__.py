@@ -1,1 +1,1 @@
-from .stats import compute_solution_variables, compute_stats, compute_stats_device  # noqa: F401
+from .stats import compute_solution_variables, compute_stats, compute_stats_device, count_nonfinite  # noqa: F401

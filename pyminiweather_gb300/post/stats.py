@@ -49,3 +49,15 @@ def compute_solution_variables(params: Dict, fields) -> torch.Tensor:
                  _native.ptr(fields.hy_dens_theta_cell), _native.ptr(st), _native.ptr(out),
                  _native.stream_handle(fields.device))
     return out
+
+
+def count_nonfinite(fields, state: torch.Tensor = None) -> int:
+    """Number of NaN / Inf interior values of the state (or of `state`, an
+    array of the state's shape and dtype); synchronises to read the count."""
+    st = fields.state if state is None else state
+    _native.require_cuda(st, "state", dtype=fields.dtype, shape=fields.shape)
+    count = torch.zeros(1, dtype=torch.int64, device=st.device)
+    fn = "mw_count_nonfinite_f64" if st.dtype == torch.float64 else "mw_count_nonfinite_f32"
+    _native.call(fn, fields.nx, fields.nz, _native.ptr(st), _native.ptr(count), _native.stream_handle(st.device))
+    return int(count.item())
+

@@ -85,7 +85,9 @@ def discrete_step(params: Dict, fields, mesh, state_init, state_forcing, state_o
 def evolve(params: Dict, fields, mesh=None, dt: float = 1e-4, nsteps: int = 1) -> None:
     """Advance fields.state by nsteps time steps of size dt (step.py:85-143).
 
-    Hyperviscosity uses params["dt"], as in the reference.
+    Hyperviscosity uses params["dt"], as in the reference.  With
+    params["check_finite"] the state is checked for NaN / Inf after the steps
+    (synchronising) and MiniWeatherError with status MW_ERR_NONFINITE is raised.
     """
     global reverse_direction
     _check_state(fields, fields.state, "fields.state")
@@ -99,6 +101,8 @@ def evolve(params: Dict, fields, mesh=None, dt: float = 1e-4, nsteps: int = 1) -
             _native.ptr(fields.src_w), _native.ptr(fields.state), _native.ptr(fields.state_tmp),
             _native.ptr(fields.scratch), int(nsteps), ctypes.byref(rv)]
     flags = params.get("step_flags", _native.MW_FLAG_WRITE_HALO)
+    if params.get("check_finite"):  # blocking: raises MiniWeatherError (status 7) on NaN / Inf
+        flags |= _native.MW_FLAG_CHECK_FINITE
     if fields.dtype == torch.float64:
         _native.call("mw_step_f64", *args, f64_mode(params), flags, _native.stream_handle(fields.device))
     else:

@@ -364,3 +364,26 @@ def test_host_step_fp32_and_native_forms():
         evolve_host(p, b, h, out, dt=p["dt"])
         torch.cuda.synchronize()
         assert torch.equal(out, a.state.cpu())
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_nonfinite_detection(dtype):
+    """Failure detection without a GPU fault: NaN / Inf planted on the host side
+    into the state are counted on the device, and a step with check_finite set
+    reports MW_ERR_NONFINITE (status 7) instead of returning quietly."""
+    from pyminiweather_gb300.post import count_nonfinite
+    p = make_params(48, 24, "collision")
+    f = initialize_fields(p, dtype=dtype)
+    init(f, p, None)
+    assert count_nonfinite(f) == 0
+    evolve(dict(p, check_finite=True), f, None, dt=p["dt"])  # a healthy step passes the check
+    bad = f.state.clone()
+    bad[0, 2 + 5, 2 + 7] = float("nan")
+    bad[3, 2 + 20, 2 + 40] = float("inf")
+    bad[1, 0, 0] = float("nan")  # a halo cell: not counted
+    assert count_nonfinite(f, bad) == 2
+    f.state.copy_(bad)
+    with pytest.raises(_native.MiniWeatherError) as ei:
+        evolve(dict(p, check_finite=True), f, None, dt=p["dt"])
+    assert ei.value.status == 7
+    assert count_nonfinite(f) > 2  # the NaN spread through the stencil
