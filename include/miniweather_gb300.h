@@ -269,6 +269,15 @@ int mw_gravity_source_f64(int nx, int nz, double xlen, double zlen, const double
  * in a fixed order (deterministic).  workspace must hold
  * mw_stats_workspace_bytes(nx, nz) bytes.
  * ------------------------------------------------------------------------- */
+/* Bounds-checked build (compiled with MW_CHECK=1, python -m pyminiweather_gb300.build
+ * --check): the split-form stage, ensemble and adjoint kernels count every array
+ * index outside its array instead of accessing it.  mw_debug_oob_count adds up
+ * that count (and resets it if asked); mw_debug_oob_selftest launches one
+ * deliberately out-of-range access that the check diverts (the count goes up by
+ * one).  Both fail with MW_ERR_INVALID_ARG in the normal build. */
+int mw_debug_oob_count(unsigned long long* count, int reset);
+int mw_debug_oob_selftest(void* stream);
+
 /* Count the non-finite (NaN, +-Inf) interior values of a (4, nz+4, nx+4)
  * state into *count (a device counter, added to, not reset); no host sync. */
 int mw_count_nonfinite_f64(int nx, int nz, const double* state, unsigned long long* count, void* stream);

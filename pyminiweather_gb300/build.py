@@ -1,6 +1,11 @@
 """Build libminiweather_gb300.so from csrc/*.cu for sm_103a, in-tree.
 
-    python -m pyminiweather_gb300.build [--force] [--ptxas-info]
+    python -m pyminiweather_gb300.build [--force] [--ptxas-info] [--check]
+
+With --check (or MW_LIBRARY_VARIANT=check in the environment of the process
+that loads the package) the bounds-checked debug library
+libminiweather_gb300_check.so is built (MW_CHECK=1: the split-form kernels
+count out-of-range indices instead of accessing memory there) and loaded.
 
 Each translation unit is compiled by nvcc in parallel and linked into
 pyminiweather_gb300/_lib/libminiweather_gb300.so (static CUDA runtime).  The
@@ -20,14 +25,25 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
-BUILD_DIR = os.path.join(PKG, "_build")
 LIB_DIR = os.path.join(PKG, "_lib")
-LIB_NAME = "libminiweather_gb300.so"
-LIB_PATH = os.path.join(LIB_DIR, LIB_NAME)
-
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+BASE_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
                      "-I" + INCLUDE]
+
+
+def configure(variant: str) -> None:
+    """Select the library variant: "" (the product) or "check" (bounds-checked)."""
+    global VARIANT, BUILD_DIR, LIB_NAME, LIB_PATH, NVCC_FLAGS
+    if variant not in ("", "check"):
+        raise ValueError("unknown library variant %r (expected '' or 'check')" % variant)
+    VARIANT = variant
+    BUILD_DIR = os.path.join(PKG, "_build", variant) if variant else os.path.join(PKG, "_build")
+    LIB_NAME = "libminiweather_gb300%s.so" % ("_" + variant if variant else "")
+    LIB_PATH = os.path.join(LIB_DIR, LIB_NAME)
+    NVCC_FLAGS = BASE_FLAGS + (["-DMW_CHECK=1"] if variant == "check" else [])
+
+
+configure(os.environ.get("MW_LIBRARY_VARIANT", ""))
 
 
 def nvcc() -> str:
@@ -87,5 +103,8 @@ if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--force", action="store_true")
     ap.add_argument("--ptxas-info", action="store_true")
+    ap.add_argument("--check", action="store_true", help="build the bounds-checked debug library")
     a = ap.parse_args()
+    if a.check:
+        configure("check")
     print(build(force=a.force, ptxas_info=a.ptxas_info, verbose=True))

@@ -69,15 +69,15 @@ __global__ void k_vjp_row_table(const double* hyc, const double* hytc, const dou
     double rho, rt, P;
     RowV* dst;
     if (r < nz) {  // x rows: cell-centre background, P = C0 (rho theta)^gamma
-      rho = hyc[r + kHs];
-      rt = hytc[r + kHs];
+      rho = MW_AT(hyc, r + kHs, nz + 2 * kHs);
+      rt = MW_AT(hytc, r + kHs, nz + 2 * kHs);
       P = kC0 * pow(rt, kGamma);
       dst = tx + r;
     } else {       // z interfaces
       const int k = r - nz;
-      rho = hyi[k];
-      rt = hyti[k];
-      P = hypi[k];
+      rho = MW_AT(hyi, k, nz + 1);
+      rt = MW_AT(hyti, k, nz + 1);
+      P = MW_AT(hypi, k, nz + 1);
       dst = tz + k;
     }
     RowV v;
@@ -134,14 +134,14 @@ template <int DIR>
 __device__ __forceinline__ double fval(const VjpSplitArgs& a, int q, int line, int p) {
   if (DIR == MW_DIR_X) {
     const int c = ((p % a.nx) + a.nx) % a.nx;
-    return a.forcing[q * a.plane + (long long)(line + kHs) * a.pitch + c + kHs];
+    return MW_AT(a.forcing, q * a.plane + (long long)(line + kHs) * a.pitch + c + kHs, 4 * a.plane);
   }
   const int col = line + kHs;
-  if (p >= 0 && p < a.nz) return a.forcing[q * a.plane + (long long)(p + kHs) * a.pitch + col];
+  if (p >= 0 && p < a.nz) return MW_AT(a.forcing, q * a.plane + (long long)(p + kHs) * a.pitch + col, 4 * a.plane);
   if (q == WMOM) return 0.0;
   const int src = p < 0 ? kHs : a.nz + kHs - 1;
-  const double s = a.forcing[q * a.plane + (long long)src * a.pitch + col];
-  if (q == UMOM) return s / a.hyc[src] * a.hyc[p + kHs];
+  const double s = MW_AT(a.forcing, q * a.plane + (long long)src * a.pitch + col, 4 * a.plane);
+  if (q == UMOM) return s / MW_AT(a.hyc, src, a.nz + 2 * kHs) * MW_AT(a.hyc, p + kHs, a.nz + 2 * kHs);
   return s;
 }
 
@@ -162,13 +162,13 @@ __device__ __forceinline__ void gload(const VjpSplitArgs& a, int line, int p, do
   }
   const long long o = cell_off<DIR>(a, line, p);
 #pragma unroll
-  for (int q = 0; q < 4; ++q) v[q] = a.gout[q * a.plane + o];
+  for (int q = 0; q < 4; ++q) v[q] = MW_AT(a.gout, q * a.plane + o, 4 * a.plane);
 }
 
 // Weight of a halo-row tap (row h) on its source row in z, for UMOM.
 __device__ __forceinline__ dw halo_umom_weight(const VjpSplitArgs& a, int h) {
   const int src = h < 0 ? kHs : a.nz + kHs - 1;
-  return from_f64(a.hyc[h + kHs] / a.hyc[src]);
+  return from_f64(MW_AT(a.hyc, h + kHs, a.nz + 2 * kHs) / MW_AT(a.hyc, src, a.nz + 2 * kHs));
 }
 
 // T_j(f) = c12_j AbG(f) - e_j 12hv Gd(f) for one (AbG, Gd) pair of a variable pair.
@@ -242,7 +242,7 @@ __device__ __forceinline__ void vjp_segments(const VjpSplitArgs& a, int nseg, lo
 #pragma unroll
           for (int j = 0; j < 4; ++j) s[pr][j] = sm.sS[w][pr][lane + j];
         const int ri = DIR == MW_DIR_X ? line : f;
-        const RowV rv = a.rows[ri];
+        const RowV rv = MW_AT(a.rows, ri, DIR == MW_DIR_X ? a.nz : a.nz + 1);
         const bool wall = DIR == MW_DIR_Z && (f == 0 || f == a.nz);
         jt_g<DIR>(s, rv, Gd, wall, Ab);
         if (wall) {
@@ -290,12 +290,12 @@ __device__ __forceinline__ void vjp_segments(const VjpSplitArgs& a, int nseg, lo
       for (int q = 0; q < 4; ++q) {
         const long long oq = q * a.plane + o;
         double base = 0.0;
-        if (a.add_gout) base += a.gout[oq];
-        if (a.base_a) base += a.base_a[oq];
-        if (a.base_b) base += a.base_b[oq];
+        if (a.add_gout) base += MW_AT(a.gout, oq, 4 * a.plane);
+        if (a.base_a) base += MW_AT(a.base_a, oq, 4 * a.plane);
+        if (a.base_b) base += MW_AT(a.base_b, oq, 4 * a.plane);
         double v = fma(a.cs, to_f64_scaled(d[q]), base);
-        if (DIR == MW_DIR_Z && q == DENS) v = fma(-a.dtg, a.gout[WMOM * a.plane + o], v);
-        a.gdst[oq] = v;
+        if (DIR == MW_DIR_Z && q == DENS) v = fma(-a.dtg, MW_AT(a.gout, WMOM * a.plane + o, 4 * a.plane), v);
+        MW_AT(a.gdst, oq, 4 * a.plane) = v;
       }
     }
     __syncwarp();
@@ -317,7 +317,7 @@ __device__ __forceinline__ void zero_frame(const VjpSplitArgs& a) {
       o = (long long)(k + kHs) * a.pitch + (h < kHs ? h : a.nx + h);
     }
 #pragma unroll
-    for (int q = 0; q < 4; ++q) a.gdst[q * a.plane + o] = 0.0;
+    for (int q = 0; q < 4; ++q) MW_AT(a.gdst, q * a.plane + o, 4 * a.plane) = 0.0;
   }
 }
 
@@ -342,6 +342,10 @@ int vjp_resident_ctas(int* out) {
 }
 
 }  // namespace
+
+#if MW_CHECK
+MW_OOB_COUNTER(oob_count_adjoint_split)
+#endif
 
 size_t vjp_split_table_bytes(int nz) { return sizeof(RowV) * (size_t)(2 * nz + 1); }
 

@@ -53,3 +53,42 @@ extern "C" const char* mw_status_string(int status) {
 }
 
 extern "C" int mw_abi_version(void) { return MW_ABI_VERSION; }
+
+// ---------------------------------------------------------------------------
+// Bounds-checked build: out-of-range index count of the checked kernels.
+#if MW_CHECK
+namespace mw {
+int oob_count_split_stage(unsigned long long* out, bool reset);
+int oob_count_adjoint_split(unsigned long long* out, bool reset);
+namespace {
+__global__ void k_oob_selftest(double* p, int n) { MW_AT(p, n, n) = 1.0; }  // one index past the end
+}  // namespace
+MW_OOB_COUNTER(oob_count_capi)
+}  // namespace mw
+#endif
+
+extern "C" int mw_debug_oob_count(unsigned long long* count, int reset) {
+  MW_REQUIRE(count != nullptr, MW_ERR_INVALID_ARG, "count must not be NULL");
+  *count = 0;
+#if MW_CHECK
+  int st;
+  if ((st = mw::oob_count_split_stage(count, reset != 0)) || (st = mw::oob_count_adjoint_split(count, reset != 0)) ||
+      (st = mw::oob_count_capi(count, reset != 0)))
+    return st;
+  return MW_OK;
+#else
+  (void)reset;
+  return mw::fail(MW_ERR_INVALID_ARG, "not a bounds-checked build (build with MW_CHECK=1)");
+#endif
+}
+
+extern "C" int mw_debug_oob_selftest(void* stream) {
+#if MW_CHECK
+  mw::k_oob_selftest<<<1, 1, 0, (cudaStream_t)stream>>>(nullptr, 4);  // the access goes to the sink
+  return mw::check_launch("oob self-test launch");
+#else
+  (void)stream;
+  return mw::fail(MW_ERR_INVALID_ARG, "not a bounds-checked build (build with MW_CHECK=1)");
+#endif
+}
+

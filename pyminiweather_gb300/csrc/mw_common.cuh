@@ -11,7 +11,45 @@
 
 #include "../../include/miniweather_gb300.h"
 
+// MW_CHECK=1 builds the bounds-checked library (a debug build): the kernels
+// that access memory through MW_AT count every index outside its array
+// instead of touching memory there, and mw_debug_oob_count reads the count.
+#ifndef MW_CHECK
+#define MW_CHECK 0
+#endif
+
 namespace mw {
+
+#if MW_CHECK
+static __device__ unsigned long long g_oob_count;           // per translation unit
+static __device__ __align__(16) unsigned char g_oob_sink[64];  // stands in for out-of-range elements
+
+template <typename T, typename I>
+__device__ __forceinline__ T& checked_at(T* p, I i, long long n) {
+  static_assert(sizeof(T) <= sizeof(g_oob_sink), "element larger than the sink");
+  if ((long long)i < 0 || (long long)i >= n) {
+    atomicAdd(&g_oob_count, 1ULL);
+    return *reinterpret_cast<T*>(g_oob_sink);
+  }
+  return p[i];
+}
+#define MW_AT(p, i, n) (::mw::checked_at((p), (i), (long long)(n)))
+// Adds this translation unit's count to *out (and resets it).
+#define MW_OOB_COUNTER(fn)                                                          \
+  int fn(unsigned long long* out, bool reset) {                                     \
+    unsigned long long v = 0;                                                       \
+    cudaError_t e = cudaMemcpyFromSymbol(&v, g_oob_count, sizeof(v));               \
+    if (e == cudaSuccess && reset) {                                                \
+      const unsigned long long z = 0;                                               \
+      e = cudaMemcpyToSymbol(g_oob_count, &z, sizeof(z));                           \
+    }                                                                               \
+    if (e != cudaSuccess) return fail(MW_ERR_CUDA, "oob counter: %s", cudaGetErrorString(e)); \
+    *out += v;                                                                      \
+    return MW_OK;                                                                   \
+  }
+#else
+#define MW_AT(p, i, n) ((p)[(i)])
+#endif
 
 // Physical constants, pyminiweather/data/constants.py:13-27.
 constexpr double kHvBeta = 0.05;

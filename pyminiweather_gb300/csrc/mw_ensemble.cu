@@ -119,6 +119,8 @@ int ens_step(void* plan, const mw_ens_plan_info* info, const double* hyc, const 
   const int2* xi = (const int2*)((const char*)plan + info->x_items_off);
   const int2* zi = (const int2*)((const char*)plan + info->z_items_off);
   es.xrows = (const char*)plan + info->xrows_off;
+  es.n_xrows = info->n_xrows;
+  es.n_members = info->n_members;
   if (std::is_same<T, double>::value && nsteps > 0 &&
       (st = launch_ens_split_rowtable(hyc, hytc, info->n_xrows, (char*)plan + info->xrows_off, stream)))
     return st;

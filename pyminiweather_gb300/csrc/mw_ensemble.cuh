@@ -27,6 +27,8 @@ struct EnsStageT {
   T* forcing;
   T* out;
   const void* xrows;  // split form: row constants indexed like the cell-centre backgrounds
+  long long n_xrows;  // entries of xrows
+  int n_members;
   cudaStream_t stream;
 };
 using EnsStage = EnsStageT<double>;

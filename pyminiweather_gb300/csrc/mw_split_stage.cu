@@ -50,8 +50,8 @@ static_assert(sizeof(RowS) == kEnsRowBytes, "row-constant table entry size");
 
 __global__ void k_ens_row_table(const double* hyc, const double* hytc, long long n, RowS* table) {
   for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x) {
-    const double hrt = hytc[j];
-    table[j] = row_consts(hyc[j], hrt, kC0 * pow(hrt, kGamma));
+    const double hrt = MW_AT(hytc, j, n);
+    MW_AT(table, j, n) = row_consts(MW_AT(hyc, j, n), hrt, kC0 * pow(hrt, kGamma));
   }
 }
 
@@ -62,6 +62,10 @@ int launch_ens_split_rowtable(const double* hyc, const double* hytc, long long n
   k_ens_row_table<<<(unsigned)blocks, 128, 0, stream>>>(hyc, hytc, n, (RowS*)table);
   return check_launch("ensemble row-table launch");
 }
+
+#if MW_CHECK
+MW_OOB_COUNTER(oob_count_split_stage)
+#endif
 
 // Ensemble members are planned with fewer than 2^31 elements per state array.
 int launch_ens_split(const EnsStage& es, int grid) { return s32::launch_ens_split(es, grid); }

@@ -20,7 +20,7 @@ constexpr int kXRowsMax = 64;        // rows of one x CTA's range (row-constant 
 
 struct SplitArgs {
   int nx, nz, pitch;
-  long long plane;
+  sidx plane;  // 32-bit in the instance for arrays of fewer than 2^31 values
   const double* hyc;
   const double* hytc;
   const double* hyi;
@@ -38,11 +38,11 @@ struct SplitArgs {
 };
 
 __device__ __forceinline__ double zval64(const SplitArgs& a, int q, int k, int col) {
-  if (k >= 0 && k < a.nz) return a.forcing[q * (sidx)a.plane + (sidx)(k + kHs) * a.pitch + col];
+  if (k >= 0 && k < a.nz) return MW_AT(a.forcing, q * (sidx)a.plane + (sidx)(k + kHs) * a.pitch + col, 4 * (long long)a.plane);
   if (q == WMOM) return 0.0;
   const int src = k < 0 ? kHs : a.nz + kHs - 1;
-  const double s = a.forcing[q * (sidx)a.plane + (sidx)src * a.pitch + col];
-  if (q == UMOM) return s / a.hyc[src] * a.hyc[k + kHs];
+  const double s = MW_AT(a.forcing, q * (sidx)a.plane + (sidx)src * a.pitch + col, 4 * (long long)a.plane);
+  if (q == UMOM) return s / MW_AT(a.hyc, src, a.nz + 2 * kHs) * MW_AT(a.hyc, k + kHs, a.nz + 2 * kHs);
   return s;
 }
 
@@ -56,8 +56,8 @@ __device__ __forceinline__ void write_z_halo_column(const SplitArgs& a, int col,
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const double v0 = zval64(a, q, r0, col), v1 = zval64(a, q, r0 + 1, col);
-      a.forcing[q * (sidx)a.plane + (sidx)(r0 + kHs) * a.pitch + col] = v0;
-      a.forcing[q * (sidx)a.plane + (sidx)(r0 + 1 + kHs) * a.pitch + col] = v1;
+      MW_AT(a.forcing, q * (sidx)a.plane + (sidx)(r0 + kHs) * a.pitch + col, 4 * (long long)a.plane) = v0;
+      MW_AT(a.forcing, q * (sidx)a.plane + (sidx)(r0 + 1 + kHs) * a.pitch + col, 4 * (long long)a.plane) = v1;
     }
   }
 }
@@ -89,7 +89,7 @@ __device__ __forceinline__ void store_update(const SplitArgs& a, sidx o, const d
     for (int q = 0; q < 4; ++q) v[q] = update(iv[q], d[q], a.c12s);
   }
 #pragma unroll
-  for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = v[q];
+  for (int q = 0; q < 4; ++q) MW_AT(a.out, q * a.plane + o, 4 * (long long)a.plane) = v[q];
 }
 
 // x, single grid: the CTA owns the contiguous range [g0, g1) of the row-major
@@ -107,8 +107,8 @@ struct SmemXW {
 };
 
 __device__ __forceinline__ RowS x_row_consts(const SplitArgs& a, int k) {
-  const double hrt = a.hytc[k + kHs];
-  return row_consts(a.hyc[k + kHs], hrt, kC0 * pow(hrt, kGamma));
+  const double hrt = MW_AT(a.hytc, k + kHs, a.nz + 2 * kHs);
+  return row_consts(MW_AT(a.hyc, k + kHs, a.nz + 2 * kHs), hrt, kC0 * pow(hrt, kGamma));
 }
 
 // row_at(k): the row constants of row k.
@@ -130,9 +130,9 @@ __device__ __forceinline__ void x_warp_segments(const SplitArgs& a, int nseg, lo
     if (c0 <= a.nx + 1) {
       const sidx col = wrap_x(c0, a.nx) + kHs;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) v0[q] = __ldg(a.forcing + q * a.plane + row + col);
+      for (int q = 0; q < 4; ++q) v0[q] = __ldg(&MW_AT(a.forcing, q * a.plane + row + col, 4 * (long long)a.plane));
     }
-    if (lane < 12 && c1 <= a.nx + 1) v1 = __ldg(a.forcing + xq * a.plane + row + wrap_x(c1, a.nx) + kHs);
+    if (lane < 12 && c1 <= a.nx + 1) v1 = __ldg(&MW_AT(a.forcing, xq * a.plane + row + wrap_x(c1, a.nx) + kHs, 4 * (long long)a.plane));
   };
   double v0[4] = {0, 0, 0, 0}, v1 = 0.0;
   load(k, sg * kWCells, v0, v1);
@@ -154,7 +154,8 @@ __device__ __forceinline__ void x_warp_segments(const SplitArgs& a, int nseg, lo
     if (halo && sg == 0 && lane < 4) {  // columns 0, 1 <- nx, nx+1; nx+2, nx+3 <- 2, 3
       const int dst = lane < 2 ? lane : a.nx + lane, src = lane < 2 ? a.nx + lane : lane;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) a.forcing[q * a.plane + row + dst] = a.forcing[q * a.plane + row + src];
+      for (int q = 0; q < 4; ++q)
+        MW_AT(a.forcing, q * a.plane + row + dst, 4 * (long long)a.plane) = MW_AT(a.forcing, q * a.plane + row + src, 4 * (long long)a.plane);
     }
     const int kc = k;
     const int i = x0 + lane;
@@ -169,7 +170,7 @@ __device__ __forceinline__ void x_warp_segments(const SplitArgs& a, int nseg, lo
     double iv[4];
     if (upd) {
 #pragma unroll
-      for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
+      for (int q = 0; q < 4; ++q) iv[q] = MW_AT(a.init, q * a.plane + o, 4 * (long long)a.plane);
     }
     __syncwarp();
     if (i <= a.nx) {
@@ -187,7 +188,7 @@ __device__ __forceinline__ void x_warp_segments(const SplitArgs& a, int nseg, lo
     if (upd) {
       dw2 dF[2] = {sub2(sm.sF[w][0][lane], sm.sF[w][0][lane + 1]), sub2(sm.sF[w][1][lane], sm.sF[w][1][lane + 1])};
       if (a.srcw) {
-        const dw ws = add(lo_of(dF[1]), mul(from_f64(a.srcw[(sidx)kc * a.nx + i]), d12));
+        const dw ws = add(lo_of(dF[1]), mul(from_f64(MW_AT(a.srcw, (sidx)kc * a.nx + i, (long long)a.nx * a.nz)), d12));
         dF[1].h.x = ws.h;
         dF[1].l.x = ws.l;
       }
@@ -208,7 +209,7 @@ __device__ __forceinline__ void z_march(const SplitArgs& a, int cb, int kbeg, in
   __syncthreads();  // the previous table is no longer read
   for (int r = threadIdx.x; r <= kend - kbeg; r += kZThreads) {
     const int k = kbeg + r;
-    sm.row[r] = row_consts(a.hyi[k], a.hyti[k], a.hypi[k]);
+    sm.row[r] = row_consts(MW_AT(a.hyi, k, a.nz + 1), MW_AT(a.hyti, k, a.nz + 1), MW_AT(a.hypi, k, a.nz + 1));
   }
   __syncthreads();
   const int c = cb * kZThreads + threadIdx.x;
@@ -239,7 +240,7 @@ __device__ __forceinline__ void z_march(const SplitArgs& a, int cb, int kbeg, in
     const sidx o = (sidx)(k + kHs) * a.pitch + col;
     double iv[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
+    for (int q = 0; q < 4; ++q) iv[q] = MW_AT(a.init, q * a.plane + o, 4 * (long long)a.plane);
     double cur[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) cur[q] = nxt[q];
@@ -264,7 +265,7 @@ __device__ __forceinline__ void z_march(const SplitArgs& a, int cb, int kbeg, in
     flux_z2(w, sm.row[k + 1 - kbeg], hv, k + 1 == a.nz, Fn);
     dw2 dF[2] = {sub2(Fp[0], Fn[0]), sub2(Fp[1], Fn[1])};
     dw dw_w = sub(lo_of(dF[1]), mul(rho_k, gz12));
-    if (a.srcw) dw_w = add(dw_w, mul(from_f64(a.srcw[(sidx)k * a.nx + c]), d12));
+    if (a.srcw) dw_w = add(dw_w, mul(from_f64(MW_AT(a.srcw, (sidx)k * a.nx + c, (long long)a.nx * a.nz)), d12));
     dF[1].h.x = dw_w.h;
     dF[1].l.x = dw_w.l;
     store_update(a, o, iv, dF);
@@ -320,12 +321,12 @@ __global__ void __launch_bounds__(kZThreads, MW_ZSPLIT_MIN_BLOCKS) k_stage_z_spl
 // Ensemble: one persistent launch per stage walks a work list over all
 // members (x: one item per member row; z: one item per member column-tile).
 __device__ SplitArgs member_args(const EnsStage& es, int e) {
-  const mw_ens_member m = es.members[e];
+  const mw_ens_member m = MW_AT(es.members, e, es.n_members);
   SplitArgs a;
   a.nx = m.nx;
   a.nz = m.nz;
   a.pitch = m.nx + 2 * kHs;
-  a.plane = (long long)(m.nz + 2 * kHs) * a.pitch;
+  a.plane = (sidx)(m.nz + 2 * kHs) * a.pitch;
   a.hyc = es.hyc + m.cell_off;
   a.hytc = es.hytc + m.cell_off;
   a.hyi = es.hyi + m.int_off;
@@ -353,10 +354,11 @@ __global__ void __launch_bounds__(kXThreads, MW_XSPLIT_MIN_BLOCKS) k_ens_x_split
   __shared__ SmemXW sm;
   const int nw = gridDim.x * kXWarps;
   for (int it = blockIdx.x * kXWarps + (threadIdx.x >> 5); it < es.n_items; it += nw) {
-    const int2 item = es.items[it];  // (member, row)
+    const int2 item = MW_AT(es.items, it, es.n_items);  // (member, row)
     const SplitArgs a = member_args(es, item.x);
     const int nseg = (a.nx + kWCells - 1) / kWCells;
-    const RowS r = reinterpret_cast<const RowS*>(es.xrows)[es.members[item.x].cell_off + item.y + kHs];
+    const RowS r = MW_AT(reinterpret_cast<const RowS*>(es.xrows), MW_AT(es.members, item.x, es.n_members).cell_off + item.y + kHs,
+                         es.n_xrows);
     x_warp_segments(a, nseg, (long long)item.y * nseg, (long long)(item.y + 1) * nseg,
                     [&](int) { return r; }, a.flags & MW_FLAG_WRITE_HALO, sm);
   }
@@ -365,7 +367,7 @@ __global__ void __launch_bounds__(kXThreads, MW_XSPLIT_MIN_BLOCKS) k_ens_x_split
 __global__ void __launch_bounds__(kZThreads, MW_ZSPLIT_MIN_BLOCKS) k_ens_z_split(EnsStage es) {
   __shared__ SmemZ sm;
   for (int it = blockIdx.x; it < es.n_items; it += gridDim.x) {
-    const int2 item = es.items[it];  // (member, column block + ncb * tile)
+    const int2 item = MW_AT(es.items, it, es.n_items);  // (member, column block + ncb * tile)
     const SplitArgs a = member_args(es, item.x);
     const int ncb = (a.nx + kZThreads - 1) / kZThreads;
     const int cb = item.y % ncb, tile = item.y / ncb;
@@ -423,7 +425,7 @@ int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, con
   a.nx = nx;
   a.nz = nz;
   a.pitch = g.pitch;
-  a.plane = g.plane;
+  a.plane = (sidx)g.plane;
   a.hyc = hyc;
   a.hytc = hytc;
   a.hyi = hyi;
