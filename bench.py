@@ -9,6 +9,11 @@ larger than the 129 MB L2, so no flush is needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
+The headline times K calls of the public step (evolve -> mw_step_f64, which
+keeps the first RK stage's result of each direction as double-FP32 pairs); the
+per-kernel figures of the roofline come from a second pass that issues the same
+six launches stage by stage through mw_dirstage_f64 with an event after each.
+
 Prints one JSON line (rank 0).  Under torchrun each rank advances its own
 replica (the step has no exchange on one GPU); value = cell-steps of all ranks
 per second of the slowest rank.
@@ -230,6 +235,28 @@ def timed_run(torch, native, p, f, steps, warmup, dist=None):
     return ms, per, 6 * steps
 
 
+def step_run(torch, p, f, steps, warmup, dist=None):
+    """Warm up, then time exactly `steps` calls of the public step (evolve ->
+    mw_step_f64 / mw_step_f32, one time step each); returns ms_total."""
+    from pyminiweather_gb300.solve import evolve, reset_direction
+    reset_direction()
+    for _ in range(warmup):
+        evolve(p, f, None, dt=p["dt"], nsteps=1)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        evolve(p, f, None, dt=p["dt"], nsteps=1)
+    e1.record()
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    return e0.elapsed_time(e1)
+
+
 def kernel_names(fp64, mode):
     if not fp64:
         return {0: "k_stage_x<float,F32>", 1: "k_stage_z<float,F32>"}
@@ -423,12 +450,19 @@ def run_gb300(args):
 
     clocks = ClockSampler(device_id_for_smi(torch, dev))
     clocks.start()
-    ms, per, launches = timed_run(torch, _native, p, f, args.steps, args.warmup, dist)
+    ms = step_run(torch, p, f, args.steps, args.warmup, dist)
     clk = clocks.stop()
     ms = replica_max(torch, ms, dist, "cuda")
     m1 = compute_stats(p, f)[0]
+    launches = 6 * args.steps
     value = job_value(world, cells, args.steps, ms)
+    # per-kernel durations: the same six launches a step makes, issued stage by
+    # stage through the C ABI with an event after each (every stage in FP64
+    # storage there; the step keeps its first RK stage's result as pairs)
+    init(f, p)
+    _, per, _ = timed_run(torch, _native, p, f, args.steps, args.warmup, dist)
     rl = roofline(per, cells, 8, peak, peak_kind, kernel_names(True, args.mode), traffic)
+    rl["kernel_timing"] = "stage-by-stage C-ABI pass, FP64 storage in every stage"
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None,
@@ -460,7 +494,9 @@ def run_gb300(args):
         torch.cuda.empty_cache()
         f32 = initialize_fields(p, dtype=torch.float32)
         init(f32, p)
-        ms32, per32, _ = timed_run(torch, _native, p, f32, args.steps, args.warmup, None)
+        ms32 = step_run(torch, p, f32, args.steps, args.warmup, None)
+        init(f32, p)
+        _, per32, _ = timed_run(torch, _native, p, f32, args.steps, args.warmup, None)
         v32 = job_value(world, cells, args.steps, ms32)
         line["fp32"] = {"value": v32, "ms_per_step": ms32 / args.steps, "speedup_vs_fp64": v32 / value,
                         "roofline": roofline(per32, cells, 4, peak, peak_kind, kernel_names(False, "split"), traffic)}
@@ -472,7 +508,9 @@ def run_gb300(args):
         fo = initialize_fields(po, dtype=torch.float64)
         init(fo, po)
         ks = max(1, min(args.steps, 3))
-        mso, pero, _ = timed_run(torch, _native, po, fo, ks, 1, None)
+        mso = step_run(torch, po, fo, ks, 1, None)
+        init(fo, po)
+        _, pero, _ = timed_run(torch, _native, po, fo, ks, 1, None)
         line["fp64_" + other] = {"value": job_value(world, cells, ks, mso), "ms_per_step": mso / ks,
                                  "roofline": roofline(pero, cells, 8, peak, peak_kind, kernel_names(True, other),
                                                       traffic)}

@@ -602,15 +602,21 @@ int check_finite_blocking(int nx, int nz, const T* state, cudaStream_t stream);
 int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
                        const double* hyi, const double* hyti, const double* hypi, const double* srcw,
                        const double* init, double* forcing, double* out, double dt_stage, int direction,
-                       unsigned flags, int r0, int r1, cudaStream_t stream);
+                       unsigned flags, int r0, int r1, int fmt, cudaStream_t stream);
+
+// Storage format of the split form's RK3 stage k (0, 1, 2) inside a whole
+// step: the first stage's result s1 is read only by the second stage of the
+// same direction, so it stays in the scratch array as double-FP32 pairs
+// (format 1 writes them, format 2 reads them); everything else is FP64.
+inline int split_step_fmt(int k) { return k == 0 ? 1 : (k == 1 ? 2 : 0); }
 
 static int stage_f64(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
                      const double* hyi, const double* hyti, const double* hypi, const double* srcw,
                      const double* init, double* forcing, double* out, double dt_stage, int direction, int mode,
-                     unsigned flags, cudaStream_t stream) {
+                     unsigned flags, cudaStream_t stream, int fmt = 0) {
   if (mode == MW_F64_SPLIT)
     return launch_stage_split(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, srcw, init, forcing, out,
-                              dt_stage, direction, flags, 0, nz, stream);
+                              dt_stage, direction, flags, 0, nz, fmt, stream);
   return launch_stage<double, MODE_NATIVE64>(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, srcw, init, forcing,
                                              out, dt_stage, direction, flags, stream);
 }
@@ -621,9 +627,9 @@ static int run_steps(double dt, T* S, T* Tmp, T* A, int nsteps, int* reverse, St
     const int dirs[2] = {*reverse ? MW_DIR_X : MW_DIR_Z, *reverse ? MW_DIR_Z : MW_DIR_X};
     for (int d = 0; d < 2; ++d) {
       int st;
-      if ((st = stage(S, S, A, dt / 3, dirs[d]))) return st;
-      if ((st = stage(S, A, Tmp, dt / 2, dirs[d]))) return st;
-      if ((st = stage(S, Tmp, S, dt / 1, dirs[d]))) return st;
+      if ((st = stage(S, S, A, dt / 3, dirs[d], 0))) return st;
+      if ((st = stage(S, A, Tmp, dt / 2, dirs[d], 1))) return st;
+      if ((st = stage(S, Tmp, S, dt / 1, dirs[d], 2))) return st;
     }
     *reverse = *reverse ? 0 : 1;
   }
@@ -687,9 +693,9 @@ extern "C" int mw_step_f64(int nx, int nz, double dx, double dz, double dt_full,
              f64_mode);
   cudaStream_t s = (cudaStream_t)stream;
   st = run_steps<double>(dt, state, state_tmp, scratch, nsteps, reverse,
-                         [&](const double* init, double* forcing, double* out, double dts, int dir) {
+                         [&](const double* init, double* forcing, double* out, double dts, int dir, int k) {
                            return stage_f64(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, src_w, init, forcing,
-                                            out, dts, dir, f64_mode, flags, s);
+                                            out, dts, dir, f64_mode, flags, s, split_step_fmt(k));
                          });
   if (st == MW_OK && nsteps > 0 && (flags & MW_FLAG_CHECK_FINITE)) st = check_finite_blocking(nx, nz, (const double*)state, s);
   return st;
@@ -706,7 +712,7 @@ extern "C" int mw_step_f32(int nx, int nz, double dx, double dz, double dt_full,
   if (st) return st;
   cudaStream_t s = (cudaStream_t)stream;
   st = run_steps<float>(dt, state, state_tmp, scratch, nsteps, reverse,
-                        [&](const float* init, float* forcing, float* out, double dts, int dir) {
+                        [&](const float* init, float* forcing, float* out, double dts, int dir, int) {
                           return launch_stage<float, MODE_F32>(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi,
                                                                src_w, init, forcing, out, dts, dir, flags, s);
                         });
@@ -783,9 +789,9 @@ extern "C" int mw_step_f64_noalloc(int nx, int nz, double dx, double dz, double 
              f64_mode);
   cudaStream_t s = (cudaStream_t)stream;
   return run_steps<double>(dt, state, state_tmp, scratch, nsteps, reverse,
-                           [&](const double* init, double* forcing, double* out, double dts, int dir) {
+                           [&](const double* init, double* forcing, double* out, double dts, int dir, int k) {
                              return stage_f64(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, src_w, init,
-                                              forcing, out, dts, dir, f64_mode, flags, s);
+                                              forcing, out, dts, dir, f64_mode, flags, s, split_step_fmt(k));
                            });
 }
 

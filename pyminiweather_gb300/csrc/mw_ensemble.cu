@@ -135,11 +135,13 @@ int ens_step(void* plan, const mw_ens_plan_info* info, const double* hyc, const 
       T* frc[3] = {S, A, Tmp};
       T* outs[3] = {A, Tmp, S};
       const int div[3] = {3, 2, 1};
+      const int fmts[3] = {1, 2, 0};  // split form: s1 kept in scratch as pairs (kToPair, kFromPair, kF64)
       for (int s = 0; s < 3; ++s) {
         es.init = ins[s];
         es.forcing = frc[s];
         es.out = outs[s];
         es.stage_div = div[s];
+        es.fmt = fmts[s];
         if ((st = launch(es, grid))) return st;
       }
     }

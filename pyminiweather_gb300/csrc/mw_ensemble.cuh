@@ -17,6 +17,7 @@ struct EnsStageT {
   int z_tile;      // rows per z item
   int direction;   // MW_DIR_X / MW_DIR_Z
   int stage_div;   // the stage uses dt / stage_div (3, 2, 1)
+  int fmt;         // split form: storage format of forcing / out (kF64, kToPair, kFromPair)
   unsigned flags;
   const double* hyc;
   const double* hytc;

@@ -24,7 +24,7 @@ namespace mw {
 int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
                        const double* hyi, const double* hyti, const double* hypi, const double* srcw,
                        const double* init, double* forcing, double* out, double dt_stage, int direction,
-                       unsigned flags, int r0, int r1, cudaStream_t stream);
+                       unsigned flags, int r0, int r1, int fmt, cudaStream_t stream);
 
 namespace {
 
@@ -115,9 +115,12 @@ extern "C" int mw_step_f64_host(int nx, int nz, double dx, double dz, double dt_
   CopyRes* c = nullptr;
   if ((st = resources(&c))) return st;
   double *S = state, *Tmp = state_tmp, *A = scratch;
+  // The first stage of a direction leaves s1 in the scratch array as
+  // double-FP32 pairs (format 1) for the second (format 2), as mw_step_f64 does.
   auto stage = [&](const double* init, double* forcing, double* out, double dts, int dir, int r0, int r1) {
+    const int fmt = out == A ? 1 : (forcing == A ? 2 : 0);
     return launch_stage_split(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, src_w, init, forcing, out, dts,
-                              dir, flags, r0, r1, s);
+                              dir, flags, r0, r1, fmt, s);
   };
   auto x_band = [&](int r0, int r1) {
     int e;

@@ -35,15 +35,16 @@ typedef long long sidx;
 }  // namespace s64
 
 // Arrays whose four planes span fewer than 2^31 elements take the 32-bit-index
-// kernels.  Output rows [r0, r1) (the whole grid: 0, nz).
+// kernels.  Output rows [r0, r1) (the whole grid: 0, nz); fmt 0 FP64 throughout, 1 forcing
+// (== init) FP64 and out as double-FP32 pairs, 2 forcing as pairs.
 int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
                        const double* hyi, const double* hyti, const double* hypi, const double* srcw,
                        const double* init, double* forcing, double* out, double dt_stage, int direction,
-                       unsigned flags, int r0, int r1, cudaStream_t stream) {
+                       unsigned flags, int r0, int r1, int fmt, cudaStream_t stream) {
   const bool small = 4 * make_geom(nx, nz).plane < (1LL << 31) && !(flags & MW_FLAG_INDEX64);
   return (small ? s32::launch_stage_split : s64::launch_stage_split)(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti,
                                                                      hypi, srcw, init, forcing, out, dt_stage,
-                                                                     direction, flags, r0, r1, stream);
+                                                                     direction, flags, r0, r1, fmt, stream);
 }
 
 static_assert(sizeof(RowS) == kEnsRowBytes, "row-constant table entry size");

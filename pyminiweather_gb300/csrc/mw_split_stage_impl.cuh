@@ -35,14 +35,42 @@ struct SplitArgs {
   double c12s;           // 2^896 dt_stage / (12 d): out = init + c12s * 2^-896 (F(i) - F(i+1))
   dwc d12;               // 12 d (source term: dt * src = c12 * 12 d * src)
   dwc gz12;              // 12 dz grav (z gravity term: dt g rho' = c12 * 12 dz g rho')
+  dwc c12;               // dt_stage / (12 d) as a pair (the pair-format update of stage 1)
 };
 
+// Storage format of a stage's forcing and output (the RK3 intermediate s1 is
+// internal to a step and may be kept as double-FP32 pairs, 8 bytes a value):
+//   kF64      forcing, init and out FP64 (the C-ABI stage, stage 3)
+//   kToPair   forcing FP64 and equal to init, out as (h, l) pairs (stage 1)
+//   kFromPair forcing as (h, l) pairs, init and out FP64 (stage 2)
+enum { kF64 = 0, kToPair = 1, kFromPair = 2 };
+
+// A loaded 8-byte value as a pair: FP64 split, or the (h, l) floats themselves.
+template <int FMT>
+__device__ __forceinline__ dw as_pair(double v) {
+  if (FMT == kFromPair) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return {__uint_as_float((unsigned)b), __uint_as_float((unsigned)(b >> 32))};
+  }
+  return from_f64(v);
+}
+__device__ __forceinline__ double pair_bits(dw d) {
+  return __longlong_as_double((long long)(((unsigned long long)__float_as_uint(d.l) << 32) | __float_as_uint(d.h)));
+}
+
+// Forcing value at row k (the wall rule in the halo rows), as loaded: FP64,
+// or the bits of an (h, l) pair for kFromPair.
+template <int FMT>
 __device__ __forceinline__ double zval64(const SplitArgs& a, int q, int k, int col) {
   if (k >= 0 && k < a.nz) return MW_AT(a.forcing, q * (sidx)a.plane + (sidx)(k + kHs) * a.pitch + col, 4 * (long long)a.plane);
   if (q == WMOM) return 0.0;
   const int src = k < 0 ? kHs : a.nz + kHs - 1;
   const double s = MW_AT(a.forcing, q * (sidx)a.plane + (sidx)src * a.pitch + col, 4 * (long long)a.plane);
-  if (q == UMOM) return s / MW_AT(a.hyc, src, a.nz + 2 * kHs) * MW_AT(a.hyc, k + kHs, a.nz + 2 * kHs);
+  if (q == UMOM) {
+    if (FMT == kFromPair)
+      return pair_bits(mul(as_pair<FMT>(s), from_f64(MW_AT(a.hyc, k + kHs, a.nz + 2 * kHs) / MW_AT(a.hyc, src, a.nz + 2 * kHs))));
+    return s / MW_AT(a.hyc, src, a.nz + 2 * kHs) * MW_AT(a.hyc, k + kHs, a.nz + 2 * kHs);
+  }
   return s;
 }
 
@@ -55,7 +83,7 @@ __device__ __forceinline__ void write_z_halo_column(const SplitArgs& a, int col,
     const int r0 = h == 0 ? -2 : a.nz;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      const double v0 = zval64(a, q, r0, col), v1 = zval64(a, q, r0 + 1, col);
+      const double v0 = zval64<kF64>(a, q, r0, col), v1 = zval64<kF64>(a, q, r0 + 1, col);
       MW_AT(a.forcing, q * (sidx)a.plane + (sidx)(r0 + kHs) * a.pitch + col, 4 * (long long)a.plane) = v0;
       MW_AT(a.forcing, q * (sidx)a.plane + (sidx)(r0 + 1 + kHs) * a.pitch + col, 4 * (long long)a.plane) = v1;
     }
@@ -78,7 +106,24 @@ struct SmemZ {
 // then per value one FP64 add merging the pair and one FP64 FMA).
 // One test per cell for non-finite increments: h - h is 0 for finite h and
 // NaN otherwise; only then are the four values merged with the per-value check.
-__device__ __forceinline__ void store_update(const SplitArgs& a, sidx o, const double iv[4], dw2 dF[2]) {
+// kToPair: out = init + c12 (F(i) - F(i+1)) in pair arithmetic from the
+// init pairs ip (the forcing's own pairs), stored as (h, l) floats.
+template <int FMT>
+__device__ __forceinline__ void store_update(const SplitArgs& a, sidx o, const double iv[4], const dw2 ip[2],
+                                             dw2 dF[2]) {
+  if (FMT == kToPair) {
+    const dw c = ld(a.c12);
+    const dw2 cv = splat(c);
+    const float2 cn = f2splat(-c.h);
+    float2* out = reinterpret_cast<float2*>(a.out);
+#pragma unroll
+    for (int pr = 0; pr < 2; ++pr) {
+      const dw2 r = add2(ip[pr], mul2n(dF[pr], cv, cn));
+      MW_AT(out, (2 * pr) * a.plane + o, 4 * (long long)a.plane) = make_float2(r.h.x, r.l.x);
+      MW_AT(out, (2 * pr + 1) * a.plane + o, 4 * (long long)a.plane) = make_float2(r.h.y, r.l.y);
+    }
+    return;
+  }
   const dw d[4] = {lo_of(dF[0]), hi_of(dF[0]), lo_of(dF[1]), hi_of(dF[1])};
   const float2 z = f2add(f2sub(dF[0].h, dF[0].h), f2sub(dF[1].h, dF[1].h));
   double v[4];
@@ -112,7 +157,7 @@ __device__ __forceinline__ RowS x_row_consts(const SplitArgs& a, int k) {
 }
 
 // row_at(k): the row constants of row k.
-template <typename RowAt>
+template <int FMT, typename RowAt>
 __device__ __forceinline__ void x_warp_segments(const SplitArgs& a, int nseg, long long g0, long long g1,
                                                 RowAt row_at, bool halo, SmemXW& sm) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -140,18 +185,18 @@ __device__ __forceinline__ void x_warp_segments(const SplitArgs& a, int nseg, lo
     const int x0 = sg * kWCells;
     const sidx row = (sidx)(k + kHs) * a.pitch;
     {
-      dw2 p[2];
-      pack4(v0, p);
-      sm.sS[w][0][lane] = p[0];
-      sm.sS[w][1][lane] = p[1];
+      const dw2 p0 = pack(as_pair<FMT>(v0[DENS]), as_pair<FMT>(v0[UMOM]));
+      const dw2 p1 = pack(as_pair<FMT>(v0[WMOM]), as_pair<FMT>(v0[RHOT]));
+      sm.sS[w][0][lane] = p0;
+      sm.sS[w][1][lane] = p1;
       if (lane < 12) {
-        const dw d = from_f64(v1);
+        const dw d = as_pair<FMT>(v1);
         float* e = reinterpret_cast<float*>(&sm.sS[w][xq >> 1][32 + xj]);  // h.x, h.y, l.x, l.y
         e[xq & 1] = d.h;
         e[2 + (xq & 1)] = d.l;
       }
     }
-    if (halo && sg == 0 && lane < 4) {  // columns 0, 1 <- nx, nx+1; nx+2, nx+3 <- 2, 3
+    if (FMT != kFromPair && halo && sg == 0 && lane < 4) {  // columns 0, 1 <- nx, nx+1; nx+2, nx+3 <- 2, 3
       const int dst = lane < 2 ? lane : a.nx + lane, src = lane < 2 ? a.nx + lane : lane;
 #pragma unroll
       for (int q = 0; q < 4; ++q)
@@ -168,7 +213,7 @@ __device__ __forceinline__ void x_warp_segments(const SplitArgs& a, int nseg, lo
     const bool more = g + 1 < g1;
     if (more) load(k, sg * kWCells, v0, v1);
     double iv[4];
-    if (upd) {
+    if (FMT != kToPair && upd) {
 #pragma unroll
       for (int q = 0; q < 4; ++q) iv[q] = MW_AT(a.init, q * a.plane + o, 4 * (long long)a.plane);
     }
@@ -192,7 +237,12 @@ __device__ __forceinline__ void x_warp_segments(const SplitArgs& a, int nseg, lo
         dF[1].h.x = ws.h;
         dF[1].l.x = ws.l;
       }
-      store_update(a, o, iv, dF);
+      dw2 ip[2];
+      if (FMT == kToPair) {  // init is the forcing: its staged pairs at cell x0+lane
+        ip[0] = sm.sS[w][0][lane + 2];
+        ip[1] = sm.sS[w][1][lane + 2];
+      }
+      store_update<FMT>(a, o, iv, ip, dF);
     }
     __syncwarp();
   }
@@ -204,8 +254,10 @@ __device__ __forceinline__ void x_warp_segments(const SplitArgs& a, int nseg, lo
 // the interface row constants are tabled in shared memory.  hbot / htop:
 // write the bottom / top wall halo rows of these columns of the forcing array
 // (cb == 0 also does the four x-halo columns).
+template <int FMT>
 __device__ __forceinline__ void z_march(const SplitArgs& a, int cb, int kbeg, int kend, bool hbot, bool htop,
                                         SmemZ& sm) {
+  if (FMT == kFromPair) hbot = htop = false;  // the pair-format forcing (internal scratch) keeps no halo
   __syncthreads();  // the previous table is no longer read
   for (int r = threadIdx.x; r <= kend - kbeg; r += kZThreads) {
     const int k = kbeg + r;
@@ -225,42 +277,39 @@ __device__ __forceinline__ void z_march(const SplitArgs& a, int cb, int kbeg, in
   for (int j = 0; j < 4; ++j) {
     double v[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) v[q] = zval64(a, q, kbeg - 2 + j, col);
-    dw2 p[2];
-    pack4(v, p);
-    w[0][j] = p[0];
-    w[1][j] = p[1];
+    for (int q = 0; q < 4; ++q) v[q] = zval64<FMT>(a, q, kbeg - 2 + j, col);
+    w[0][j] = pack(as_pair<FMT>(v[DENS]), as_pair<FMT>(v[UMOM]));
+    w[1][j] = pack(as_pair<FMT>(v[WMOM]), as_pair<FMT>(v[RHOT]));
   }
   double nxt[4];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) nxt[q] = zval64(a, q, kbeg + 2, col);
+  for (int q = 0; q < 4; ++q) nxt[q] = zval64<FMT>(a, q, kbeg + 2, col);
   dw2 Fp[2];
   flux_z2(w, sm.row[0], hv, kbeg == 0, Fp);
   for (int k = kbeg; k < kend; ++k) {
     const sidx o = (sidx)(k + kHs) * a.pitch + col;
     double iv[4];
+    if (FMT != kToPair) {
 #pragma unroll
-    for (int q = 0; q < 4; ++q) iv[q] = MW_AT(a.init, q * a.plane + o, 4 * (long long)a.plane);
+      for (int q = 0; q < 4; ++q) iv[q] = MW_AT(a.init, q * a.plane + o, 4 * (long long)a.plane);
+    }
     double cur[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) cur[q] = nxt[q];
     if (k + 1 < kend) {
 #pragma unroll
-      for (int q = 0; q < 4; ++q) nxt[q] = zval64(a, q, k + 3, col);
+      for (int q = 0; q < 4; ++q) nxt[q] = zval64<FMT>(a, q, k + 3, col);
     }
     const dw rho_k = lo_of(w[0][2]);
+    const dw2 ip[2] = {w[0][2], w[1][2]};  // kToPair: init is the forcing at row k
 #pragma unroll
     for (int pr = 0; pr < 2; ++pr) {
       w[pr][0] = w[pr][1];
       w[pr][1] = w[pr][2];
       w[pr][2] = w[pr][3];
     }
-    {
-      dw2 p[2];
-      pack4(cur, p);
-      w[0][3] = p[0];
-      w[1][3] = p[1];
-    }
+    w[0][3] = pack(as_pair<FMT>(cur[DENS]), as_pair<FMT>(cur[UMOM]));
+    w[1][3] = pack(as_pair<FMT>(cur[WMOM]), as_pair<FMT>(cur[RHOT]));
     dw2 Fn[2];
     flux_z2(w, sm.row[k + 1 - kbeg], hv, k + 1 == a.nz, Fn);
     dw2 dF[2] = {sub2(Fp[0], Fn[0]), sub2(Fp[1], Fn[1])};
@@ -268,7 +317,7 @@ __device__ __forceinline__ void z_march(const SplitArgs& a, int cb, int kbeg, in
     if (a.srcw) dw_w = add(dw_w, mul(from_f64(MW_AT(a.srcw, (sidx)k * a.nx + c, (long long)a.nx * a.nz)), d12));
     dF[1].h.x = dw_w.h;
     dF[1].l.x = dw_w.l;
-    store_update(a, o, iv, dF);
+    store_update<FMT>(a, o, iv, ip, dF);
     Fp[0] = Fn[0];
     Fp[1] = Fn[1];
   }
@@ -283,6 +332,7 @@ __device__ __forceinline__ void z_march(const SplitArgs& a, int cb, int kbeg, in
 #define MW_XSPLIT_MIN_BLOCKS 3
 #endif
 // Segments [gbase, gbase + total) (rows gbase / nseg onwards).
+template <int FMT>
 __global__ void __launch_bounds__(kXThreads, MW_XSPLIT_MIN_BLOCKS) k_stage_x_split(SplitArgs a, int nseg, long long total,
                                                                                    long long gbase) {
   __shared__ SmemXW sm;
@@ -293,8 +343,8 @@ __global__ void __launch_bounds__(kXThreads, MW_XSPLIT_MIN_BLOCKS) k_stage_x_spl
   __syncthreads();
   const int w = threadIdx.x >> 5;
   const long long n = g1 - g0;
-  x_warp_segments(a, nseg, g0 + n * w / kXWarps, g0 + n * (w + 1) / kXWarps,
-                  [&](int k) { return sm.row[k - row0]; }, a.flags & MW_FLAG_WRITE_HALO, sm);
+  x_warp_segments<FMT>(a, nseg, g0 + n * w / kXWarps, g0 + n * (w + 1) / kXWarps,
+                       [&](int k) { return sm.row[k - row0]; }, a.flags & MW_FLAG_WRITE_HALO, sm);
 }
 
 // z, single grid: the CTA owns the contiguous range [u0, u1) of the
@@ -302,6 +352,7 @@ __global__ void __launch_bounds__(kXThreads, MW_XSPLIT_MIN_BLOCKS) k_stage_x_spl
 // units, so it marches one or two column-block pieces.  The launch sizes the
 // grid to a whole number of resident waves of equal ranges.
 // Rows [r0, r1) of every column block.
+template <int FMT>
 __global__ void __launch_bounds__(kZThreads, MW_ZSPLIT_MIN_BLOCKS) k_stage_z_split(SplitArgs a, int ncb, int r0, int r1) {
   __shared__ SmemZ sm;
   const int rows = r1 - r0;
@@ -312,7 +363,7 @@ __global__ void __launch_bounds__(kZThreads, MW_ZSPLIT_MIN_BLOCKS) k_stage_z_spl
   while (u < u1) {
     const int cb = (int)(u / rows), k0 = r0 + (int)(u - (long long)cb * rows);
     const int kend = (int)std::min<long long>(r1, k0 + (u1 - u));
-    z_march(a, cb, k0, kend, halo && k0 == 0, halo && kend == a.nz, sm);
+    z_march<FMT>(a, cb, k0, kend, halo && k0 == 0, halo && kend == a.nz, sm);
     u += kend - k0;
   }
 }
@@ -344,12 +395,14 @@ __device__ SplitArgs member_args(const EnsStage& es, int e) {
   a.c12s = dts / (12.0 * d) * kTwoPow896;  // exact: a power-of-two scale
   a.d12 = split_rn(12.0 * d);
   a.gz12 = split_rn(12.0 * m.dz * kGrav);
+  a.c12 = split_rn(dts / (12.0 * d));
   return a;
 }
 
 // x items are rows (member, row), one per warp: the warp walks the row's
 // 31-cell segments as the single-grid kernel does, with the row constants read
 // from the plan's table (written once per step call, no FP64 pow per row).
+template <int FMT>
 __global__ void __launch_bounds__(kXThreads, MW_XSPLIT_MIN_BLOCKS) k_ens_x_split(EnsStage es) {
   __shared__ SmemXW sm;
   const int nw = gridDim.x * kXWarps;
@@ -359,11 +412,12 @@ __global__ void __launch_bounds__(kXThreads, MW_XSPLIT_MIN_BLOCKS) k_ens_x_split
     const int nseg = (a.nx + kWCells - 1) / kWCells;
     const RowS r = MW_AT(reinterpret_cast<const RowS*>(es.xrows), MW_AT(es.members, item.x, es.n_members).cell_off + item.y + kHs,
                          es.n_xrows);
-    x_warp_segments(a, nseg, (long long)item.y * nseg, (long long)(item.y + 1) * nseg,
+    x_warp_segments<FMT>(a, nseg, (long long)item.y * nseg, (long long)(item.y + 1) * nseg,
                     [&](int) { return r; }, a.flags & MW_FLAG_WRITE_HALO, sm);
   }
 }
 
+template <int FMT>
 __global__ void __launch_bounds__(kZThreads, MW_ZSPLIT_MIN_BLOCKS) k_ens_z_split(EnsStage es) {
   __shared__ SmemZ sm;
   for (int it = blockIdx.x; it < es.n_items; it += gridDim.x) {
@@ -373,7 +427,7 @@ __global__ void __launch_bounds__(kZThreads, MW_ZSPLIT_MIN_BLOCKS) k_ens_z_split
     const int cb = item.y % ncb, tile = item.y / ncb;
     const int k0 = tile * es.z_tile, kend = min(k0 + es.z_tile, a.nz);
     const bool halo = a.flags & MW_FLAG_WRITE_HALO;
-    z_march(a, cb, k0, kend, halo && k0 == 0, halo && kend == a.nz, sm);
+    z_march<FMT>(a, cb, k0, kend, halo && k0 == 0, halo && kend == a.nz, sm);
   }
 }
 
@@ -381,23 +435,36 @@ __global__ void __launch_bounds__(kZThreads, MW_ZSPLIT_MIN_BLOCKS) k_ens_z_split
 
 int launch_ens_split(const EnsStage& es, int grid) {
   if (es.n_items == 0) return MW_OK;
-  if (es.direction == MW_DIR_X)
-    k_ens_x_split<<<grid, kXThreads, 0, es.stream>>>(es);
-  else
-    k_ens_z_split<<<grid, kZThreads, 0, es.stream>>>(es);
+  MW_REQUIRE(es.fmt == kF64 || es.fmt == kToPair || es.fmt == kFromPair, MW_ERR_INVALID_ARG, "bad stage format");
+  if (es.direction == MW_DIR_X) {
+    if (es.fmt == kToPair)
+      k_ens_x_split<kToPair><<<grid, kXThreads, 0, es.stream>>>(es);
+    else if (es.fmt == kFromPair)
+      k_ens_x_split<kFromPair><<<grid, kXThreads, 0, es.stream>>>(es);
+    else
+      k_ens_x_split<kF64><<<grid, kXThreads, 0, es.stream>>>(es);
+  } else {
+    if (es.fmt == kToPair)
+      k_ens_z_split<kToPair><<<grid, kZThreads, 0, es.stream>>>(es);
+    else if (es.fmt == kFromPair)
+      k_ens_z_split<kFromPair><<<grid, kZThreads, 0, es.stream>>>(es);
+    else
+      k_ens_z_split<kF64><<<grid, kZThreads, 0, es.stream>>>(es);
+  }
   return check_launch("ensemble split stage launch");
 }
 
 int ens_split_occupancy(int direction, int* blocks_per_sm) {
   cudaError_t e = direction == MW_DIR_X
-                      ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_ens_x_split, kXThreads, 0)
-                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_ens_z_split, kZThreads, 0);
+                      ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_ens_x_split<kF64>, kXThreads, 0)
+                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_ens_z_split<kF64>, kZThreads, 0);
   if (e != cudaSuccess) return fail(MW_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
   return MW_OK;
 }
 
-// CTAs of k_stage_x_split (which 0) / k_stage_z_split (which 1) resident on
-// the current device, cached per device.
+// CTAs of k_stage_x_split (which 0) / k_stage_z_split (which 1) of format fmt
+// resident on the current device, cached per device.
+template <int FMT>
 int resident_ctas(int which, int* out) {
   static std::atomic<int> cache[2][64];
   int dev = 0;
@@ -405,8 +472,8 @@ int resident_ctas(int which, int* out) {
   const bool cached = dev >= 0 && dev < 64;
   if (cached && (*out = cache[which][dev].load(std::memory_order_relaxed)) > 0) return MW_OK;
   int per_sm = 0, sms = 0;
-  cudaError_t e = which == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage_x_split, kXThreads, 0)
-                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage_z_split, kZThreads, 0);
+  cudaError_t e = which == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage_x_split<FMT>, kXThreads, 0)
+                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage_z_split<FMT>, kZThreads, 0);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return fail(MW_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
   *out = std::max(1, per_sm) * sms;
@@ -414,10 +481,11 @@ int resident_ctas(int which, int* out) {
   return MW_OK;
 }
 
-int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
-                       const double* hyi, const double* hyti, const double* hypi, const double* srcw,
-                       const double* init, double* forcing, double* out, double dt_stage, int direction,
-                       unsigned flags, int r0, int r1, cudaStream_t stream) {
+template <int FMT>
+int launch_stage_split_fmt(int nx, int nz, double dx, double dz, double dt_full, const double* hyc,
+                           const double* hytc, const double* hyi, const double* hyti, const double* hypi,
+                           const double* srcw, const double* init, double* forcing, double* out, double dt_stage,
+                           int direction, unsigned flags, int r0, int r1, cudaStream_t stream) {
   const Geom g = make_geom(nx, nz);
   MW_REQUIRE(0 <= r0 && r0 < r1 && r1 <= nz, MW_ERR_INVALID_ARG, "row range [%d, %d) outside [0, %d)", r0, r1, nz);
   const int rows = r1 - r0;
@@ -444,10 +512,11 @@ int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, con
              "dt_stage / (12 d) = %g is above the split form's range (use the native FP64 mode)", dt_stage / (12.0 * d));
   a.d12 = split_host(12.0 * d);
   a.gz12 = split_host(12.0 * dz * kGrav);
+  a.c12 = split_host(dt_stage / (12.0 * d));
   if (direction == MW_DIR_X) {
     const int nseg = (nx + kWCells - 1) / kWCells;
     const long long total = (long long)nseg * rows;
-    int resident = 0, st = resident_ctas(0, &resident);
+    int resident = 0, st = resident_ctas<FMT>(0, &resident);
     if (st) return st;
     // One resident wave (at least one segment per warp) for small grids;
     // MW_XSPLIT_SEGS_PER_WARP segments per warp for large ones, so that the
@@ -457,17 +526,30 @@ int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, con
     if (MW_XSPLIT_SEGS_PER_WARP > 0) grid = std::max<long long>(grid, total / (kXWarps * MW_XSPLIT_SEGS_PER_WARP));
     grid = std::max<long long>(grid, (rows + kXRowsMax - 3) / (kXRowsMax - 2));
     MW_REQUIRE(grid <= 0x7fffffffLL, MW_ERR_SHAPE, "grid too large for the x direction-stage launch");
-    k_stage_x_split<<<(unsigned)grid, kXThreads, 0, stream>>>(a, nseg, total, (long long)r0 * nseg);
+    k_stage_x_split<FMT><<<(unsigned)grid, kXThreads, 0, stream>>>(a, nseg, total, (long long)r0 * nseg);
   } else {
     const int ncb = (nx + kZThreads - 1) / kZThreads;
     const long long units = (long long)ncb * rows;
-    int resident = 0, st = resident_ctas(1, &resident);
+    int resident = 0, st = resident_ctas<FMT>(1, &resident);
     if (st) return st;
     long long grid = resident * ((units + (long long)kZTileMax * resident - 1) / ((long long)kZTileMax * resident));
     grid = std::max<long long>(1, std::min<long long>(grid, units / kZMinRows));
     MW_REQUIRE(grid <= 0x7fffffffLL, MW_ERR_SHAPE, "grid too large for the z direction-stage launch");
-    k_stage_z_split<<<(unsigned)grid, kZThreads, 0, stream>>>(a, ncb, r0, r1);
+    k_stage_z_split<FMT><<<(unsigned)grid, kZThreads, 0, stream>>>(a, ncb, r0, r1);
   }
   return check_launch(direction == MW_DIR_X ? "x split direction-stage launch" : "z split direction-stage launch");
+}
+
+// fmt: kF64, kToPair (forcing == init, out as pairs) or kFromPair (forcing as pairs).
+int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
+                       const double* hyi, const double* hyti, const double* hypi, const double* srcw,
+                       const double* init, double* forcing, double* out, double dt_stage, int direction,
+                       unsigned flags, int r0, int r1, int fmt, cudaStream_t stream) {
+  MW_REQUIRE(fmt == kF64 || fmt == kToPair || fmt == kFromPair, MW_ERR_INVALID_ARG, "bad stage format %d", fmt);
+  MW_REQUIRE(fmt != kToPair || init == forcing, MW_ERR_INVALID_ARG, "the pair-output stage needs init == forcing");
+  auto fn = fmt == kToPair ? launch_stage_split_fmt<kToPair>
+                           : (fmt == kFromPair ? launch_stage_split_fmt<kFromPair> : launch_stage_split_fmt<kF64>);
+  return fn(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, srcw, init, forcing, out, dt_stage, direction, flags,
+            r0, r1, stream);
 }
 
