@@ -119,7 +119,7 @@ int mw_step_f64(int nx, int nz, double dx, double dz, double dt_full, double dt,
  * is copied into state, the step runs as mw_step_f64 with nsteps = 1, and the
  * resulting state is copied into h_out (which may equal h_in).  Enqueued on
  * `stream`; h_out is complete once the stream is.  In the split form the
- * copies overlap the computation by nbands row bands (<= 16, at least 16 rows
+ * copies overlap the computation by nbands row bands (<= 64, at least 16 rows
  * each); the results are those of copy-in, mw_step_f64, copy-out bit for bit.
  * h_in / h_out should be page-locked for the copies to run asynchronously.
  * Calls on one device share internal copy streams and are serialised. */

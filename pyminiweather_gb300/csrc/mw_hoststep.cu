@@ -3,17 +3,15 @@
 // bands (the end-to-end use of the step by a caller whose arrays live on the
 // host).
 //
-// The x direction only couples cells of the same row, so its three stages can
-// run on a band of rows as soon as that band has arrived, and the band can
-// leave as soon as its last x stage is done.  A z stage needs two rows of the
-// neighbouring bands, so it runs over a band once those have arrived (first
-// stage) or over the whole grid.  For the order x then z: bands stream in
-// under the x stages, z stages 1-2 run over the grid, z stage 3 runs band by
-// band and each band streams out behind it.  For z then x: z stage 1 runs
-// band by band behind the copies in, z stages 2-3 over the grid, and the x
-// stages band by band ahead of the copies out.  All kernels run in order on
-// the caller's stream, so every read sees the same data as in mw_step_f64;
-// the copies run on two side streams ordered against it by events.
+// The step runs band by band as a wavefront three bands deep behind the
+// copies in, and each band streams out as soon as its last stage is done, so
+// the copies in, the computation and the copies out all overlap.  The x
+// direction only couples cells of the same row; a z stage over a band reads
+// two rows of each neighbouring band, so it follows the previous stage of the
+// band above it.  All kernels run in order on the caller's stream, in an order
+// in which every read sees the same data as in mw_step_f64 (the results are
+// identical bit for bit); the copies run on two side streams ordered against
+// it by events.
 #include <algorithm>
 #include <mutex>
 
@@ -28,7 +26,7 @@ int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, con
 
 namespace {
 
-constexpr int kMaxBands = 16;
+constexpr int kMaxBands = 64;
 
 struct CopyRes {
   bool ready = false;
@@ -122,11 +120,23 @@ extern "C" int mw_step_f64_host(int nx, int nz, double dx, double dz, double dt_
     return launch_stage_split(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, src_w, init, forcing, out, dts,
                               dir, flags, r0, r1, fmt, s);
   };
-  auto x_band = [&](int r0, int r1) {
-    int e;
+  auto rows_of = [&](int b, int* r0, int* r1) {
+    int a0, a1;
+    band_rows(nz, nb, b, r0, r1, &a0, &a1);
+  };
+  auto x_band = [&](int b) {
+    int r0, r1, e;
+    rows_of(b, &r0, &r1);
     if ((e = stage(S, S, A, dt / 3, MW_DIR_X, r0, r1))) return e;
     if ((e = stage(S, A, Tmp, dt / 2, MW_DIR_X, r0, r1))) return e;
     return stage(S, Tmp, S, dt, MW_DIR_X, r0, r1);
+  };
+  auto z_band = [&](int k, int b) {  // z stage k (0, 1, 2) over the rows of band b
+    int r0, r1;
+    rows_of(b, &r0, &r1);
+    if (k == 0) return stage(S, S, A, dt / 3, MW_DIR_Z, r0, r1);
+    if (k == 1) return stage(S, A, Tmp, dt / 2, MW_DIR_Z, r0, r1);
+    return stage(S, Tmp, S, dt, MW_DIR_Z, r0, r1);
   };
   cudaError_t e = cudaEventRecord(c->start, s);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(c->h2d, c->start, 0);
@@ -137,6 +147,10 @@ extern "C" int mw_step_f64_host(int nx, int nz, double dx, double dz, double dt_
     if (e == cudaSuccess) e = cudaEventRecord(c->in[b], c->h2d);
   }
   if (e != cudaSuccess) return fail(MW_ERR_CUDA, "copy in: %s", cudaGetErrorString(e));
+  auto wait_in = [&](int b) {
+    cudaError_t ee = cudaStreamWaitEvent(s, c->in[b], 0);
+    return ee == cudaSuccess ? MW_OK : fail(MW_ERR_CUDA, "wait: %s", cudaGetErrorString(ee));
+  };
   auto band_out = [&](int b) {
     int r0, r1, a0, a1;
     band_rows(nz, nb, b, &r0, &r1, &a0, &a1);
@@ -145,33 +159,31 @@ extern "C" int mw_step_f64_host(int nx, int nz, double dx, double dz, double dt_
     if (ee == cudaSuccess) ee = copy_band(h_out, S, g, a0, a1, cudaMemcpyDeviceToHost, c->d2h);
     return ee == cudaSuccess ? MW_OK : fail(MW_ERR_CUDA, "copy out: %s", cudaGetErrorString(ee));
   };
-  if (*reverse) {  // x then z
-    for (int b = 0; b < nb; ++b) {
-      int r0, r1, a0, a1;
-      band_rows(nz, nb, b, &r0, &r1, &a0, &a1);
-      if ((e = cudaStreamWaitEvent(s, c->in[b], 0)) != cudaSuccess) return fail(MW_ERR_CUDA, "wait: %s", cudaGetErrorString(e));
-      if ((st = x_band(r0, r1))) return st;
+  // A wavefront over the bands, three bands deep.  A z stage over band b reads
+  // its forcing two rows into bands b - 1 and b + 1, so it follows the previous
+  // z stage (or the copy in, or the x stages) of band b + 1; the x stages of a
+  // band need only that band.  The order in which the kernels are issued also
+  // keeps every array row from being overwritten before its last reader:
+  //   x then z, iteration i: x(i), z1(i-1), z2(i-2), z3(i-3), out(i-3)
+  //   z then x, iteration i: z1(i), z2(i-1), z3(i-2), x(i-3), out(i-3)
+  // (z3(b+1) reads state_tmp rows of band b, which x(b) rewrites; z1(b+1) and
+  // z2(b+1) read the state and scratch rows of band b, which x(b) rewrites too.)
+  for (int i = 0; i < nb + 3; ++i) {
+    if (*reverse) {  // x then z
+      if (i < nb && ((st = wait_in(i)) || (st = x_band(i)))) return st;
+      for (int k = 0; k < 3; ++k) {
+        const int b = i - 1 - k;
+        if (b >= 0 && b < nb && (st = z_band(k, b))) return st;
+      }
+    } else {  // z then x
+      for (int k = 0; k < 3; ++k) {
+        const int b = i - k;
+        if (k == 0 && b < nb && (st = wait_in(std::min(b + 1, nb - 1)))) return st;
+        if (b >= 0 && b < nb && (st = z_band(k, b))) return st;
+      }
+      if (i - 3 >= 0 && i - 3 < nb && (st = x_band(i - 3))) return st;
     }
-    if ((st = stage(S, S, A, dt / 3, MW_DIR_Z, 0, nz)) || (st = stage(S, A, Tmp, dt / 2, MW_DIR_Z, 0, nz))) return st;
-    for (int b = 0; b < nb; ++b) {
-      int r0, r1, a0, a1;
-      band_rows(nz, nb, b, &r0, &r1, &a0, &a1);
-      if ((st = stage(S, Tmp, S, dt, MW_DIR_Z, r0, r1)) || (st = band_out(b))) return st;
-    }
-  } else {  // z then x
-    for (int b = 0; b < nb; ++b) {
-      int r0, r1, a0, a1;
-      band_rows(nz, nb, b, &r0, &r1, &a0, &a1);
-      if ((e = cudaStreamWaitEvent(s, c->in[std::min(b + 1, nb - 1)], 0)) != cudaSuccess)
-        return fail(MW_ERR_CUDA, "wait: %s", cudaGetErrorString(e));
-      if ((st = stage(S, S, A, dt / 3, MW_DIR_Z, r0, r1))) return st;
-    }
-    if ((st = stage(S, A, Tmp, dt / 2, MW_DIR_Z, 0, nz)) || (st = stage(S, Tmp, S, dt, MW_DIR_Z, 0, nz))) return st;
-    for (int b = 0; b < nb; ++b) {
-      int r0, r1, a0, a1;
-      band_rows(nz, nb, b, &r0, &r1, &a0, &a1);
-      if ((st = x_band(r0, r1)) || (st = band_out(b))) return st;
-    }
+    if (i - 3 >= 0 && i - 3 < nb && (st = band_out(i - 3))) return st;
   }
   e = cudaEventRecord(c->done, c->d2h);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c->done, 0);
