@@ -119,8 +119,8 @@ int mw_step_f64(int nx, int nz, double dx, double dz, double dt_full, double dt,
  * is copied into state, the step runs as mw_step_f64 with nsteps = 1, and the
  * resulting state is copied into h_out (which may equal h_in).  Enqueued on
  * `stream`; h_out is complete once the stream is.  In the split form the
- * copies overlap the computation by nbands row bands (<= 64, at least 16 rows
- * each); the results are those of copy-in, mw_step_f64, copy-out bit for bit.
+ * copies overlap the computation by nbands row bands (at most 64 and at most
+ * nz / 16); the results are those of copy-in, mw_step_f64, copy-out bit for bit.
  * h_in / h_out should be page-locked for the copies to run asynchronously.
  * Calls on one device share internal copy streams and are serialised. */
 int mw_step_f64_host(int nx, int nz, double dx, double dz, double dt_full, double dt, const double* hy_dens_cell,

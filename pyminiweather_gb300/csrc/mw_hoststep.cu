@@ -56,12 +56,23 @@ int resources(CopyRes** r) {
   return MW_OK;
 }
 
+// First interior row of band b.  With ten or more bands the first three and
+// the last three are half as tall as the others, so that the copies out start
+// sooner and the last copy out ends sooner after the last copy in.
+long long band_weight_before(int nb, int b) {
+  if (nb < 10) return b;
+  const int lo = std::min(b, 3), hi = std::max(0, b - (nb - 3));
+  return 2LL * b - lo - hi;
+}
+int band_start(int nz, int nb, int b) {
+  return (int)((long long)nz * band_weight_before(nb, b) / band_weight_before(nb, nb));
+}
+
 // The array rows a band moves between host and device: its interior rows, plus
 // the wall halo rows for the first and last band.
 void band_rows(int nz, int nb, int b, int* r0, int* r1, int* a0, int* a1) {
-  const int per = (nz + nb - 1) / nb;
-  *r0 = std::min(nz, b * per);
-  *r1 = std::min(nz, *r0 + per);
+  *r0 = band_start(nz, nb, b);
+  *r1 = band_start(nz, nb, b + 1);
   *a0 = b == 0 ? 0 : *r0 + kHs;
   *a1 = b == nb - 1 ? nz + 2 * kHs : *r1 + kHs;
 }

@@ -111,7 +111,7 @@ def evolve(params: Dict, fields, mesh=None, dt: float = 1e-4, nsteps: int = 1) -
 
 
 def evolve_host(params: Dict, fields, h_in: torch.Tensor, h_out: torch.Tensor, dt: float = 1e-4,
-                nbands: int = 16) -> None:
+                nbands: int = 32) -> None:
     """One time step of a state held in host memory: h_in (a CPU tensor of the
     state's shape, ideally pinned) is copied into fields.state, the step runs as
     evolve() would run it, and the new state is copied into h_out (may be
