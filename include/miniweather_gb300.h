@@ -105,7 +105,9 @@ int mw_dirstage_f32(int nx, int nz, double dx, double dz, double dt_full, const 
  * run with dt/3, dt/2, dt:
  *   scratch = S + dt/3 L(S);  state_tmp = S + dt/2 L(scratch);  S = S + dt L(state_tmp)
  * so state_tmp ends holding what the reference's state_tmp holds.  scratch is
- * a third state-sized array (the fused kernel cannot update in place).  dt is
+ * a third state-sized array (the fused kernel cannot update in place); its
+ * contents after the call are unspecified (in the split form each 8-byte slot
+ * holds the first stage's result as a pair of floats, not a double).  dt is
  * evolve's time step; dt_full is params["dt"], the hyperviscosity time scale
  * (the reference uses both, step.py:85 and interpolate.py:99-101).
  * ------------------------------------------------------------------------- */
