@@ -57,7 +57,7 @@ enum mw_f64_mode {
 #define MW_FLAG_INDEX64 2u    /* split form: use the 64-bit-index kernels even
                                  when 32-bit indices suffice (for testing; arrays
                                  of 2^31 or more values always use them) */
-#define MW_FLAG_CHECK_FINITE 4u /* mw_step_f64 / _f32: after the steps, count the
+#define MW_FLAG_CHECK_FINITE 4u /* mw_step_f64 / _f32 / _f64_host: after the steps, count the
                                  non-finite interior values of the state and
                                  return MW_ERR_NONFINITE if there are any
                                  (synchronises the stream to read the count) */
@@ -178,7 +178,8 @@ typedef struct mw_ens_plan_info {
   int n_members, n_x_items, n_z_items, z_tile;
   size_t members_off, x_items_off, z_items_off, bytes; /* byte offsets / size of the device plan */
   size_t xrows_off;    /* split form: per-row background constants, written by each step call */
-  long long n_xrows;   /* entries of that table: the length of the cell-centre backgrounds used */
+  long long n_xrows;   /* entries of that table: the length of the cell-centre backgrounds used;
+                          the members' stage constants follow it, up to `bytes` */
 } mw_ens_plan_info;
 
 /* Size and layout of the work plan for these members (host array) with z

@@ -5,7 +5,9 @@
 // The plan lives in caller-provided device memory:
 //   [members: n x mw_ens_member][x items: int2 (member, row)]
 //   [z items: int2 (member, column block + ncb * z tile)]
-// x work items are member rows (a CTA walks all chunks of the row); z items
+//   [row constants: n_xrows x 32 B, written by each split-form step call]
+//   [stage constants: n x 6 x EnsMemberConsts, written with the plan]
+// x work items are member rows (one warp walks the segments of the row); z items
 // are 128-column x z_tile-row tiles.  A persistent CTA takes items
 // blockIdx.x, blockIdx.x + gridDim.x, ...
 #include <algorithm>
@@ -14,8 +16,11 @@
 #include <numeric>
 #include <vector>
 
+#include <cmath>
+
 #include "mw_common.cuh"
 #include "mw_ensemble.cuh"
+#include "mw_split.cuh"
 
 namespace mw {
 namespace {
@@ -68,7 +73,7 @@ int layout(int n, const mw_ens_member* m, int z_tile, mw_ens_plan_info* info) {
   info->z_items_off = align16(info->x_items_off + sizeof(int2) * (size_t)nxi);
   info->xrows_off = align16(info->z_items_off + sizeof(int2) * (size_t)nzi);
   info->n_xrows = nrows;
-  info->bytes = align16(info->xrows_off + kEnsRowBytes * (size_t)nrows);
+  info->bytes = align16(ens_consts_off(*info) + sizeof(EnsMemberConsts) * kEnsConstsPerMember * (size_t)n);
   return MW_OK;
 }
 
@@ -119,6 +124,7 @@ int ens_step(void* plan, const mw_ens_plan_info* info, const double* hyc, const 
   const int2* xi = (const int2*)((const char*)plan + info->x_items_off);
   const int2* zi = (const int2*)((const char*)plan + info->z_items_off);
   es.xrows = (const char*)plan + info->xrows_off;
+  es.mconsts = (const char*)plan + ens_consts_off(*info);
   es.n_xrows = info->n_xrows;
   es.n_members = info->n_members;
   if (std::is_same<T, double>::value && nsteps > 0 &&
@@ -174,6 +180,28 @@ extern "C" int mw_ensemble_plan(int n_members, const mw_ens_member* members, int
   std::memcpy(host.data() + info->members_off, members, sizeof(mw_ens_member) * (size_t)n_members);
   int2* xi = (int2*)(host.data() + info->x_items_off);
   int2* zi = (int2*)(host.data() + info->z_items_off);
+  EnsMemberConsts* mc = (EnsMemberConsts*)(host.data() + ens_consts_off(*info));
+  for (int e = 0; e < n_members; ++e) {
+    const mw_ens_member& m = members[e];
+    for (int dir = 0; dir < 2; ++dir) {
+      const double d = dir == 0 ? m.dx : m.dz;
+      const double hv = -kHvBeta * d / (16 * m.dt);
+      for (int k = 0; k < 3; ++k) {
+        const double dts = m.dt / (double)(3 - k);  // dt/3, dt/2, dt/1 as evolve forms them
+        EnsMemberConsts& c = mc[(e * 2 + dir) * 3 + k];
+        const split::dwc hv12 = split::split_host(12.0 * hv), d12 = split::split_host(12.0 * d),
+                         gz12 = split::split_host(12.0 * m.dz * kGrav), c12 = split::split_host(dts / (12.0 * d));
+        c.hv12[0] = hv12.h, c.hv12[1] = hv12.l;
+        c.d12[0] = d12.h, c.d12[1] = d12.l;
+        c.gz12[0] = gz12.h, c.gz12[1] = gz12.l;
+        c.c12[0] = c12.h, c.c12[1] = c12.l;
+        c.c12s = dts / (12.0 * d) * split::kTwoPow896;  // exact: a power-of-two scale
+        c.pad = 0.0;
+        MW_REQUIRE(std::isfinite(c.c12s), MW_ERR_INVALID_ARG,
+                   "member %d: dt / (12 d) = %g is above the split form's range", e, dts / (12.0 * d));
+      }
+    }
+  }
   long long a = 0, b = 0;
   for (int e = 0; e < n_members; ++e) {
     for (int k = 0; k < members[e].nz; ++k) xi[a++] = make_int2(e, k);

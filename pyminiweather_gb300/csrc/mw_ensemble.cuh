@@ -29,6 +29,7 @@ struct EnsStageT {
   T* out;
   const void* xrows;  // split form: row constants indexed like the cell-centre backgrounds
   long long n_xrows;  // entries of xrows
+  const void* mconsts;  // split form: EnsMemberConsts per (member, direction, stage)
   int n_members;
   cudaStream_t stream;
 };
@@ -42,6 +43,22 @@ int ens_f32_occupancy(int direction, int* blocks_per_sm);
 
 constexpr int kEnsZTileMax = 64;
 constexpr size_t kEnsRowBytes = 32;  // one row's background constants (four double-FP32 pairs)
+
+// Stage constants of one member for one direction-stage, formed on the host
+// when the plan is built, exactly as the single-grid launch forms them:
+// (h, l) float pairs of 12 hv, 12 d, 12 dz g and dt_stage / (12 d), and
+// dt_stage / (12 d) * 2^896 in FP64.  Entry (member * 2 + (direction == z)) * 3
+// + stage (stage 0, 1, 2: dt/3, dt/2, dt).
+struct EnsMemberConsts {
+  float hv12[2], d12[2], gz12[2], c12[2];
+  double c12s;
+  double pad;
+};
+static_assert(sizeof(EnsMemberConsts) == 48, "EnsMemberConsts layout");
+constexpr int kEnsConstsPerMember = 6;
+inline size_t ens_consts_off(const mw_ens_plan_info& info) {
+  return (info.xrows_off + kEnsRowBytes * (size_t)info.n_xrows + 15) & ~(size_t)15;
+}
 
 // Row-constant table of the split ensemble x kernels: entry j from hyc[j], hytc[j].
 int launch_ens_split_rowtable(const double* hyc, const double* hytc, long long n, void* table, cudaStream_t stream);

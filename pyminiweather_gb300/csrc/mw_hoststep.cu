@@ -92,6 +92,11 @@ cudaError_t copy_band(double* dst, const double* src, const Geom& g, int a0, int
 
 using namespace mw;
 
+namespace mw {
+template <typename T>
+int check_finite_blocking(int nx, int nz, const T* state, cudaStream_t stream);  // mw_aux.cu
+}
+
 extern "C" int mw_step_f64(int nx, int nz, double dx, double dz, double dt_full, double dt, const double* hyc,
                            const double* hytc, const double* hyi, const double* hyti, const double* hypi,
                            const double* src_w, double* state, double* state_tmp, double* scratch, int nsteps,
@@ -179,6 +184,7 @@ extern "C" int mw_step_f64_host(int nx, int nz, double dx, double dz, double dt_
   //   z then x, iteration i: z1(i), z2(i-1), z3(i-2), x(i-3), out(i-3)
   // (z3(b+1) reads state_tmp rows of band b, which x(b) rewrites; z1(b+1) and
   // z2(b+1) read the state and scratch rows of band b, which x(b) rewrites too.)
+  auto wavefront = [&]() -> int {
   for (int i = 0; i < nb + 3; ++i) {
     if (*reverse) {  // x then z
       if (i < nb && ((st = wait_in(i)) || (st = x_band(i)))) return st;
@@ -196,9 +202,17 @@ extern "C" int mw_step_f64_host(int nx, int nz, double dx, double dz, double dt_
     }
     if (i - 3 >= 0 && i - 3 < nb && (st = band_out(i - 3))) return st;
   }
+  return MW_OK;
+  };
+  st = wavefront();
+  // The caller's stream waits for both copy streams, also after an error.
   e = cudaEventRecord(c->done, c->d2h);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c->done, 0);
+  if (e == cudaSuccess) e = cudaEventRecord(c->done, c->h2d);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c->done, 0);
+  if (st) return st;
   if (e != cudaSuccess) return fail(MW_ERR_CUDA, "join: %s", cudaGetErrorString(e));
   *reverse = *reverse ? 0 : 1;
+  if (flags & MW_FLAG_CHECK_FINITE) return check_finite_blocking(nx, nz, (const double*)state, s);
   return MW_OK;
 }

@@ -388,14 +388,15 @@ __device__ SplitArgs member_args(const EnsStage& es, int e) {
   a.forcing = es.forcing + m.state_off;
   a.out = es.out + m.state_off;
   a.flags = es.flags;
-  const double d = es.direction == MW_DIR_X ? m.dx : m.dz;
-  const double dts = m.dt / (double)es.stage_div;  // dt/3, dt/2, dt/1 as evolve forms them
-  const double hv = -kHvBeta * d / (16 * m.dt);
-  a.hv12 = split_rn(12.0 * hv);
-  a.c12s = dts / (12.0 * d) * kTwoPow896;  // exact: a power-of-two scale
-  a.d12 = split_rn(12.0 * d);
-  a.gz12 = split_rn(12.0 * m.dz * kGrav);
-  a.c12 = split_rn(dts / (12.0 * d));
+  // stage constants from the plan (formed on the host, no FP64 work per item)
+  const EnsMemberConsts& c =
+      MW_AT(reinterpret_cast<const EnsMemberConsts*>(es.mconsts),
+            (e * 2 + (es.direction == MW_DIR_X ? 0 : 1)) * 3 + (3 - es.stage_div), (long long)kEnsConstsPerMember * es.n_members);
+  a.hv12 = {c.hv12[0], c.hv12[1]};
+  a.c12s = c.c12s;
+  a.d12 = {c.d12[0], c.d12[1]};
+  a.gz12 = {c.gz12[0], c.gz12[1]};
+  a.c12 = {c.c12[0], c.c12[1]};
   return a;
 }
 

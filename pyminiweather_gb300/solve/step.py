@@ -135,6 +135,8 @@ def evolve_host(params: Dict, fields, h_in: torch.Tensor, h_out: torch.Tensor, d
     rv = ctypes.c_int(1 if reverse_direction else 0)
     hb = [_native.ptr(a) for a in fields.backgrounds()]
     flags = params.get("step_flags", _native.MW_FLAG_WRITE_HALO)
+    if params.get("check_finite"):  # blocking: raises MiniWeatherError (status 7) on NaN / Inf
+        flags |= _native.MW_FLAG_CHECK_FINITE
     _native.call("mw_step_f64_host", fields.nx, fields.nz, float(params["dx"]), float(params["dz"]),
                  float(params["dt"]), float(dt), *hb, _native.ptr(fields.src_w), ctypes.c_void_p(h_in.data_ptr()),
                  ctypes.c_void_p(h_out.data_ptr()), _native.ptr(fields.state), _native.ptr(fields.state_tmp),

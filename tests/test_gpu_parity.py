@@ -388,3 +388,15 @@ def test_nonfinite_detection(dtype):
         evolve(dict(p, check_finite=True), f, None, dt=p["dt"])
     assert ei.value.status == 7
     assert count_nonfinite(f) > 2  # the NaN spread through the stencil
+    if dtype == torch.float64:  # the host-buffer step (row bands) checks the same way
+        from pyminiweather_gb300.solve import evolve_host
+        q = make_params(64, 48, "collision")
+        g = initialize_fields(q)
+        init(g, q, None)
+        h = g.state.cpu().pin_memory()
+        evolve_host(dict(q, check_finite=True), g, h, h, dt=q["dt"], nbands=3)
+        torch.cuda.synchronize()
+        h[2, 2 + 30, 2 + 11] = float("nan")
+        with pytest.raises(_native.MiniWeatherError) as ei:
+            evolve_host(dict(q, check_finite=True), g, h, h, dt=q["dt"], nbands=3)
+        assert ei.value.status == 7
