@@ -156,12 +156,17 @@ __device__ __forceinline__ RowS x_row_consts(const SplitArgs& a, int k) {
   return row_consts(MW_AT(a.hyc, k + kHs, a.nz + 2 * kHs), hrt, kC0 * pow(hrt, kGamma));
 }
 
-// row_at(k): the row constants of row k.
-template <int FMT, typename RowAt>
+// row_at(k): the row constants of row k.  prologue() runs once, after the
+// first segment's loads are issued (so that their latency overlaps it), also
+// when the range is empty (it may contain a CTA barrier).
+template <int FMT, typename RowAt, typename Prologue>
 __device__ __forceinline__ void x_warp_segments(const SplitArgs& a, int nseg, long long g0, long long g1,
-                                                RowAt row_at, bool halo, SmemXW& sm) {
+                                                RowAt row_at, bool halo, SmemXW& sm, Prologue prologue) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (g0 >= g1) return;
+  if (g0 >= g1) {
+    prologue();
+    return;
+  }
   const Hv2 hv = make_hv2(ld(a.hv12));
   const dw d12 = ld(a.d12);
   int k = (int)(g0 / nseg), sg = (int)(g0 - (long long)k * nseg);
@@ -181,6 +186,7 @@ __device__ __forceinline__ void x_warp_segments(const SplitArgs& a, int nseg, lo
   };
   double v0[4] = {0, 0, 0, 0}, v1 = 0.0;
   load(k, sg * kWCells, v0, v1);
+  prologue();
   for (long long g = g0; g < g1; ++g) {
     const int x0 = sg * kWCells;
     const sidx row = (sidx)(k + kHs) * a.pitch;
@@ -339,12 +345,15 @@ __global__ void __launch_bounds__(kXThreads, MW_XSPLIT_MIN_BLOCKS) k_stage_x_spl
   const long long g0 = gbase + total * blockIdx.x / gridDim.x, g1 = gbase + total * (blockIdx.x + 1) / gridDim.x;
   if (g0 >= g1) return;
   const int row0 = (int)(g0 / nseg), nrows = (int)((g1 - 1) / nseg) - row0 + 1;  // nrows <= kXRowsMax (host)
-  for (int r = threadIdx.x; r < nrows; r += kXThreads) sm.row[r] = x_row_consts(a, row0 + r);
-  __syncthreads();
   const int w = threadIdx.x >> 5;
   const long long n = g1 - g0;
+  // the row-constant table (an FP64 pow per row) is formed while the warps'
+  // first loads are in flight
   x_warp_segments<FMT>(a, nseg, g0 + n * w / kXWarps, g0 + n * (w + 1) / kXWarps,
-                       [&](int k) { return sm.row[k - row0]; }, a.flags & MW_FLAG_WRITE_HALO, sm);
+                       [&](int k) { return sm.row[k - row0]; }, a.flags & MW_FLAG_WRITE_HALO, sm, [&]() {
+                         for (int r = threadIdx.x; r < nrows; r += kXThreads) sm.row[r] = x_row_consts(a, row0 + r);
+                         __syncthreads();
+                       });
 }
 
 // z, single grid: the CTA owns the contiguous range [u0, u1) of the
@@ -414,7 +423,7 @@ __global__ void __launch_bounds__(kXThreads, MW_XSPLIT_MIN_BLOCKS) k_ens_x_split
     const RowS r = MW_AT(reinterpret_cast<const RowS*>(es.xrows), MW_AT(es.members, item.x, es.n_members).cell_off + item.y + kHs,
                          es.n_xrows);
     x_warp_segments<FMT>(a, nseg, (long long)item.y * nseg, (long long)(item.y + 1) * nseg,
-                    [&](int) { return r; }, a.flags & MW_FLAG_WRITE_HALO, sm);
+                    [&](int) { return r; }, a.flags & MW_FLAG_WRITE_HALO, sm, []() {});
   }
 }
 
