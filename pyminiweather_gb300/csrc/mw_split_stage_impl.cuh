@@ -332,10 +332,13 @@ __device__ __forceinline__ void z_march(const SplitArgs& a, int cb, int kbeg, in
 // ---------------------------------------------------------------------------
 // Single grid: x CTA (blockIdx.x, row) walks a run of chunks; z CTA is one tile.
 #ifndef MW_XSPLIT_SEGS_PER_WARP
-#define MW_XSPLIT_SEGS_PER_WARP 32  // segments per warp (0: one resident wave of CTAs)
+#define MW_XSPLIT_SEGS_PER_WARP 48  // segments per warp (0: one resident wave of CTAs)
 #endif
 #ifndef MW_XSPLIT_MIN_BLOCKS
 #define MW_XSPLIT_MIN_BLOCKS 3
+#endif
+#ifndef MW_XSPLIT_WHOLE_WAVES
+#define MW_XSPLIT_WHOLE_WAVES 1  // round the grid up to a whole number of resident waves
 #endif
 // Segments [gbase, gbase + total) (rows gbase / nseg onwards).
 template <int FMT>
@@ -529,11 +532,15 @@ int launch_stage_split_fmt(int nx, int nz, double dx, double dz, double dt_full,
     int resident = 0, st = resident_ctas<FMT>(0, &resident);
     if (st) return st;
     // One resident wave (at least one segment per warp) for small grids;
-    // MW_XSPLIT_SEGS_PER_WARP segments per warp for large ones, so that the
-    // block scheduler evens out the warps' speeds; at most kXRowsMax rows per
-    // CTA range.
+    // about MW_XSPLIT_SEGS_PER_WARP segments per warp for large ones, in a
+    // whole number of resident waves of equal ranges, so that the block
+    // scheduler evens out the warps' speeds; at most kXRowsMax rows per CTA
+    // range.
     long long grid = std::min<long long>(resident, (total + kXWarps - 1) / kXWarps);
     if (MW_XSPLIT_SEGS_PER_WARP > 0) grid = std::max<long long>(grid, total / (kXWarps * MW_XSPLIT_SEGS_PER_WARP));
+#if MW_XSPLIT_WHOLE_WAVES
+    if (grid > resident) grid = (grid + resident - 1) / resident * resident;  // a whole number of waves
+#endif
     grid = std::max<long long>(grid, (rows + kXRowsMax - 3) / (kXRowsMax - 2));
     MW_REQUIRE(grid <= 0x7fffffffLL, MW_ERR_SHAPE, "grid too large for the x direction-stage launch");
     k_stage_x_split<FMT><<<(unsigned)grid, kXThreads, 0, stream>>>(a, nseg, total, (long long)r0 * nseg);
