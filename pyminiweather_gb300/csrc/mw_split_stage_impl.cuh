@@ -7,7 +7,8 @@ namespace {
 
 constexpr int kXThreads = 256;
 #ifndef MW_ZSPLIT_MIN_BLOCKS
-#define MW_ZSPLIT_MIN_BLOCKS 5  // z CTAs per SM the register allocation must allow
+#define MW_ZSPLIT_MIN_BLOCKS 5  // z CTAs per SM the register allocation must allow (one fewer
+                                // for the pair-reading stage, whose march needs more registers)
 #endif
 constexpr int kZThreads = 128;
 constexpr int kZTileMax = 64;  // rows per shared-memory row-constant table
@@ -365,7 +366,8 @@ __global__ void __launch_bounds__(kXThreads, MW_XSPLIT_MIN_BLOCKS) k_stage_x_spl
 // grid to a whole number of resident waves of equal ranges.
 // Rows [r0, r1) of every column block.
 template <int FMT>
-__global__ void __launch_bounds__(kZThreads, MW_ZSPLIT_MIN_BLOCKS) k_stage_z_split(SplitArgs a, int ncb, int r0, int r1) {
+__global__ void __launch_bounds__(kZThreads, FMT == kFromPair ? MW_ZSPLIT_MIN_BLOCKS - 1 : MW_ZSPLIT_MIN_BLOCKS)
+    k_stage_z_split(SplitArgs a, int ncb, int r0, int r1) {
   __shared__ SmemZ sm;
   const int rows = r1 - r0;
   const long long U = (long long)ncb * rows;
@@ -431,7 +433,8 @@ __global__ void __launch_bounds__(kXThreads, MW_XSPLIT_MIN_BLOCKS) k_ens_x_split
 }
 
 template <int FMT>
-__global__ void __launch_bounds__(kZThreads, MW_ZSPLIT_MIN_BLOCKS) k_ens_z_split(EnsStage es) {
+__global__ void __launch_bounds__(kZThreads, FMT == kFromPair ? MW_ZSPLIT_MIN_BLOCKS - 1 : MW_ZSPLIT_MIN_BLOCKS)
+    k_ens_z_split(EnsStage es) {
   __shared__ SmemZ sm;
   for (int it = blockIdx.x; it < es.n_items; it += gridDim.x) {
     const int2 item = MW_AT(es.items, it, es.n_items);  // (member, column block + ncb * tile)
