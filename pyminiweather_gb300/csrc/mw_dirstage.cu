@@ -432,8 +432,8 @@ __device__ StageArgs<float> member_args_f32(const EnsStageT<float>& es, int e) {
   a.plane = (long long)(m.nz + 2 * kHs) * a.pitch;
   a.dx = m.dx;
   a.dz = m.dz;
-  a.hv = -kHvBeta * (es.direction == MW_DIR_X ? m.dx : m.dz) / (16 * m.dt);
-  a.dt_stage = m.dt / (double)es.stage_div;
+  a.hv = 0.0;        // the FP32 kernels read hv_f, c_f, dt_f (below)
+  a.dt_stage = 0.0;
   a.hyc = es.hyc + m.cell_off;
   a.hytc = es.hytc + m.cell_off;
   a.hyi = es.hyi + m.int_off;
@@ -446,7 +446,11 @@ __device__ StageArgs<float> member_args_f32(const EnsStageT<float>& es, int e) {
   a.flags = es.flags;
   a.chunks_per_block = 0;
   a.z_tile = es.z_tile;
-  set_f32_constants(a, es.direction);
+  // hv_f, c_f, dt_f from the plan (formed on the host as set_f32_constants forms them)
+  const EnsMemberConsts& c = reinterpret_cast<const EnsMemberConsts*>(es.mconsts)[mconsts_index(es, e)];
+  a.hv_f = c.hv_f;
+  a.c_f = c.c_f;
+  a.dt_f = c.dt_f;
   return a;
 }
 

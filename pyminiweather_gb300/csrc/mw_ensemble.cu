@@ -196,7 +196,10 @@ extern "C" int mw_ensemble_plan(int n_members, const mw_ens_member* members, int
         c.gz12[0] = gz12.h, c.gz12[1] = gz12.l;
         c.c12[0] = c12.h, c.c12[1] = c12.l;
         c.c12s = dts / (12.0 * d) * split::kTwoPow896;  // exact: a power-of-two scale
-        c.pad = 0.0;
+        c.hv_f = (float)hv;
+        c.c_f = (float)(dts / d);
+        c.dt_f = (float)dts;
+        c.pad = 0.0f;
         MW_REQUIRE(std::isfinite(c.c12s), MW_ERR_INVALID_ARG,
                    "member %d: dt / (12 d) = %g is above the split form's range", e, dts / (12.0 * d));
       }

@@ -8,6 +8,19 @@
 
 namespace mw {
 
+// Stage constants of one member for one direction-stage, formed on the host
+// when the plan is built, exactly as the single-grid launches form them.
+// Split form: (h, l) float pairs of 12 hv, 12 d, 12 dz g and dt_stage / (12 d),
+// and dt_stage / (12 d) * 2^896 in FP64.  FP32 form: hv, dt_stage / d and
+// dt_stage rounded to float.  Entry (member * 2 + (direction == z)) * 3 + stage
+// (stage 0, 1, 2: dt/3, dt/2, dt).
+struct EnsMemberConsts {
+  float hv12[2], d12[2], gz12[2], c12[2];
+  double c12s;
+  float hv_f, c_f, dt_f, pad;
+};
+static_assert(sizeof(EnsMemberConsts) == 56, "EnsMemberConsts layout");
+
 // Arguments of one ensemble direction-stage launch (T = state storage type).
 template <typename T>
 struct EnsStageT {
@@ -29,11 +42,17 @@ struct EnsStageT {
   T* out;
   const void* xrows;  // split form: row constants indexed like the cell-centre backgrounds
   long long n_xrows;  // entries of xrows
-  const void* mconsts;  // split form: EnsMemberConsts per (member, direction, stage)
+  const void* mconsts;  // EnsMemberConsts per (member, direction, stage), written with the plan
   int n_members;
   cudaStream_t stream;
 };
 using EnsStage = EnsStageT<double>;
+
+// Index of member e's entry for this launch's direction and stage in mconsts.
+template <typename T>
+__host__ __device__ inline int mconsts_index(const EnsStageT<T>& es, int e) {
+  return (e * 2 + (es.direction == MW_DIR_X ? 0 : 1)) * 3 + (3 - es.stage_div);
+}
 
 // Launchers (defined next to the kernels they launch).
 int launch_ens_split(const EnsStage& es, int grid);
@@ -44,17 +63,6 @@ int ens_f32_occupancy(int direction, int* blocks_per_sm);
 constexpr int kEnsZTileMax = 64;
 constexpr size_t kEnsRowBytes = 32;  // one row's background constants (four double-FP32 pairs)
 
-// Stage constants of one member for one direction-stage, formed on the host
-// when the plan is built, exactly as the single-grid launch forms them:
-// (h, l) float pairs of 12 hv, 12 d, 12 dz g and dt_stage / (12 d), and
-// dt_stage / (12 d) * 2^896 in FP64.  Entry (member * 2 + (direction == z)) * 3
-// + stage (stage 0, 1, 2: dt/3, dt/2, dt).
-struct EnsMemberConsts {
-  float hv12[2], d12[2], gz12[2], c12[2];
-  double c12s;
-  double pad;
-};
-static_assert(sizeof(EnsMemberConsts) == 48, "EnsMemberConsts layout");
 constexpr int kEnsConstsPerMember = 6;
 inline size_t ens_consts_off(const mw_ens_plan_info& info) {
   return (info.xrows_off + kEnsRowBytes * (size_t)info.n_xrows + 15) & ~(size_t)15;

@@ -403,9 +403,8 @@ __device__ SplitArgs member_args(const EnsStage& es, int e) {
   a.out = es.out + m.state_off;
   a.flags = es.flags;
   // stage constants from the plan (formed on the host, no FP64 work per item)
-  const EnsMemberConsts& c =
-      MW_AT(reinterpret_cast<const EnsMemberConsts*>(es.mconsts),
-            (e * 2 + (es.direction == MW_DIR_X ? 0 : 1)) * 3 + (3 - es.stage_div), (long long)kEnsConstsPerMember * es.n_members);
+  const EnsMemberConsts& c = MW_AT(reinterpret_cast<const EnsMemberConsts*>(es.mconsts), mconsts_index(es, e),
+                                   (long long)kEnsConstsPerMember * es.n_members);
   a.hv12 = {c.hv12[0], c.hv12[1]};
   a.c12s = c.c12s;
   a.d12 = {c.d12[0], c.d12[1]};
