@@ -322,17 +322,17 @@ __device__ __forceinline__ void x_rowrun_t(const StageArgs<T>& a, int k, int cbe
 // thread per column marching the rows with a rolling 4-row window, the next
 // row loaded one step ahead.  halo: write the wall halo rows of these columns
 // (cb == 0 also does the four x-halo columns).
-template <typename T, int MODE>
+template <typename T, int MODE, int NC = kZThreads>
 __device__ __forceinline__ void z_tile_t(const StageArgs<T>& a, int cb, int z0, int zt, bool halo, SmemZT& sm) {
   const int z1 = min(z0 + zt, a.nz);
   if constexpr (MODE != MODE_NATIVE64) {
-    for (int r = threadIdx.x; r <= z1 - z0; r += kZThreads) {
+    for (int r = threadIdx.x; r <= z1 - z0; r += NC) {
       const int k = z0 + r;
       sm.row[r] = rowf_z(a.hyi[k], a.hyti[k], a.hypi[k]);
     }
     __syncthreads();
   }
-  const int c = cb * kZThreads + threadIdx.x;  // interior column
+  const int c = cb * NC + threadIdx.x;  // interior column
   if (halo && cb == 0 && threadIdx.x < 4) {
     const int hcol[4] = {0, 1, a.nx + kHs, a.nx + kHs + 1};
     write_z_halo_column(a, hcol[threadIdx.x]);
@@ -508,14 +508,15 @@ __global__ void __launch_bounds__(kXThreads) k_ens_x_f32(EnsStageT<float> es) {
   }
 }
 
-__global__ void __launch_bounds__(kZThreads) k_ens_z_f32(EnsStageT<float> es) {
+__global__ void __launch_bounds__(kEnsZCols) k_ens_z_f32(EnsStageT<float> es) {
   __shared__ SmemZT sm;
   for (int it = blockIdx.x; it < es.n_items; it += gridDim.x) {
     const int2 item = es.items[it];
     const StageArgs<float> a = member_args_f32(es, item.x);
-    const int ncb = (a.nx + kZThreads - 1) / kZThreads;
+    const int ncb = (a.nx + kEnsZCols - 1) / kEnsZCols;
     const int cb = item.y % ncb, tile = item.y / ncb;
-    z_tile_t<float, MODE_F32>(a, cb, tile * es.z_tile, es.z_tile, (a.flags & MW_FLAG_WRITE_HALO) && tile == 0, sm);
+    z_tile_t<float, MODE_F32, kEnsZCols>(a, cb, tile * es.z_tile, es.z_tile,
+                                         (a.flags & MW_FLAG_WRITE_HALO) && tile == 0, sm);
   }
 }
 
@@ -524,14 +525,14 @@ int launch_ens_f32(const EnsStageT<float>& es, int grid) {
   if (es.direction == MW_DIR_X)
     k_ens_x_f32<<<grid, kXThreads, 0, es.stream>>>(es);
   else
-    k_ens_z_f32<<<grid, kZThreads, 0, es.stream>>>(es);
+    k_ens_z_f32<<<grid, kEnsZCols, 0, es.stream>>>(es);
   return check_launch("ensemble FP32 stage launch");
 }
 
 int ens_f32_occupancy(int direction, int* blocks_per_sm) {
   cudaError_t e = direction == MW_DIR_X
                       ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_ens_x_f32, kXThreads, 0)
-                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_ens_z_f32, kZThreads, 0);
+                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_ens_z_f32, kEnsZCols, 0);
   if (e != cudaSuccess) return fail(MW_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
   return MW_OK;
 }

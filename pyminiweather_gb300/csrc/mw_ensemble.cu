@@ -8,7 +8,7 @@
 //   [row constants: n_xrows x 32 B, written by each split-form step call]
 //   [stage constants: n x 6 x EnsMemberConsts, written with the plan]
 // x work items are member rows (one warp walks the segments of the row); z items
-// are 128-column x z_tile-row tiles.  A persistent CTA takes items
+// are kEnsZCols-column x z_tile-row tiles.  A persistent CTA takes items
 // blockIdx.x, blockIdx.x + gridDim.x, ...
 #include <algorithm>
 #include <type_traits>
@@ -25,7 +25,6 @@
 namespace mw {
 namespace {
 
-constexpr int kEnsZThreads = 128;  // columns per z work item
 
 size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
 
@@ -61,7 +60,7 @@ int layout(int n, const mw_ens_member* m, int z_tile, mw_ens_plan_info* info) {
   for (int e = 0; e < n; ++e) {
     nrows = std::max(nrows, m[e].cell_off + m[e].nz + 2LL * kHs);
     nxi += m[e].nz;
-    nzi += (long long)((m[e].nx + kEnsZThreads - 1) / kEnsZThreads) * ((m[e].nz + z_tile - 1) / z_tile);
+    nzi += (long long)((m[e].nx + kEnsZCols - 1) / kEnsZCols) * ((m[e].nz + z_tile - 1) / z_tile);
   }
   MW_REQUIRE(nxi < (1LL << 31) && nzi < (1LL << 31), MW_ERR_SHAPE, "ensemble too large for one work list");
   info->n_members = n;
@@ -208,7 +207,7 @@ extern "C" int mw_ensemble_plan(int n_members, const mw_ens_member* members, int
   long long a = 0, b = 0;
   for (int e = 0; e < n_members; ++e) {
     for (int k = 0; k < members[e].nz; ++k) xi[a++] = make_int2(e, k);
-    const int ncb = (members[e].nx + kEnsZThreads - 1) / kEnsZThreads;
+    const int ncb = (members[e].nx + kEnsZCols - 1) / kEnsZCols;
     const int ntile = (members[e].nz + z_tile - 1) / z_tile;
     for (int t = 0; t < ntile; ++t)
       for (int cb = 0; cb < ncb; ++cb) zi[b++] = make_int2(e, cb + ncb * t);

@@ -61,6 +61,7 @@ int launch_ens_f32(const EnsStageT<float>& es, int grid);
 int ens_f32_occupancy(int direction, int* blocks_per_sm);
 
 constexpr int kEnsZTileMax = 64;
+constexpr int kEnsZCols = 64;  // columns per z work item (one CTA of kEnsZCols threads)
 constexpr size_t kEnsRowBytes = 32;  // one row's background constants (four double-FP32 pairs)
 
 constexpr int kEnsConstsPerMember = 6;

@@ -10,7 +10,7 @@ constexpr int kXThreads = 256;
 #define MW_ZSPLIT_MIN_BLOCKS 5  // z CTAs per SM the register allocation must allow (one fewer
                                 // for the pair-reading stage, whose march needs more registers)
 #endif
-constexpr int kZThreads = 128;
+constexpr int kZThreads = 128;  // single grid: columns per z CTA (ensemble: mw::kEnsZCols)
 constexpr int kZTileMax = 64;  // rows per shared-memory row-constant table
 constexpr int kZMinRows = 8;   // single grid: fewest rows per z CTA
 // Single-grid x: warps walk 31-cell segments independently (32 interfaces each).
@@ -261,17 +261,17 @@ __device__ __forceinline__ void x_warp_segments(const SplitArgs& a, int nseg, lo
 // the interface row constants are tabled in shared memory.  hbot / htop:
 // write the bottom / top wall halo rows of these columns of the forcing array
 // (cb == 0 also does the four x-halo columns).
-template <int FMT>
+template <int FMT, int NT = kZThreads>
 __device__ __forceinline__ void z_march(const SplitArgs& a, int cb, int kbeg, int kend, bool hbot, bool htop,
                                         SmemZ& sm) {
   if (FMT == kFromPair) hbot = htop = false;  // the pair-format forcing (internal scratch) keeps no halo
   __syncthreads();  // the previous table is no longer read
-  for (int r = threadIdx.x; r <= kend - kbeg; r += kZThreads) {
+  for (int r = threadIdx.x; r <= kend - kbeg; r += NT) {
     const int k = kbeg + r;
     sm.row[r] = row_consts(MW_AT(a.hyi, k, a.nz + 1), MW_AT(a.hyti, k, a.nz + 1), MW_AT(a.hypi, k, a.nz + 1));
   }
   __syncthreads();
-  const int c = cb * kZThreads + threadIdx.x;
+  const int c = cb * NT + threadIdx.x;
   if ((hbot || htop) && cb == 0 && threadIdx.x < 4)
     write_z_halo_column(a, threadIdx.x < 2 ? threadIdx.x : a.nx + threadIdx.x, hbot, htop);
   if (c >= a.nx) return;
@@ -432,17 +432,18 @@ __global__ void __launch_bounds__(kXThreads, MW_XSPLIT_MIN_BLOCKS) k_ens_x_split
 }
 
 template <int FMT>
-__global__ void __launch_bounds__(kZThreads, FMT == kFromPair ? MW_ZSPLIT_MIN_BLOCKS - 1 : MW_ZSPLIT_MIN_BLOCKS)
+__global__ void __launch_bounds__(kEnsZCols,
+                                  (kZThreads / kEnsZCols) * (FMT == kFromPair ? MW_ZSPLIT_MIN_BLOCKS - 1 : MW_ZSPLIT_MIN_BLOCKS))
     k_ens_z_split(EnsStage es) {
   __shared__ SmemZ sm;
   for (int it = blockIdx.x; it < es.n_items; it += gridDim.x) {
     const int2 item = MW_AT(es.items, it, es.n_items);  // (member, column block + ncb * tile)
     const SplitArgs a = member_args(es, item.x);
-    const int ncb = (a.nx + kZThreads - 1) / kZThreads;
+    const int ncb = (a.nx + kEnsZCols - 1) / kEnsZCols;
     const int cb = item.y % ncb, tile = item.y / ncb;
     const int k0 = tile * es.z_tile, kend = min(k0 + es.z_tile, a.nz);
     const bool halo = a.flags & MW_FLAG_WRITE_HALO;
-    z_march<FMT>(a, cb, k0, kend, halo && k0 == 0, halo && kend == a.nz, sm);
+    z_march<FMT, kEnsZCols>(a, cb, k0, kend, halo && k0 == 0, halo && kend == a.nz, sm);
   }
 }
 
@@ -460,11 +461,11 @@ int launch_ens_split(const EnsStage& es, int grid) {
       k_ens_x_split<kF64><<<grid, kXThreads, 0, es.stream>>>(es);
   } else {
     if (es.fmt == kToPair)
-      k_ens_z_split<kToPair><<<grid, kZThreads, 0, es.stream>>>(es);
+      k_ens_z_split<kToPair><<<grid, kEnsZCols, 0, es.stream>>>(es);
     else if (es.fmt == kFromPair)
-      k_ens_z_split<kFromPair><<<grid, kZThreads, 0, es.stream>>>(es);
+      k_ens_z_split<kFromPair><<<grid, kEnsZCols, 0, es.stream>>>(es);
     else
-      k_ens_z_split<kF64><<<grid, kZThreads, 0, es.stream>>>(es);
+      k_ens_z_split<kF64><<<grid, kEnsZCols, 0, es.stream>>>(es);
   }
   return check_launch("ensemble split stage launch");
 }
@@ -472,7 +473,7 @@ int launch_ens_split(const EnsStage& es, int grid) {
 int ens_split_occupancy(int direction, int* blocks_per_sm) {
   cudaError_t e = direction == MW_DIR_X
                       ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_ens_x_split<kF64>, kXThreads, 0)
-                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_ens_z_split<kF64>, kZThreads, 0);
+                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_ens_z_split<kF64>, kEnsZCols, 0);
   if (e != cudaSuccess) return fail(MW_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
   return MW_OK;
 }

@@ -137,7 +137,7 @@ def test_ensemble_plan_validation():
     mem = (M * 2)(M(64, 32, 312.5, 312.5, 0.1, 0, 0, 0), M(100, 50, 200.0, 200.0, 0.1, 4 * 68 * 36, 36, 33))
     assert L.mw_ensemble_plan_info(2, mem, 16, ctypes.byref(info)) == OK
     assert info.n_x_items == 32 + 50
-    assert info.n_z_items == 1 * 2 + 1 * 4
+    assert info.n_z_items == 1 * 2 + 2 * 4  # (64-column blocks) x (16-row tiles) per member
     assert info.bytes % 16 == 0 and info.z_items_off >= info.x_items_off + 8 * info.n_x_items
     # the split form's row-constant table: one 32-byte entry per cell-centre background value used
     assert info.n_xrows == max(0 + 32 + 4, 36 + 50 + 4)
