@@ -100,15 +100,15 @@ __device__ __forceinline__ dw rcp(dw y) {
 // Conversions by integer operations on the IEEE-754 bit patterns.
 
 // FP64 -> double-word.  h takes the leading 24 significand bits (truncated),
-// l the next 23 rounded to nearest, so |x - (h + l)| <= 2^-47 |x|.
+// l the other 29 rounded to 24 significant bits, so |x - (h + l)| <= 2^-47 |x|.
 //   h: the float bit pattern is bits 60..29 of the double (one funnel shift)
 //      with the exponent rebiased from 1023 to 127: adding 0x40000000 modulo
 //      2^32 turns the low 8 exponent bits into the float exponent for every
 //      exponent in float range; the sign is put back with one LOP3.
-//   l: the 29 remaining significand bits, rounded to 23, placed under the
-//      exponent of h minus 23 with an implicit 1 that a float subtraction
-//      removes exactly.
-// |x| < 2^-100 (zero included) gives (0, 0), absolute error < 8e-31; NaN, Inf
+//   l: the 29 remaining significand bits as an integer, converted to float
+//      (rounded to nearest) and scaled by sign * 2^(E - 52), E the exponent
+//      of x, a float built from the bits of h.
+// |x| < 2^-74 (zero included) gives (0, 0), absolute error < 6e-23; NaN, Inf
 // and |x| >= 2^128 give NaN.
 __device__ __forceinline__ dw from_f64(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
@@ -116,13 +116,12 @@ __device__ __forceinline__ dw from_f64(double x) {
   const unsigned ex = hi & 0x7ff00000u;
   const unsigned sh = __funnelshift_l(lo, hi, 3);
   const unsigned hb = ((sh + 0x40000000u) & 0x7fffffffu) | (hi & 0x80000000u);
-  const unsigned base = (hb & 0xff800000u) - (23u << 23);
-  const unsigned m23 = ((lo & 0x1fffffffu) + 32u) >> 6;
+  const float scale = __uint_as_float((hb & 0xff800000u) - (52u << 23));
   float h = __uint_as_float(hb);
-  float l = __uint_as_float(base + m23) - __uint_as_float(base);
+  float l = __uint2float_rn(lo & 0x1fffffffu) * scale;
   // one unsigned range test; the rare out-of-range values take a branch
-  if (ex - ((1023u - 100u) << 20) > ((100u + 127u) << 20)) {
-    h = ex < ((1023u - 100u) << 20) ? 0.0f : __uint_as_float(0x7fc00000u);
+  if (ex - ((1023u - 74u) << 20) > ((74u + 127u) << 20)) {
+    h = ex < ((1023u - 74u) << 20) ? 0.0f : __uint_as_float(0x7fc00000u);
     l = 0.0f;
   }
   return {h, l};
