@@ -449,9 +449,29 @@ __global__ void __launch_bounds__(kEnsZCols,
 
 }  // namespace
 
+// Resident CTAs per SM of the ensemble z kernel of format FMT, cached per device.
+template <int FMT>
+int ens_z_per_sm() {
+  static std::atomic<int> cache[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+  int v = cache[dev].load(std::memory_order_relaxed);
+  if (v > 0) return v;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_ens_z_split<FMT>, kEnsZCols, 0) != cudaSuccess || v < 1) v = 1;
+  cache[dev].store(v, std::memory_order_relaxed);
+  return v;
+}
+
 int launch_ens_split(const EnsStage& es, int grid) {
   if (es.n_items == 0) return MW_OK;
   MW_REQUIRE(es.fmt == kF64 || es.fmt == kToPair || es.fmt == kFromPair, MW_ERR_INVALID_ARG, "bad stage format");
+  // The grid is sized for the FP64-storage z kernel; the pair-reading one fits
+  // fewer CTAs per SM, so its persistent grid shrinks in proportion (its items
+  // are strided statically over the CTAs, which must all be resident at once).
+  if (es.direction == MW_DIR_Z && es.fmt == kFromPair) {
+    const int b0 = ens_z_per_sm<kF64>(), b1 = ens_z_per_sm<kFromPair>();
+    if (b1 < b0) grid = std::max(1, (int)((long long)grid * b1 / b0));
+  }
   if (es.direction == MW_DIR_X) {
     if (es.fmt == kToPair)
       k_ens_x_split<kToPair><<<grid, kXThreads, 0, es.stream>>>(es);
