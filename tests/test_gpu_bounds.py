@@ -31,7 +31,8 @@ DRIVER = textwrap.dedent("""
     _native.call("mw_debug_oob_count", ctypes.byref(n), 1)
     assert n.value == 1, n.value  # the planted index was caught (and diverted)
     for nx, nz, ic in [(2, 1, "collision"), (3, 2, "thermal"), (37, 13, "collision"), (31, 5, "gravity"),
-                       (62, 17, "density-current"), (130, 70, "collision"), (257, 129, "gravity")]:
+                       (62, 17, "density-current"), (130, 70, "collision"), (257, 129, "gravity"),
+                       (96, 320, "thermal")]:  # 16 host-step bands, the end ones half as tall
         p = make_params(nx, nz, ic)
         for flags in (1, 0):
             f = initialize_fields(p)
