@@ -417,8 +417,9 @@ __global__ void __launch_bounds__(kXThreads) k_stage_x(StageArgs<T> a) {
 template <typename T, int MODE>
 __global__ void __launch_bounds__(kZThreads) k_stage_z(StageArgs<T> a) {
   __shared__ SmemZT sm;
-  z_tile_t<T, MODE>(a, blockIdx.x, blockIdx.y * a.z_tile, a.z_tile,
-                    (a.flags & MW_FLAG_WRITE_HALO) && blockIdx.y == 0, sm);
+  // row tiles blockIdx.y, blockIdx.y + gridDim.y, ... (grid.y is capped at 65535)
+  for (int tile = blockIdx.y; (long long)tile * a.z_tile < a.nz; tile += gridDim.y)
+    z_tile_t<T, MODE>(a, blockIdx.x, tile * a.z_tile, a.z_tile, (a.flags & MW_FLAG_WRITE_HALO) && tile == 0, sm);
 }
 
 // ---------------------------------------------------------------------------
@@ -593,7 +594,7 @@ static int launch_stage(int nx, int nz, double dx, double dz, double dt_full, co
     dim3 grid((nchunks + a.chunks_per_block - 1) / a.chunks_per_block, (unsigned)min(nz, 65535));
     k_stage_x<T, MODE><<<grid, kXThreads, 0, stream>>>(a);
   } else {
-    dim3 grid((nx + kZThreads - 1) / kZThreads, (nz + a.z_tile - 1) / a.z_tile);
+    dim3 grid((nx + kZThreads - 1) / kZThreads, (unsigned)min((nz + a.z_tile - 1) / a.z_tile, 65535));
     k_stage_z<T, MODE><<<grid, kZThreads, 0, stream>>>(a);
   }
   return check_launch(direction == MW_DIR_X ? "x direction-stage launch" : "z direction-stage launch");
