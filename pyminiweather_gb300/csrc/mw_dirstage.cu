@@ -415,11 +415,10 @@ __global__ void __launch_bounds__(kXThreads) k_stage_x(StageArgs<T> a) {
 }
 
 template <typename T, int MODE>
-__global__ void __launch_bounds__(kZThreads) k_stage_z(StageArgs<T> a) {
+__global__ void __launch_bounds__(kZThreads) k_stage_z(StageArgs<T> a, int tile0) {
   __shared__ SmemZT sm;
-  // row tiles blockIdx.y, blockIdx.y + gridDim.y, ... (grid.y is capped at 65535)
-  for (int tile = blockIdx.y; (long long)tile * a.z_tile < a.nz; tile += gridDim.y)
-    z_tile_t<T, MODE>(a, blockIdx.x, tile * a.z_tile, a.z_tile, (a.flags & MW_FLAG_WRITE_HALO) && tile == 0, sm);
+  const int tile = tile0 + blockIdx.y;  // row tile (grid.y is capped at 65535: one launch per 65535 tiles)
+  z_tile_t<T, MODE>(a, blockIdx.x, tile * a.z_tile, a.z_tile, (a.flags & MW_FLAG_WRITE_HALO) && tile == 0, sm);
 }
 
 // ---------------------------------------------------------------------------
@@ -594,8 +593,15 @@ static int launch_stage(int nx, int nz, double dx, double dz, double dt_full, co
     dim3 grid((nchunks + a.chunks_per_block - 1) / a.chunks_per_block, (unsigned)min(nz, 65535));
     k_stage_x<T, MODE><<<grid, kXThreads, 0, stream>>>(a);
   } else {
-    dim3 grid((nx + kZThreads - 1) / kZThreads, (unsigned)min((nz + a.z_tile - 1) / a.z_tile, 65535));
-    k_stage_z<T, MODE><<<grid, kZThreads, 0, stream>>>(a);
+    const int ntiles = (nz + a.z_tile - 1) / a.z_tile;
+    for (int t0 = 0; t0 < ntiles; t0 += 65535) {
+      dim3 grid((nx + kZThreads - 1) / kZThreads, (unsigned)min(ntiles - t0, 65535));
+      k_stage_z<T, MODE><<<grid, kZThreads, 0, stream>>>(a, t0);
+      if (t0 + 65535 < ntiles) {
+        const int st = check_launch("z direction-stage launch");
+        if (st) return st;
+      }
+    }
   }
   return check_launch(direction == MW_DIR_X ? "x direction-stage launch" : "z direction-stage launch");
 }
