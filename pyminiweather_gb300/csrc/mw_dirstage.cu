@@ -318,7 +318,7 @@ __device__ __forceinline__ void x_rowrun_t(const StageArgs<T>& a, int k, int cbe
   }
 }
 
-// z: columns [cb*128, cb*128+128), rows [z0, z0+zt), zt <= kEnsZTileMax; one
+// z: columns [cb*NC, cb*NC+NC) (NC threads), rows [z0, z0+zt), zt <= kEnsZTileMax; one
 // thread per column marching the rows with a rolling 4-row window, the next
 // row loaded one step ahead.  halo: write the wall halo rows of these columns
 // (cb == 0 also does the four x-halo columns).
