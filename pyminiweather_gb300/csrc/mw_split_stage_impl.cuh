@@ -255,7 +255,7 @@ __device__ __forceinline__ void x_warp_segments(const SplitArgs& a, int nseg, lo
   }
 }
 
-// z: columns [cb*128, cb*128+128), rows [kbeg, kend), kend - kbeg <=
+// z: columns [cb*NT, cb*NT+NT) (the NT threads of the CTA), rows [kbeg, kend), kend - kbeg <=
 // kZTileMax: one thread per column marching the rows with a rolling window of
 // variable pairs; the next row and the init values are loaded one step ahead;
 // the interface row constants are tabled in shared memory.  hbot / htop:
