@@ -156,6 +156,35 @@ __global__ void k_gravity_source(int nx, int nz, double xlen, double zlen, const
 constexpr int kStatThreads = 256;
 constexpr int kStatMaxBlocks = 1024;
 
+// Sum of a and b over the NT threads of the block, in a fixed order (so the
+// result is bit-reproducible): a shuffle tree inside each warp, then the warp
+// sums by the same tree in warp 0.  Thread 0 ends with the sums; wa / wb hold
+// NT / 32 doubles of shared memory.
+template <int NT>
+__device__ __forceinline__ void block_sum2(double& a, double& b, double* wa, double* wb) {
+  static_assert(NT % 32 == 0 && NT / 32 <= 32, "block size");
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a = add_(a, __shfl_down_sync(0xffffffffu, a, o));
+    b = add_(b, __shfl_down_sync(0xffffffffu, b, o));
+  }
+  if (lane == 0) {
+    wa[w] = a;
+    wb[w] = b;
+  }
+  __syncthreads();
+  if (w == 0) {
+    a = lane < NT / 32 ? wa[lane] : 0.0;
+    b = lane < NT / 32 ? wb[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a = add_(a, __shfl_down_sync(0xffffffffu, a, o));
+      b = add_(b, __shfl_down_sync(0xffffffffu, b, o));
+    }
+  }
+}
+
 __device__ __forceinline__ double load_state(const double* p) { return *p; }
 __device__ __forceinline__ double load_state(const float* p) { return split::f2d(*p); }
 
@@ -163,7 +192,7 @@ template <typename T>
 __global__ void __launch_bounds__(kStatThreads) k_stats_partial(int nx, int nz, int rpb, double dx, double dz,
                                                                 const double* hyc, const double* hytc, const T* state,
                                                                 double* part) {
-  __shared__ double sm[kStatThreads], se[kStatThreads];
+  __shared__ double sm[kStatThreads / 32], se[kStatThreads / 32];
   const int NX = nx + 2 * kHs;
   const long long plane = (long long)NX * (nz + 2 * kHs);
   double m = 0.0, e = 0.0;
@@ -185,39 +214,23 @@ __global__ void __launch_bounds__(kStatThreads) k_stats_partial(int nx, int nz, 
       e = add_(e, add_(ke, ie));
     }
   }
-  sm[threadIdx.x] = m;
-  se[threadIdx.x] = e;
-  __syncthreads();
-  for (int s = kStatThreads / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) {
-      sm[threadIdx.x] = add_(sm[threadIdx.x], sm[threadIdx.x + s]);
-      se[threadIdx.x] = add_(se[threadIdx.x], se[threadIdx.x + s]);
-    }
-    __syncthreads();
-  }
+  block_sum2<kStatThreads>(m, e, sm, se);
   if (threadIdx.x == 0) {
-    part[2 * blockIdx.x] = sm[0];
-    part[2 * blockIdx.x + 1] = se[0];
+    part[2 * blockIdx.x] = m;
+    part[2 * blockIdx.x + 1] = e;
   }
 }
 
 __global__ void __launch_bounds__(kStatMaxBlocks) k_stats_final(int nblocks, double dx, double dz, const double* part,
                                                                 double* out2) {
-  __shared__ double sm[kStatMaxBlocks], se[kStatMaxBlocks];
+  __shared__ double sm[kStatMaxBlocks / 32], se[kStatMaxBlocks / 32];
   const int t = threadIdx.x;
-  sm[t] = t < nblocks ? part[2 * t] : 0.0;
-  se[t] = t < nblocks ? part[2 * t + 1] : 0.0;
-  __syncthreads();
-  for (int s = kStatMaxBlocks / 2; s > 0; s >>= 1) {
-    if (t < s) {
-      sm[t] = add_(sm[t], sm[t + s]);
-      se[t] = add_(se[t], se[t + s]);
-    }
-    __syncthreads();
-  }
+  double m = t < nblocks ? part[2 * t] : 0.0;
+  double e = t < nblocks ? part[2 * t + 1] : 0.0;
+  block_sum2<kStatMaxBlocks>(m, e, sm, se);
   if (t == 0) {
-    out2[0] = mul_(mul_(sm[0], dx), dz);
-    out2[1] = mul_(mul_(se[0], dx), dz);
+    out2[0] = mul_(mul_(m, dx), dz);
+    out2[1] = mul_(mul_(e, dx), dz);
   }
 }
 
