@@ -21,10 +21,12 @@
 // rule (bcs.py:92-148): rho', (rho theta)' copied, (rho u)' scaled by the
 // background ratio, (rho w)' zero.
 //
-// One kernel per stage: each warp walks 29-cell segments of a line (a row
-// in x, a column in z); lane l owns interface p0-1+l and, for l < 29, cell
-// p0+l.  Interface background constants come from a table that
-// k_vjp_row_table writes into the caller's workspace.
+// One kernel per stage: a warp walks 29-cell segments of a line (a row in x,
+// a column in z); lane l owns interface p0-1+l and, for l < 29, cell p0+l.
+// In x the warps read their rows directly; in z (k_vjp_split_zt) a CTA stages
+// a tile of a few columns x one segment through shared memory so that every
+// global access is row-contiguous.  Interface background constants come from
+// a table that k_vjp_row_table writes into the caller's workspace.
 #include <algorithm>
 
 #include "mw_common.cuh"
@@ -331,6 +333,145 @@ __global__ void __launch_bounds__(kVThreads) k_vjp_split(VjpSplitArgs a, int nse
   vjp_segments<DIR>(a, nseg, g0 + n * w / kVWarps, g0 + n * (w + 1) / kVWarps, sm);
 }
 
+// z, tiled: the z lines are columns, so a warp walking one column directly
+// would read 32 different rows per access.  Here a CTA takes a tile of kZTCols
+// columns x one 29-row segment: the forcing (rows p0-3 .. p0+31) and g (rows
+// p0-2 .. p0+30) of its columns are staged into shared memory by row-contiguous
+// loads (consecutive threads, consecutive columns); each warp then runs the
+// per-column computation of vjp_segments on its column from shared memory, and
+// the results are written back row-contiguously by the whole CTA.
+#ifndef MW_VJP_ZT_COLS
+#define MW_VJP_ZT_COLS 4
+#endif
+constexpr int kZTCols = MW_VJP_ZT_COLS;  // columns per tile = warps per CTA (one column each)
+constexpr int kZTThreads = 32 * kZTCols;
+constexpr int kZTPos = kVCells + 6;  // staged forcing positions
+constexpr int kZTG = kVCells + 4;    // staged g positions
+struct SmemVZ {
+  dw2 sF[2][kZTCols][kZTPos];     // forcing pairs [pair][column][position p0-3+j]
+  dw2 sG[2][kZTCols][kZTG];       // g pairs [pair][column][position p0-2+i]
+  dw2 sO[2][kZTCols][kVCells];    // S (the scaled increment) [pair][column][cell p0+t]
+  dw2 sH[kZTCols][2][32];         // AbG at interfaces p0-1 .. p0+30 (per warp)
+  dw2 sD[kZTCols][2][32];         // Gd
+};
+
+__global__ void __launch_bounds__(kZTThreads) k_vjp_split_zt(VjpSplitArgs a, int nseg, int ncb, long long total) {
+  extern __shared__ __align__(16) unsigned char vz_raw[];
+  SmemVZ& sm = *reinterpret_cast<SmemVZ*>(vz_raw);
+  if (blockIdx.x == 0) zero_frame(a);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const dw hv12 = ld(a.hv12);
+  const dw2 hv = splat(hv12);
+  const float2 nhv = f2splat(-hv12.h);
+  for (long long it = blockIdx.x; it < total; it += gridDim.x) {
+    const int cb = (int)(it % ncb), sg = (int)(it / ncb);
+    const int c0 = cb * kZTCols, p0 = sg * kVCells;
+    // stage forcing and g (column fastest over the threads)
+    for (int e = threadIdx.x; e < kZTCols * kZTPos; e += kZTThreads) {
+      const int cl = e % kZTCols, j = e / kZTCols, c = c0 + cl, pp = p0 - 3 + j;
+      double v[4] = {0, 0, 0, 0};
+      if (c < a.nx && pp >= -2 && pp <= a.nz + 1) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[q] = fval<MW_DIR_Z>(a, q, c, pp);
+      }
+      dw2 pk[2];
+      pack4(v, pk);
+      sm.sF[0][cl][j] = pk[0];
+      sm.sF[1][cl][j] = pk[1];
+    }
+    for (int e = threadIdx.x; e < kZTCols * kZTG; e += kZTThreads) {
+      const int cl = e % kZTCols, i = e / kZTCols, c = c0 + cl;
+      double v[4] = {0, 0, 0, 0};
+      if (c < a.nx) gload<MW_DIR_Z>(a, c, p0 - 2 + i, v);
+      dw2 pk[2];
+      pack4(v, pk);
+      sm.sG[0][cl][i] = pk[0];
+      sm.sG[1][cl][i] = pk[1];
+    }
+    __syncthreads();
+    for (int cl = w; cl < kZTCols; cl += kZTCols) {
+      if (c0 + cl >= a.nx) break;  // warp-uniform; columns beyond nx are skipped by every later warp too
+      // interface f = p0 - 1 + lane
+      {
+        const int f = p0 - 1 + lane;
+        dw2 Ab[2], Gd[2];
+        if (f >= 0 && f <= a.nz) {
+          Gd[0] = sub2(sm.sG[0][cl][lane + 1], sm.sG[0][cl][lane]);
+          Gd[1] = sub2(sm.sG[1][cl][lane + 1], sm.sG[1][cl][lane]);
+          dw2 s[2][4];
+#pragma unroll
+          for (int pr = 0; pr < 2; ++pr)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) s[pr][j] = sm.sF[pr][cl][lane + j];
+          const RowV rv = MW_AT(a.rows, f, a.nz + 1);
+          const bool wall = f == 0 || f == a.nz;
+          jt_g<MW_DIR_Z>(s, rv, Gd, wall, Ab);
+          if (wall) {
+            Gd[0].h.x = 0.f;
+            Gd[0].l.x = 0.f;
+          }
+        } else {
+          Ab[0] = Ab[1] = Gd[0] = Gd[1] = pack(dw{0.f, 0.f}, dw{0.f, 0.f});
+        }
+        sm.sH[w][0][lane] = Ab[0];
+        sm.sH[w][1][lane] = Ab[1];
+        sm.sD[w][0][lane] = Gd[0];
+        sm.sD[w][1][lane] = Gd[1];
+      }
+      __syncwarp();
+      // cell t = p0 + lane
+      const int t = p0 + lane;
+      if (lane < kVCells && t < a.nz) {
+        dw2 S[2];
+#pragma unroll
+        for (int pr = 0; pr < 2; ++pr) {
+          const dw2 Ac = acombo2(sm.sH[w][pr][lane], sm.sH[w][pr][lane + 1], sm.sH[w][pr][lane + 2], sm.sH[w][pr][lane + 3]);
+          const dw2 Dc = dcombo2(sm.sD[w][pr][lane], sm.sD[w][pr][lane + 1], sm.sD[w][pr][lane + 2], sm.sD[w][pr][lane + 3]);
+          S[pr] = add2(Ac, mul2n(Dc, hv, nhv));
+        }
+        if (t == 0 || t == a.nz - 1) {  // halo-row taps, as in vjp_segments
+          const int hs[6] = {-2, -1, -1, a.nz, a.nz, a.nz + 1};
+          const int fs[6] = {0, 0, 1, a.nz - 1, a.nz, a.nz};
+          const int js[6] = {0, 1, 0, 3, 2, 3};
+          for (int m = (t == 0 ? 0 : 3); m < (t == a.nz - 1 ? 6 : 3); ++m) {
+            const int li = fs[m] - p0 + 1;
+            dw2 T0 = tap_term(js[m], sm.sH[w][0][li], sm.sD[w][0][li], hv, nhv);
+            dw2 T1 = tap_term(js[m], sm.sH[w][1][li], sm.sD[w][1][li], hv, nhv);
+            T0 = pack(lo_of(T0), mul(hi_of(T0), halo_umom_weight(a, hs[m])));
+            T1 = pack(dw{0.f, 0.f}, hi_of(T1));
+            S[0] = add2(S[0], T0);
+            S[1] = add2(S[1], T1);
+          }
+        }
+        sm.sO[0][cl][lane] = S[0];
+        sm.sO[1][cl][lane] = S[1];
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+    // g_dst = bases + dt/(12 dz) S [- dt grav g_w on rho'], row-contiguous
+    for (int e = threadIdx.x; e < kZTCols * kVCells; e += kZTThreads) {
+      const int cl = e % kZTCols, j = e / kZTCols, c = c0 + cl, t = p0 + j;
+      if (c >= a.nx || t >= a.nz) continue;
+      const dw2 S0 = sm.sO[0][cl][j], S1 = sm.sO[1][cl][j];
+      const dw d[4] = {lo_of(S0), hi_of(S0), lo_of(S1), hi_of(S1)};
+      const long long o = cell_off<MW_DIR_Z>(a, c, t);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const long long oq = q * a.plane + o;
+        double base = 0.0;
+        if (a.add_gout) base += MW_AT(a.gout, oq, 4 * a.plane);
+        if (a.base_a) base += MW_AT(a.base_a, oq, 4 * a.plane);
+        if (a.base_b) base += MW_AT(a.base_b, oq, 4 * a.plane);
+        double v = fma(a.cs, to_f64_scaled(d[q]), base);
+        if (q == DENS) v = fma(-a.dtg, MW_AT(a.gout, WMOM * a.plane + o, 4 * a.plane), v);
+        MW_AT(a.gdst, oq, 4 * a.plane) = v;
+      }
+    }
+    __syncthreads();  // the tiles are rewritten by the next item
+  }
+}
+
 int vjp_resident_ctas(int* out) {
   int per_sm = 0, sms = 0, dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -389,10 +530,21 @@ int launch_vjp_split(int nx, int nz, double dx, double dz, double dt_full, const
   long long grid = std::min<long long>(resident, (total + kVWarps - 1) / kVWarps);
   grid = std::max<long long>(grid, total / (kVWarps * 32));
   grid = std::max<long long>(1, std::min<long long>(grid, 0x7fffffffLL));
-  if (direction == MW_DIR_X)
+  if (direction == MW_DIR_X) {
     k_vjp_split<MW_DIR_X><<<(unsigned)grid, kVThreads, 0, stream>>>(a, nseg, total);
-  else
-    k_vjp_split<MW_DIR_Z><<<(unsigned)grid, kVThreads, 0, stream>>>(a, nseg, total);
+  } else {  // tiles of kZTCols columns x one segment, a grid of resident CTAs
+    const int ncb = (nx + kZTCols - 1) / kZTCols;
+    const long long tiles = (long long)ncb * nseg;
+    int per_sm = 0, sms = 0, dev = 0;
+    const size_t smem = sizeof(SmemVZ);
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_vjp_split_zt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_vjp_split_zt, kZTThreads, smem);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return fail(MW_ERR_CUDA, "z vjp setup: %s", cudaGetErrorString(e));
+    const long long gz = std::max<long long>(1, std::min<long long>(tiles, (long long)std::max(1, per_sm) * sms));
+    k_vjp_split_zt<<<(unsigned)gz, kZTThreads, smem, stream>>>(a, nseg, ncb, tiles);
+  }
   return check_launch("split vjp launch");
 }
 
