@@ -323,6 +323,9 @@ __device__ __forceinline__ void zero_frame(const VjpSplitArgs& a) {
   }
 }
 
+// Launched for the x direction (rows are contiguous); the z direction runs
+// k_vjp_split_zt below, which applies the same per-line computation to
+// shared-memory tiles.
 template <int DIR>
 __global__ void __launch_bounds__(kVThreads) k_vjp_split(VjpSplitArgs a, int nseg, long long total) {
   __shared__ SmemV sm;
