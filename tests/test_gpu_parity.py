@@ -316,7 +316,8 @@ def test_errors_surface_as_exceptions():
 
 @pytest.mark.parametrize("nx,nz,nbands,flags", [(512, 256, 8, 1), (300, 150, 16, 1), (300, 150, 4, 0), (64, 40, 8, 1),
                                                 (100, 20, 8, 1), (96, 1024, 64, 1), (130, 48, 3, 0), (70, 35, 2, 1),
-                                                (200, 320, 12, 0), (256, 256, 16, 1)])
+                                                (200, 320, 12, 0), (256, 256, 16, 1),
+                                                (8192, 4096, 32, 1)])  # the benchmark's grid and band count
 def test_host_step_matches_copy_step_copy(nx, nz, nbands, flags):
     """evolve_host (copies overlapped with the step by row bands) against copy-in,
     evolve, copy-out: bit-identical states and host results for both direction
