@@ -56,12 +56,16 @@ __device__ __forceinline__ dw2 sub2(dw2 x, dw2 y) {
   return fast_two_sum2(s.h, f2add(s.l, f2sub(x.l, y.l)));
 }
 // x * y; ny_h = -y.h (callers multiplying by a constant pass it precomputed)
+// The leading product is formed only negated, pn = x.h * (-y.h) = -p exactly
+// (rounding is symmetric), so FastTwoSum(p, e) is written with pn:
+// s = RN(e - pn) = RN(p + e), err = e - RN(s + pn) = e - RN(s - p).
 __device__ __forceinline__ dw2 mul2n(dw2 x, dw2 y, float2 ny_h) {
-  const float2 p = f2mul(x.h, y.h);
-  float2 e = f2fma(x.h, y.h, f2mul(x.h, ny_h));  // exact product error: x.h*y.h - p
+  const float2 pn = f2mul(x.h, ny_h);
+  float2 e = f2fma(x.h, y.h, pn);  // exact product error: x.h*y.h - p
   e = f2fma(x.h, y.l, e);
   e = f2fma(x.l, y.h, e);
-  return fast_two_sum2(p, e);
+  const float2 sum = f2sub(e, pn);
+  return {sum, f2sub(e, f2add(sum, pn))};
 }
 __device__ __forceinline__ dw2 mul2(dw2 x, dw2 y) {
   return mul2n(x, y, f2mul(y.h, make_float2(-1.f, -1.f)));
