@@ -92,20 +92,27 @@ __device__ __forceinline__ dw pgm1(dw d) { return pow_m1(c_pow_g, kGamma, d); }
 // leading floats are combined with error-free transformations (exact), the
 // trailing floats and the rounding errors are summed in FP32 (error about
 // 2^-48 of the operands), and each result is renormalised once.
+// The products 7 a.h and 3 q.h are formed only negated (a7n = -a7 and q3n =
+// -q3 exactly, rounding being symmetric), and the error-free steps that take
+// them are written for the negated value, giving the same bits as the plain
+// form: TwoSum(a7n, b.h) = -TwoDiff(a7, b.h), TwoSum(p.h, q3n) =
+// TwoDiff(p.h, q3), and FastTwoSum(r.h, lo) = (RN(lo - rn.h), lo - RN(s + rn.h))
+// with rn = -r.
 __device__ __forceinline__ void interp2(dw2 s0, dw2 s1, dw2 s2, dw2 s3, dw2& A, dw2& D) {
   const float2 c7 = f2splat(7.0f), m7 = f2splat(-7.0f), c3 = f2splat(3.0f), m3 = f2splat(-3.0f);
   const dw2 a = two_sum2(s1.h, s2.h);
   const dw2 b = two_sum2(s0.h, s3.h);
-  const float2 a7 = f2mul(a.h, c7);
-  const float2 a7e = f2fma(a.h, c7, f2mul(a.h, m7));  // exact: 7 a.h - a7
-  const dw2 r = two_diff2(a7, b.h);
-  const float2 lo = f2add(f2sub(f2fma(c7, f2add(f2add(s1.l, s2.l), a.l), a7e), f2add(f2add(s0.l, s3.l), b.l)), r.l);
-  A = fast_two_sum2(r.h, lo);
+  const float2 a7n = f2mul(a.h, m7);                  // -RN(7 a.h)
+  const float2 a7e = f2fma(a.h, c7, a7n);             // exact: 7 a.h - RN(7 a.h)
+  const dw2 rn = two_sum2(a7n, b.h);                  // -(7 a.h - b.h) exactly
+  const float2 lo = f2sub(f2sub(f2fma(c7, f2add(f2add(s1.l, s2.l), a.l), a7e), f2add(f2add(s0.l, s3.l), b.l)), rn.l);
+  const float2 Ah = f2sub(lo, rn.h);
+  A = {Ah, f2sub(lo, f2add(Ah, rn.h))};
   const dw2 p = two_diff2(s3.h, s0.h);
   const dw2 q = two_diff2(s2.h, s1.h);
-  const float2 q3 = f2mul(q.h, c3);
-  const float2 q3e = f2fma(q.h, c3, f2mul(q.h, m3));
-  const dw2 t = two_diff2(p.h, q3);
+  const float2 q3n = f2mul(q.h, m3);                  // -RN(3 q.h)
+  const float2 q3e = f2fma(q.h, c3, q3n);
+  const dw2 t = two_sum2(p.h, q3n);
   const float2 lo2 =
       f2add(f2sub(f2add(f2sub(s3.l, s0.l), p.l), f2fma(c3, f2add(f2sub(s2.l, s1.l), q.l), q3e)), t.l);
   D = fast_two_sum2(t.h, lo2);
@@ -117,19 +124,20 @@ __device__ __forceinline__ dw2 acombo2(dw2 s0, dw2 s1, dw2 s2, dw2 s3) {
   const float2 c7 = f2splat(7.0f), m7 = f2splat(-7.0f);
   const dw2 a = two_sum2(s1.h, s2.h);
   const dw2 b = two_sum2(s0.h, s3.h);
-  const float2 a7 = f2mul(a.h, c7);
-  const float2 a7e = f2fma(a.h, c7, f2mul(a.h, m7));
-  const dw2 r = two_diff2(a7, b.h);
-  const float2 lo = f2add(f2sub(f2fma(c7, f2add(f2add(s1.l, s2.l), a.l), a7e), f2add(f2add(s0.l, s3.l), b.l)), r.l);
-  return fast_two_sum2(r.h, lo);
+  const float2 a7n = f2mul(a.h, m7);
+  const float2 a7e = f2fma(a.h, c7, a7n);
+  const dw2 rn = two_sum2(a7n, b.h);
+  const float2 lo = f2sub(f2sub(f2fma(c7, f2add(f2add(s1.l, s2.l), a.l), a7e), f2add(f2add(s0.l, s3.l), b.l)), rn.l);
+  const float2 Ah = f2sub(lo, rn.h);
+  return {Ah, f2sub(lo, f2add(Ah, rn.h))};
 }
 __device__ __forceinline__ dw2 dcombo2(dw2 s0, dw2 s1, dw2 s2, dw2 s3) {
   const float2 c3 = f2splat(3.0f), m3 = f2splat(-3.0f);
   const dw2 p = two_diff2(s3.h, s0.h);
   const dw2 q = two_diff2(s2.h, s1.h);
-  const float2 q3 = f2mul(q.h, c3);
-  const float2 q3e = f2fma(q.h, c3, f2mul(q.h, m3));
-  const dw2 t = two_diff2(p.h, q3);
+  const float2 q3n = f2mul(q.h, m3);
+  const float2 q3e = f2fma(q.h, c3, q3n);
+  const dw2 t = two_sum2(p.h, q3n);
   const float2 lo2 =
       f2add(f2sub(f2add(f2sub(s3.l, s0.l), p.l), f2fma(c3, f2add(f2sub(s2.l, s1.l), q.l), q3e)), t.l);
   return fast_two_sum2(t.h, lo2);
