@@ -165,7 +165,6 @@ def device_id_for_smi(torch, dev):
 
 # ---------------------------------------------------------------------------
 def make_params(args, dtype_name="fp64"):
-    from oracle import oracle as O  # noqa: F401  (params helper only; no oracle compute here)
     p = dict(nx=args.nx, nz=args.nz, xlen=2e4, zlen=1e4, hs=2, s=4, ic_type=args.ic, cfl=1.5, max_speed=450.0)
     p["dx"] = p["xlen"] / p["nx"]
     p["dz"] = p["zlen"] / p["nz"]

@@ -57,10 +57,12 @@ enum mw_f64_mode {
 #define MW_FLAG_INDEX64 2u    /* split form: use the 64-bit-index kernels even
                                  when 32-bit indices suffice (for testing; arrays
                                  of 2^31 or more values always use them) */
-#define MW_FLAG_CHECK_FINITE 4u /* mw_step_f64 / _f32 / _f64_host: after the steps, count the
-                                 non-finite interior values of the state and
-                                 return MW_ERR_NONFINITE if there are any
-                                 (synchronises the stream to read the count) */
+#define MW_FLAG_CHECK_FINITE 4u /* mw_step_f64 / _f32 / _f64_host / _f64_noalloc: after the
+                                 steps, count the non-finite interior values of
+                                 the state and return MW_ERR_NONFINITE if there
+                                 are any (synchronises the stream to read the
+                                 count, which is kept in the first 8 bytes of
+                                 the scratch array: nothing is allocated) */
 
 /* Background profile of the initial condition. */
 enum mw_background {
@@ -148,10 +150,13 @@ int mw_step_f32(int nx, int nz, double dx, double dz, double dt_full, double dt,
  * the library holds the array (4.3 MB) until the process exits.  The first
  * call on each device looks up the array's device address (once per device,
  * with that device current); make that first call before any stream capture.
+ * The address is kept for the life of the process, so do not reset a device
+ * (cudaDeviceReset) while this entry point is in use on it.
  * All calls share the one array and nothing in it needs to start at zero:
  * calls that overlap on the GPU (other streams, other host threads) race on
  * it, so issue them one after another.  Arguments and results are those of
- * mw_step_f64 without `scratch`; it never calls cudaMalloc or cudaFree.
+ * mw_step_f64 without `scratch`, MW_FLAG_CHECK_FINITE included (its counter
+ * lives in the same array); it never calls cudaMalloc or cudaFree.
  * ------------------------------------------------------------------------- */
 int mw_step_f64_noalloc(int nx, int nz, double dx, double dz, double dt_full, double dt, const double* hy_dens_cell,
                         const double* hy_dens_theta_cell, const double* hy_dens_int, const double* hy_dens_theta_int,

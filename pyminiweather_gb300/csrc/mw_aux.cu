@@ -629,8 +629,12 @@ extern "C" int mw_add_source_f64(int nx, int nz, const double* src_w, double* te
 // Non-finite values of the interior (failure detection after a step).
 namespace mw {
 namespace {
+// Adds the number of non-finite interior values to *count (when non-NULL);
+// the step entry points' check instead sets flag[0] = 1 and adds the count to
+// flag[1] (two 32-bit words: the decision does not depend on the count, which
+// may wrap for more than 2^32 values).
 template <typename T>
-__global__ void k_count_nonfinite(int nx, int nz, const T* s, unsigned long long* count) {
+__global__ void k_count_nonfinite(int nx, int nz, const T* s, unsigned long long* count, unsigned* flag) {
   const int pitch = nx + 2 * kHs;
   const long long plane = (long long)(nz + 2 * kHs) * pitch;
   const long long n = 4LL * nz * nx;
@@ -642,46 +646,54 @@ __global__ void k_count_nonfinite(int nx, int nz, const T* s, unsigned long long
     c += !isfinite(v);
   }
   for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
-  if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, (unsigned long long)c);
+  if ((threadIdx.x & 31) == 0 && c) {
+    if (count) atomicAdd(count, (unsigned long long)c);
+    if (flag) {
+      atomicOr(flag, 1u);
+      atomicAdd(flag + 1, c);
+    }
+  }
 }
 
 template <typename T>
-int count_nonfinite(int nx, int nz, const T* state, unsigned long long* count, cudaStream_t stream) {
+int count_nonfinite(int nx, int nz, const T* state, unsigned long long* count, unsigned* flag, cudaStream_t stream) {
   int st = check_grid(nx, nz);
   if (st) return st;
-  MW_REQUIRE(state && count, MW_ERR_INVALID_ARG, "NULL pointer argument");
+  MW_REQUIRE(state && (count || flag), MW_ERR_INVALID_ARG, "NULL pointer argument");
   const long long n = 4LL * nz * nx;
   const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 8);
-  k_count_nonfinite<T><<<(unsigned)blocks, 256, 0, stream>>>(nx, nz, state, count);
+  k_count_nonfinite<T><<<(unsigned)blocks, 256, 0, stream>>>(nx, nz, state, count, flag);
   return check_launch("non-finite count launch");
 }
 }  // namespace
 
-// The MW_FLAG_CHECK_FINITE tail of the step entry points (blocking).
+// The MW_FLAG_CHECK_FINITE tail of the step entry points (blocking).  It
+// allocates nothing: the two 32-bit words it counts into are lent by the
+// caller -- the first 8 bytes of the step's scratch array, whose contents
+// after a step are unspecified (4-byte alignment suffices).
 template <typename T>
-int check_finite_blocking(int nx, int nz, const T* state, cudaStream_t stream) {
-  unsigned long long* d = nullptr;
-  unsigned long long h = 0;
-  cudaError_t e = cudaMallocAsync((void**)&d, sizeof(*d), stream);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d, 0, sizeof(*d), stream);
+int check_finite_blocking(int nx, int nz, const T* state, void* counter8, cudaStream_t stream) {
+  MW_REQUIRE(counter8 && ((uintptr_t)counter8 % 4) == 0, MW_ERR_INVALID_ARG, "non-finite check: bad counter word");
+  unsigned* d = static_cast<unsigned*>(counter8);
+  unsigned h[2] = {0u, 0u};
+  cudaError_t e = cudaMemsetAsync(d, 0, 2 * sizeof(unsigned), stream);
   if (e != cudaSuccess) return fail(MW_ERR_CUDA, "non-finite check: %s", cudaGetErrorString(e));
-  int st = count_nonfinite(nx, nz, state, d, stream);
-  e = cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, stream);
-  cudaError_t e2 = cudaFreeAsync(d, stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  int st = count_nonfinite<T>(nx, nz, state, nullptr, d, stream);
   if (st) return st;
-  if (e != cudaSuccess || e2 != cudaSuccess) return fail(MW_ERR_CUDA, "non-finite check: %s", cudaGetErrorString(e));
-  if (h) return fail(MW_ERR_NONFINITE, "%llu non-finite interior values in the state after the step", h);
+  e = cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return fail(MW_ERR_CUDA, "non-finite check: %s", cudaGetErrorString(e));
+  if (h[0]) return fail(MW_ERR_NONFINITE, "%u non-finite interior values (modulo 2^32) in the state after the step", h[1]);
   return MW_OK;
 }
-template int check_finite_blocking<double>(int, int, const double*, cudaStream_t);
-template int check_finite_blocking<float>(int, int, const float*, cudaStream_t);
+template int check_finite_blocking<double>(int, int, const double*, void*, cudaStream_t);
+template int check_finite_blocking<float>(int, int, const float*, void*, cudaStream_t);
 }  // namespace mw
 
 extern "C" int mw_count_nonfinite_f64(int nx, int nz, const double* state, unsigned long long* count, void* stream) {
-  return mw::count_nonfinite(nx, nz, state, count, (cudaStream_t)stream);
+  return mw::count_nonfinite(nx, nz, state, count, nullptr, (cudaStream_t)stream);
 }
 extern "C" int mw_count_nonfinite_f32(int nx, int nz, const float* state, unsigned long long* count, void* stream) {
-  return mw::count_nonfinite(nx, nz, state, count, (cudaStream_t)stream);
+  return mw::count_nonfinite(nx, nz, state, count, nullptr, (cudaStream_t)stream);
 }
 

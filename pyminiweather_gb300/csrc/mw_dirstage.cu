@@ -606,9 +606,10 @@ static int launch_stage(int nx, int nz, double dx, double dz, double dt_full, co
   return check_launch(direction == MW_DIR_X ? "x direction-stage launch" : "z direction-stage launch");
 }
 
-// MW_FLAG_CHECK_FINITE: count non-finite interior values, blocking (mw_aux.cu).
+// MW_FLAG_CHECK_FINITE: count non-finite interior values, blocking (mw_aux.cu);
+// counter8 is 8 bytes of the step's scratch array (nothing is allocated).
 template <typename T>
-int check_finite_blocking(int nx, int nz, const T* state, cudaStream_t stream);
+int check_finite_blocking(int nx, int nz, const T* state, void* counter8, cudaStream_t stream);
 
 // Split-arithmetic launches live in mw_split_stage.cu.
 int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
@@ -709,7 +710,7 @@ extern "C" int mw_step_f64(int nx, int nz, double dx, double dz, double dt_full,
                            return stage_f64(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, src_w, init, forcing,
                                             out, dts, dir, f64_mode, flags, s, split_step_fmt(k));
                          });
-  if (st == MW_OK && nsteps > 0 && (flags & MW_FLAG_CHECK_FINITE)) st = check_finite_blocking(nx, nz, (const double*)state, s);
+  if (st == MW_OK && nsteps > 0 && (flags & MW_FLAG_CHECK_FINITE)) st = check_finite_blocking(nx, nz, (const double*)state, scratch, s);
   return st;
 }
 
@@ -728,7 +729,7 @@ extern "C" int mw_step_f32(int nx, int nz, double dx, double dz, double dt_full,
                           return launch_stage<float, MODE_F32>(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi,
                                                                src_w, init, forcing, out, dts, dir, flags, s);
                         });
-  if (st == MW_OK && nsteps > 0 && (flags & MW_FLAG_CHECK_FINITE)) st = check_finite_blocking(nx, nz, (const float*)state, s);
+  if (st == MW_OK && nsteps > 0 && (flags & MW_FLAG_CHECK_FINITE)) st = check_finite_blocking(nx, nz, (const float*)state, scratch, s);
   return st;
 }
 
@@ -756,7 +757,9 @@ double* g_noalloc_addr[kNoAllocMaxDevices] = {};
 
 // Device address of g_noalloc_scratch on the current device.  The host-side
 // name is only a stand-in for the symbol, so the address is asked of the
-// runtime once per device, with that device current.
+// runtime once per device, with that device current, and kept for the life of
+// the process: a device must not be reset (cudaDeviceReset) while this entry
+// point is in use, since the array is loaded again at a new address.
 int noalloc_scratch(double** out) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
@@ -800,11 +803,14 @@ extern "C" int mw_step_f64_noalloc(int nx, int nz, double dx, double dz, double 
   MW_REQUIRE(f64_mode == MW_F64_NATIVE || f64_mode == MW_F64_SPLIT, MW_ERR_INVALID_ARG, "unknown f64_mode %d",
              f64_mode);
   cudaStream_t s = (cudaStream_t)stream;
-  return run_steps<double>(dt, state, state_tmp, scratch, nsteps, reverse,
-                           [&](const double* init, double* forcing, double* out, double dts, int dir, int k) {
-                             return stage_f64(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, src_w, init,
-                                              forcing, out, dts, dir, f64_mode, flags, s, split_step_fmt(k));
-                           });
+  st = run_steps<double>(dt, state, state_tmp, scratch, nsteps, reverse,
+                         [&](const double* init, double* forcing, double* out, double dts, int dir, int k) {
+                           return stage_f64(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, src_w, init,
+                                            forcing, out, dts, dir, f64_mode, flags, s, split_step_fmt(k));
+                         });
+  // the finite check counts into the first 8 bytes of the built-in array (no allocation)
+  if (st == MW_OK && nsteps > 0 && (flags & MW_FLAG_CHECK_FINITE)) st = check_finite_blocking(nx, nz, (const double*)state, scratch, s);
+  return st;
 }
 
 // ---------------------------------------------------------------------------

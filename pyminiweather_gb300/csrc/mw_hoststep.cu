@@ -94,7 +94,7 @@ using namespace mw;
 
 namespace mw {
 template <typename T>
-int check_finite_blocking(int nx, int nz, const T* state, cudaStream_t stream);  // mw_aux.cu
+int check_finite_blocking(int nx, int nz, const T* state, void* counter8, cudaStream_t stream);  // mw_aux.cu
 }
 
 extern "C" int mw_step_f64(int nx, int nz, double dx, double dz, double dt_full, double dt, const double* hyc,
@@ -213,6 +213,6 @@ extern "C" int mw_step_f64_host(int nx, int nz, double dx, double dz, double dt_
   if (st) return st;
   if (e != cudaSuccess) return fail(MW_ERR_CUDA, "join: %s", cudaGetErrorString(e));
   *reverse = *reverse ? 0 : 1;
-  if (flags & MW_FLAG_CHECK_FINITE) return check_finite_blocking(nx, nz, (const double*)state, s);
+  if (flags & MW_FLAG_CHECK_FINITE) return check_finite_blocking(nx, nz, (const double*)state, scratch, s);
   return MW_OK;
 }

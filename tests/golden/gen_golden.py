@@ -2,7 +2,7 @@
 
 Run from the repository root, in a container that holds the reference checkout:
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/gen_golden.py --ref /root/reference
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/gen_golden.py --ref <checkout of the reference>
 
 The reference (shriram-jagan/pyminiweather) is imported with its NumPy/SciPy
 backend.  Its module-global direction flag (pyminiweather/solve/step.py:18) is

@@ -66,3 +66,27 @@ def test_noalloc_rejects_grids_beyond_its_array():
     assert st == 6  # MW_ERR_WORKSPACE
     assert b"512 x 256" in L.mw_last_error()
     assert rv.value == 0
+
+
+@pytest.mark.parametrize("mode", ["split", "native"])
+def test_noalloc_check_finite_flag(mode):
+    """MW_FLAG_CHECK_FINITE is honoured without allocating: a NaN planted in the
+    state on the host makes the call return MW_ERR_NONFINITE (7), a clean state
+    MW_OK, as mw_step_f64 does."""
+    p = make_params(64, 32, "thermal")
+    f = initialize_fields(p)
+    init(f, p)
+    L = _native.load()
+    m = _native.F64_MODES[mode]
+    flags = _native.MW_FLAG_WRITE_HALO | _native.MW_FLAG_CHECK_FINITE
+    stream = _native.stream_handle()
+    rv = ctypes.c_int(0)
+    st = L.mw_step_f64_noalloc(*_args(p, f), _native.ptr(f.state), _native.ptr(f.state_tmp), 1, ctypes.byref(rv), m,
+                               flags, stream)
+    assert st == 0, L.mw_last_error()
+    f.state[3, 10, 20] = float("nan")  # planted on the host side of the API, not by a kernel fault
+    st = L.mw_step_f64_noalloc(*_args(p, f), _native.ptr(f.state), _native.ptr(f.state_tmp), 1, ctypes.byref(rv), m,
+                               flags, stream)
+    torch.cuda.synchronize()
+    assert st == 7, (st, L.mw_last_error())
+    assert b"non-finite" in L.mw_last_error()
