@@ -55,7 +55,7 @@ def parse_args():
     ap.add_argument("--nx", type=int, default=8192)
     ap.add_argument("--nz", type=int, default=4096)
     ap.add_argument("--ic", default="collision")
-    ap.add_argument("--mode", default="split", choices=["split", "native"])
+    ap.add_argument("--mode", default="fp64", choices=["fp64", "split", "native"])
     ap.add_argument("--no-extras", action="store_true", help="skip the FP32 / native-FP64 / e2e / CPU legs")
     ap.add_argument("--cpu-steps", type=int, default=2, help="time steps in the CPU-baseline sample")
     return ap.parse_args()
@@ -261,6 +261,8 @@ def kernel_names(fp64, mode):
         return {0: "k_stage_x<float,F32>", 1: "k_stage_z<float,F32>"}
     if mode == "split":
         return {0: "k_stage_x_split", 1: "k_stage_z_split"}
+    if mode == "fp64":
+        return {0: "k_stage_x_ieee", 1: "k_stage_z_ieee"}
     return {0: "k_stage_x<double,NATIVE64>", 1: "k_stage_z<double,NATIVE64>"}
 
 

@@ -46,9 +46,15 @@ enum mw_direction { MW_DIR_X = 0, MW_DIR_Z = 1 }; /* ics/directions.py:4-6 */
 
 /* Arithmetic of the FP64-storage direction-stage kernels. */
 enum mw_f64_mode {
-  MW_F64_NATIVE = 0, /* every operation on the FP64 pipe, the reference's formulas */
-  MW_F64_SPLIT = 1   /* GB300 form: FP64 loads/stores and update, interior
-                        arithmetic in pairs of FP32 (about 2^-46 relative) */
+  MW_F64_NATIVE = 0, /* IEEE FP64, the reference's formulas as written (a pow
+                        and three divides per interface) */
+  MW_F64_SPLIT = 1,  /* FP64 loads/stores and update, interior arithmetic in
+                        pairs of FP32: about 47 significant bits, FP32 exponent
+                        range -- NOT IEEE FP64 arithmetic */
+  MW_F64_IEEE = 2    /* IEEE FP64 arithmetic throughout with the fewest FP64
+                        operations: 1/rho by a Newton step, the pressure
+                        perturbation by its binomial series, values scaled by
+                        12 (no divisions per cell) */
 };
 
 /* Flags of the direction-stage and step entry points. */
@@ -122,9 +128,10 @@ int mw_step_f64(int nx, int nz, double dx, double dz, double dt_full, double dt,
  * reference, whose arrays are host arrays to begin with): h_in (4, nz+4, nx+4)
  * is copied into state, the step runs as mw_step_f64 with nsteps = 1, and the
  * resulting state is copied into h_out (which may equal h_in).  Enqueued on
- * `stream`; h_out is complete once the stream is.  In the split form the
- * copies overlap the computation by nbands row bands (at most 64 and at most
- * nz / 16); the results are those of copy-in, mw_step_f64, copy-out bit for bit.
+ * `stream`; h_out is complete once the stream is.  In the IEEE-FP64 and split
+ * forms the copies overlap the computation by nbands row bands (at most 64 and
+ * at most nz / 16); the results are those of copy-in, mw_step_f64, copy-out
+ * bit for bit.
  * h_in / h_out should be page-locked for the copies to run asynchronously.
  * Calls on one device share internal copy streams and are serialised. */
 int mw_step_f64_host(int nx, int nz, double dx, double dz, double dt_full, double dt, const double* hy_dens_cell,
@@ -221,9 +228,9 @@ int mw_ensemble_step_f32(void* plan_device, const mw_ens_plan_info* info, const 
  * (a halo value's adjoint returns to the cell it was copied or scaled from),
  * the hyperviscosity and the gravity term.  Arrays are (4, nz+4, nx+4) FP64;
  * a base may be g_dst itself (accumulation); g_dst must not overlap g_out or
- * forcing.  f64_mode: MW_F64_NATIVE (FP64 arithmetic, two kernels) or
- * MW_F64_SPLIT (double-FP32 interior arithmetic as the split forward, one
- * kernel after a small background-table kernel).
+ * forcing.  f64_mode: MW_F64_NATIVE or MW_F64_IEEE (FP64 arithmetic, two
+ * kernels) or MW_F64_SPLIT (double-FP32 interior arithmetic as the split
+ * forward, one kernel after a small background-table kernel).
  * workspace: mw_dirstage_vjp_workspace_bytes.
  * ------------------------------------------------------------------------- */
 size_t mw_dirstage_vjp_workspace_bytes(int nx, int nz);

@@ -53,8 +53,9 @@ def get_parser():
                    help="Output file of the state (default: PyMiniWeatherData.txt)")
     p.add_argument("--app-log-file", action="store", type=Path, default=None, metavar="FILE",
                    help="Write messages from the application to a file")
-    p.add_argument("--f64-mode", type=str, default="split", choices=["split", "native"], dest="f64_mode",
-                   help="FP64 arithmetic form: split (double-FP32 interior, default) or native")
+    p.add_argument("--f64-mode", type=str, default="fp64", choices=["fp64", "native", "split"], dest="f64_mode",
+                   help="FP64 arithmetic form: fp64 (IEEE FP64, fewest operations; default), native (IEEE FP64, "
+                        "the reference's formulas) or split (double-FP32 interior, not IEEE FP64)")
     p.add_argument("--fp32", action="store_true", default=False, dest="fp32",
                    help="FP32 perturbation fields (the precision form)")
     p.add_argument("--checkpoint-file", type=str, default=None, dest="checkpoint_file",

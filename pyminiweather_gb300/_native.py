@@ -19,14 +19,14 @@ _lib = None
 
 MW_OK = 0
 MW_DIR_X, MW_DIR_Z = 0, 1
-MW_F64_NATIVE, MW_F64_SPLIT = 0, 1
+MW_F64_NATIVE, MW_F64_SPLIT, MW_F64_IEEE = 0, 1, 2
 MW_FLAG_WRITE_HALO = 1
 MW_FLAG_INDEX64 = 2
 MW_FLAG_CHECK_FINITE = 4
 MW_BG_CONST_THETA, MW_BG_BVFREQ = 0, 1
 MW_MAX_BUBBLES = 8
 
-F64_MODES = {"native": MW_F64_NATIVE, "split": MW_F64_SPLIT}
+F64_MODES = {"native": MW_F64_NATIVE, "split": MW_F64_SPLIT, "fp64": MW_F64_IEEE}
 
 _i, _u, _d, _P, _sz = ctypes.c_int, ctypes.c_uint, ctypes.c_double, ctypes.c_void_p, ctypes.c_size_t
 

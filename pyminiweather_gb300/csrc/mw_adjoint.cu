@@ -248,8 +248,8 @@ static int vjp_stage(int nx, int nz, double dx, double dz, double dt_full, const
   MW_REQUIRE((!g_base_a || g_base_a == g_dst || !ranges_overlap(g_dst, bytes, g_base_a, bytes)) &&
                  (!g_base_b || g_base_b == g_dst || !ranges_overlap(g_dst, bytes, g_base_b, bytes)),
              MW_ERR_ALIAS, "a base array must equal g_dst or not overlap it");
-  MW_REQUIRE(f64_mode == MW_F64_NATIVE || f64_mode == MW_F64_SPLIT, MW_ERR_INVALID_ARG,
-             "f64_mode must be MW_F64_NATIVE or MW_F64_SPLIT");
+  MW_REQUIRE(valid_f64_mode(f64_mode), MW_ERR_INVALID_ARG, "f64_mode must be MW_F64_NATIVE, _SPLIT or _IEEE");
+  // MW_F64_IEEE (the same step as MW_F64_NATIVE up to rounding) takes the FP64 kernels below.
   const size_t need = mw_dirstage_vjp_workspace_bytes(nx, nz);
   MW_REQUIRE(workspace_bytes >= need, MW_ERR_WORKSPACE, "vjp workspace needs %zu bytes, got %zu", need,
              workspace_bytes);

@@ -103,6 +103,8 @@ inline bool ranges_overlap(const void* a, size_t abytes, const void* b, size_t b
 
 int check_grid(int nx, int nz);
 
+inline bool valid_f64_mode(int m) { return m == MW_F64_NATIVE || m == MW_F64_SPLIT || m == MW_F64_IEEE; }
+
 // Rows per z CTA for a single-grid launch: the largest tile up to max_rows
 // that still gives about two CTAs per SM (152 SMs), at least 8 rows.
 inline int z_tile_rows(int nx, int nz, int cols_per_cta, int max_rows) {

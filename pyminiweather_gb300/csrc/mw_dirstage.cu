@@ -617,6 +617,12 @@ int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, con
                        const double* init, double* forcing, double* out, double dt_stage, int direction,
                        unsigned flags, int r0, int r1, int fmt, cudaStream_t stream);
 
+// IEEE-FP64 launches live in mw_fp64_stage.cu.
+int launch_stage_ieee(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
+                      const double* hyi, const double* hyti, const double* hypi, const double* srcw,
+                      const double* init, double* forcing, double* out, double dt_stage, int direction,
+                      unsigned flags, int r0, int r1, cudaStream_t stream);
+
 // Storage format of the split form's RK3 stage k (0, 1, 2) inside a whole
 // step: the first stage's result s1 is read only by the second stage of the
 // same direction, so it stays in the scratch array as double-FP32 pairs
@@ -630,6 +636,9 @@ static int stage_f64(int nx, int nz, double dx, double dz, double dt_full, const
   if (mode == MW_F64_SPLIT)
     return launch_stage_split(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, srcw, init, forcing, out,
                               dt_stage, direction, flags, 0, nz, fmt, stream);
+  if (mode == MW_F64_IEEE)
+    return launch_stage_ieee(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, srcw, init, forcing, out, dt_stage,
+                             direction, flags, 0, nz, stream);
   return launch_stage<double, MODE_NATIVE64>(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, srcw, init, forcing,
                                              out, dt_stage, direction, flags, stream);
 }
@@ -674,7 +683,7 @@ extern "C" int mw_dirstage_f64(int nx, int nz, double dx, double dz, double dt_f
                                double dt_stage, int direction, int f64_mode, unsigned flags, void* stream) {
   int st = validate_stage<double>(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, init, forcing, out, direction);
   if (st) return st;
-  MW_REQUIRE(f64_mode == MW_F64_NATIVE || f64_mode == MW_F64_SPLIT, MW_ERR_INVALID_ARG, "unknown f64_mode %d",
+  MW_REQUIRE(valid_f64_mode(f64_mode), MW_ERR_INVALID_ARG, "unknown f64_mode %d",
              f64_mode);
   MW_REQUIRE(std::isfinite(dt_stage), MW_ERR_INVALID_ARG, "dt_stage must be finite");
   return stage_f64(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, src_w, init, forcing, out, dt_stage,
@@ -702,7 +711,7 @@ extern "C" int mw_step_f64(int nx, int nz, double dx, double dz, double dt_full,
   if (st) return st;
   MW_REQUIRE(finite_pos(dt), MW_ERR_INVALID_ARG, "dt must be finite and positive");
   if (st) return st;
-  MW_REQUIRE(f64_mode == MW_F64_NATIVE || f64_mode == MW_F64_SPLIT, MW_ERR_INVALID_ARG, "unknown f64_mode %d",
+  MW_REQUIRE(valid_f64_mode(f64_mode), MW_ERR_INVALID_ARG, "unknown f64_mode %d",
              f64_mode);
   cudaStream_t s = (cudaStream_t)stream;
   st = run_steps<double>(dt, state, state_tmp, scratch, nsteps, reverse,
@@ -800,7 +809,7 @@ extern "C" int mw_step_f64_noalloc(int nx, int nz, double dx, double dz, double 
                              reverse);
   if (st) return st;
   MW_REQUIRE(finite_pos(dt), MW_ERR_INVALID_ARG, "dt must be finite and positive");
-  MW_REQUIRE(f64_mode == MW_F64_NATIVE || f64_mode == MW_F64_SPLIT, MW_ERR_INVALID_ARG, "unknown f64_mode %d",
+  MW_REQUIRE(valid_f64_mode(f64_mode), MW_ERR_INVALID_ARG, "unknown f64_mode %d",
              f64_mode);
   cudaStream_t s = (cudaStream_t)stream;
   st = run_steps<double>(dt, state, state_tmp, scratch, nsteps, reverse,
@@ -825,7 +834,7 @@ extern "C" int mw_step_record_f64(int nx, int nz, double dx, double dz, double d
                                   MW_DIR_X);
   if (st) return st;
   MW_REQUIRE(finite_pos(dt), MW_ERR_INVALID_ARG, "dt must be finite and positive");
-  MW_REQUIRE(f64_mode == MW_F64_NATIVE || f64_mode == MW_F64_SPLIT, MW_ERR_INVALID_ARG, "unknown f64_mode %d",
+  MW_REQUIRE(valid_f64_mode(f64_mode), MW_ERR_INVALID_ARG, "unknown f64_mode %d",
              f64_mode);
   MW_REQUIRE(!ranges_overlap(stages, 6 * n * sizeof(double), state_out, n * sizeof(double)) &&
                  !ranges_overlap(stages, 6 * n * sizeof(double), state_in, n * sizeof(double)),

@@ -1,0 +1,437 @@
+// mw_fp64_stage.cu -- direction-stage kernels in IEEE FP64 arithmetic with
+// the fewest FP64 operations (f64_mode MW_F64_IEEE): the FP64 form of
+// discrete_step (pyminiweather/solve/step.py:21-82).
+//
+// Every floating-point operation on state values is an FP64 add, multiply or
+// FMA (no FP32 arithmetic on them, no double-FP32 pairs).  On GB300 the FP64
+// pipe retires about 1.9 operations per clock per SM, so one FP64
+// warp-instruction occupies it for ~17 SM clocks, in which the SM can issue
+// ~67 other warp-instructions: the kernels are bound by their FP64 operation
+// count, and integer work (conversions, index arithmetic, table look-ups) is
+// nearly free.  Against the reference's formulas (one pow, three divides and
+// ~50 operations per interface, interpolate.py:82-186) each interface costs
+// ~39 + n FP64 operations and each cell update 8:
+//   - quantities are carried scaled by 12, so the 4-point interpolation is
+//     A = 7 (s1 + s2) - (s0 + s3) and needs no division; the third
+//     difference is D = (s3 - s0) + 3 (s1 - s2): 6 operations per variable;
+//   - one reciprocal per interface: an FP32 hardware estimate of 1/rho
+//     (operand and result converted by integer operations) refined by one
+//     cubic Newton step in FP64, r = r0 (1 + e + e^2), e = 1 - rho r0
+//     (relative error e^3 <= 2^-66 before rounding): 3 FP64 operations;
+//   - pressure enters as the perturbation P_row ((1 + delta)^gamma - 1),
+//     delta = (rho theta)' / (rho theta)_bg, P_row = C0 (rho theta)_bg^gamma:
+//     exactly the reference's p - hy_pressure_int in z (hy_pressure_int is
+//     C0 hy_dens_theta_int^gamma, ics/initial.py:105); in x the row constant
+//     cancels in the flux difference.  (1 + delta)^gamma - 1 is its binomial
+//     series summed by Horner's rule to the degree n that the warp's largest
+//     |delta| needs for a truncation below 2^-54 relative (n = 2..4 in smooth
+//     regions, 15 for |delta| < 1/8), and expm1(gamma log1p(delta)) beyond;
+//   - the stage update is out = init + c (F(i) - F(i+1)), c = dt / (12 d):
+//     2 operations per value.
+//
+// x pass: a CTA walks a run of 255-cell chunks of one row; thread t evaluates
+// the flux at interface x0+t into shared memory, and after one barrier
+// updates cell x0+t.  z pass: one thread per column marching a tile of rows
+// with a rolling 4-row window, so each interface flux is evaluated once.
+// Halo cells are never read: the periodic-x and wall-z rules of ics/bcs.py
+// are applied to the indices and values as they are loaded.  Every global
+// access goes through MW_AT (bounds-checked in the debug library).
+#include <algorithm>
+
+#include "mw_common.cuh"
+#include "mw_ensemble.cuh"
+
+namespace mw {
+namespace ieee {
+
+constexpr int kXT = 256;            // interfaces per x chunk
+constexpr int kXC = kXT - 1;        // cells per x chunk
+constexpr int kXBlocksPerRow = 4;   // x CTAs per row
+constexpr int kZT = 128;            // columns per z CTA
+constexpr int kZTileMax = 64;       // rows per z CTA
+
+// ---- constant tables ------------------------------------------------------
+constexpr double binom(double e, int n) {  // C(e, n)
+  double c = 1.0;
+  for (int k = 0; k < n; ++k) c = c * (e - k) / (k + 1);
+  return c;
+}
+constexpr double cabs(double v) { return v < 0 ? -v : v; }
+
+constexpr int kMaxDeg = 15;
+struct Coef {
+  double c[kMaxDeg + 1];
+};
+constexpr Coef make_coef() {
+  Coef t{};
+  for (int n = 0; n <= kMaxDeg; ++n) t.c[n] = binom(kGamma, n);
+  return t;
+}
+// deg[s]: the Horner degree for |delta| < 2^-s (s >= 3): the smallest n with
+// |C(gamma, n+1) / C(gamma, 1)| 2^(-s n) <= 2^-54.
+struct Deg {
+  unsigned char n[65];
+};
+constexpr Deg make_deg() {
+  Deg t{};
+  for (int s = 0; s <= 64; ++s) {
+    int n = kMaxDeg;
+    if (s >= 3) {
+      for (n = 1; n < kMaxDeg; ++n) {
+        double b = cabs(binom(kGamma, n + 1) / binom(kGamma, 1));
+        for (int j = 0; j < s * n && b > 0.0; ++j) b *= 0.5;
+        if (b <= 5.551115123125783e-17) break;  // 2^-54
+      }
+    }
+    t.n[s] = (unsigned char)n;
+  }
+  return t;
+}
+__constant__ Coef c_coef = make_coef();
+__constant__ Deg c_deg = make_deg();
+
+// ---- FP64 building blocks --------------------------------------------------
+// 1/y: FP32 estimate refined by one cubic Newton step (3 FP64 operations).
+// |y| outside [2^-125, 2^126) (and Inf, NaN, 0) takes the FP64 division.
+__device__ __forceinline__ double rcp(double y) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(y);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const unsigned ex = (hi >> 20) & 0x7ffu;
+  // float with y's sign, rebiased exponent and leading 23 significand bits
+  const unsigned fb = ((__funnelshift_l(lo, hi, 3) + 0x40000000u) & 0x7fffffffu) | (hi & 0x80000000u);
+  float rf;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(__uint_as_float(fb)));
+  const unsigned rb = __float_as_uint(rf);
+  const unsigned rhi = (((rb >> 3) & 0x0fffffffu) + (896u << 20)) | (rb & 0x80000000u);
+  const double r0 = __longlong_as_double((long long)(((unsigned long long)rhi << 32) | (rb << 29)));
+  const double e = fma(-y, r0, 1.0);
+  const double t = fma(e, e, e);
+  double r = fma(r0, t, r0);
+  if (ex - (1023u - 125u) > 250u) r = 1.0 / y;
+  return r;
+}
+
+// (1 + d)^gamma - 1 for the lanes in `mask`, which call it together: the
+// binomial series to the degree the largest |d| among them needs (a
+// warp-uniform loop), or expm1(gamma log1p(d)) for |d| >= 1/8, Inf and NaN.
+__device__ __forceinline__ double pgm1(double d, unsigned mask) {
+  const unsigned ex = ((unsigned)((unsigned long long)__double_as_longlong(d) >> 52)) & 0x7ffu;
+  const bool big = ex >= 1020u;  // |d| >= 2^-3
+  const unsigned exm = __reduce_max_sync(mask, big ? 0u : ex);
+  const int s = min(1022 - (int)exm, 64);  // |d| < 2^-s for every series lane
+  const int n = c_deg.n[s];
+  double g = c_coef.c[n];
+  for (int k = n - 1; k >= 1; --k) g = fma(g, d, c_coef.c[k]);
+  double f = d * g;
+  if (big) f = expm1(kGamma * log1p(d));
+  return f;
+}
+
+// 12 x the 4-point interpolation and the third difference of one variable
+// (the stencils of interpolate.py:33-43 and 69-79).
+__device__ __forceinline__ void interp(double s0, double s1, double s2, double s3, double& A, double& D) {
+  A = fma(7.0, s1 + s2, -(s0 + s3));
+  D = fma(3.0, s1 - s2, s3 - s0);
+}
+
+// Row constants, scaled by 12 like the interpolated values.
+struct RowD {
+  double R12;    // 12 background rho
+  double RT12;   // 12 background rho theta
+  double IRT12;  // 1 / (12 background rho theta)
+  double P12;    // 12 background pressure C0 (rho theta)^gamma
+};
+__device__ __forceinline__ RowD row_consts(double r, double rt, double P) {
+  return {12.0 * r, 12.0 * rt, 1.0 / (12.0 * rt), 12.0 * P};
+}
+
+// x flux times 12 (interpolate.py:82-129): with u = (rho u)' / rho,
+// F = ((rho u)', u (rho u)' + p', u (rho w)', u (rho theta)) - hv d3, HV = -12 hv.
+__device__ __forceinline__ void flux_x(const double s[4][4], const RowD& r, double HV, unsigned mask, double F[4]) {
+  double A[4], D[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) interp(s[q][0], s[q][1], s[q][2], s[q][3], A[q], D[q]);
+  const double ri = rcp(A[DENS] + r.R12);
+  const double u = A[UMOM] * ri;
+  const double f = pgm1(A[RHOT] * r.IRT12, mask);
+  F[0] = fma(HV, D[DENS], A[UMOM]);
+  F[1] = fma(A[UMOM], u, fma(r.P12, f, HV * D[UMOM]));
+  F[2] = fma(u, A[WMOM], HV * D[WMOM]);
+  F[3] = fma(u, A[RHOT] + r.RT12, HV * D[RHOT]);
+}
+
+// z flux times 12 (interpolate.py:132-186); w and d3[DENS] vanish at the walls.
+__device__ __forceinline__ void flux_z(const double s[4][4], const RowD& r, double HV, bool wall, unsigned mask,
+                                       double F[4]) {
+  double A[4], D[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) interp(s[q][0], s[q][1], s[q][2], s[q][3], A[q], D[q]);
+  double AW = A[WMOM];
+  if (wall) {
+    AW = 0.0;
+    D[DENS] = 0.0;
+  }
+  const double ri = rcp(A[DENS] + r.R12);
+  const double w = AW * ri;
+  const double f = pgm1(A[RHOT] * r.IRT12, mask);
+  F[0] = fma(HV, D[DENS], AW);
+  F[1] = fma(w, A[UMOM], HV * D[UMOM]);
+  F[2] = fma(AW, w, fma(r.P12, f, HV * D[WMOM]));
+  F[3] = fma(w, A[RHOT] + r.RT12, HV * D[RHOT]);
+}
+
+// ---- arguments -------------------------------------------------------------
+struct Args {
+  int nx, nz, pitch;
+  long long plane;
+  const double* hyc;
+  const double* hytc;
+  const double* hyi;
+  const double* hyti;
+  const double* hypi;
+  const double* srcw;
+  const double* init;
+  double* forcing;
+  double* out;
+  unsigned flags;
+  double HV;    // -12 hv, hv = -hv_beta d / (16 dt_full) (interpolate.py:101,149)
+  double c;     // dt_stage / (12 d)
+  double dt;    // dt_stage (source terms)
+  double gdt;   // -dt_stage grav (z)
+  int chunks_per_block;
+  int z_tile;
+  int r0, r1;   // output rows [r0, r1)
+};
+
+__device__ __forceinline__ int wrap_x(int j, int nx) { return j < 0 ? j + nx : (j >= nx ? j - nx : j); }
+
+#define MW_F(a, off) MW_AT((a).forcing, (off), 4 * (a).plane)
+
+// Forcing value of variable q at interior row k in [-2, nz+1] of the
+// halo-indexed column col, with the wall rule of ics/bcs.py:92-148 in the halo rows.
+__device__ __forceinline__ double zval(const Args& a, int q, int k, int col) {
+  if (k >= 0 && k < a.nz) return MW_F(a, q * a.plane + (long long)(k + kHs) * a.pitch + col);
+  if (q == WMOM) return 0.0;
+  const int src = k < 0 ? kHs : a.nz + kHs - 1;
+  const double s = MW_F(a, q * a.plane + (long long)src * a.pitch + col);
+  if (q == UMOM) return s / MW_AT(a.hyc, src, a.nz + 2 * kHs) * MW_AT(a.hyc, k + kHs, a.nz + 2 * kHs);
+  return s;
+}
+
+// Wall halo rows of one column of the forcing array: -2, -1 (bottom) from
+// row 0, nz and nz+1 (top) from row nz-1.
+__device__ __forceinline__ void write_z_halo_column(const Args& a, int col, bool bottom, bool top) {
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    if (!(h == 0 ? bottom : top)) continue;
+    const int r0 = h == 0 ? -2 : a.nz;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const double v0 = zval(a, q, r0, col), v1 = zval(a, q, r0 + 1, col);
+      MW_F(a, q * a.plane + (long long)(r0 + kHs) * a.pitch + col) = v0;
+      MW_F(a, q * a.plane + (long long)(r0 + 1 + kHs) * a.pitch + col) = v1;
+    }
+  }
+}
+
+// ---- x ---------------------------------------------------------------------
+struct SmemX {
+  double sF[4][kXT];
+  RowD row;
+};
+
+// Row k, chunks [cbeg, cend) of kXC cells; every thread of the CTA calls it.
+__device__ __forceinline__ void x_row(const Args& a, int k, int cbeg, int cend, bool halo, SmemX& sm) {
+  const int t = threadIdx.x;
+  const long long row = (long long)(k + kHs) * a.pitch;
+  const int n4 = a.nz + 2 * kHs;
+  if (t == 0) {
+    const double rt = MW_AT(a.hytc, k + kHs, n4);
+    sm.row = row_consts(MW_AT(a.hyc, k + kHs, n4), rt, kC0 * pow(rt, kGamma));
+  }
+  if (halo && t < 4) {  // columns 0, 1 <- nx, nx+1; nx+2, nx+3 <- 2, 3 (ics/bcs.py:35-39)
+    const int dst = t < 2 ? t : a.nx + t, src = t < 2 ? a.nx + t : t;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) MW_F(a, q * a.plane + row + dst) = MW_F(a, q * a.plane + row + src);
+  }
+  __syncthreads();
+  const RowD r = sm.row;
+  for (int chunk = cbeg; chunk < cend; ++chunk) {
+    const int i = chunk * kXC + t;  // interface i, between cells i-1 and i
+    const bool upd = t < kXC && i < a.nx;
+    const long long o = row + i + kHs;
+    double iv[4];
+    if (upd) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) iv[q] = MW_AT(a.init, q * a.plane + o, 4 * a.plane);
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, i <= a.nx);
+    if (i <= a.nx) {
+      double s[4][4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const long long col = wrap_x(i - 2 + j, a.nx) + kHs;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) s[q][j] = __ldg(&MW_F(a, q * a.plane + row + col));
+      }
+      double F[4];
+      flux_x(s, r, a.HV, mask, F);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) sm.sF[q][t] = F[q];
+    }
+    __syncthreads();
+    if (upd) {
+      double v[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) v[q] = fma(a.c, sm.sF[q][t] - sm.sF[q][t + 1], iv[q]);
+      if (a.srcw) v[WMOM] = fma(a.dt, MW_AT(a.srcw, (long long)k * a.nx + i, (long long)a.nx * a.nz), v[WMOM]);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) MW_AT(a.out, q * a.plane + o, 4 * a.plane) = v[q];
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kXT) k_stage_x_ieee(Args a) {
+  __shared__ SmemX sm;
+  const int nchunks = (a.nx + kXC - 1) / kXC;
+  const int cbeg = blockIdx.x * a.chunks_per_block;
+  const int cend = min(cbeg + a.chunks_per_block, nchunks);
+  const bool halo = (a.flags & MW_FLAG_WRITE_HALO) && blockIdx.x == 0;
+  for (int k = a.r0 + blockIdx.y; k < a.r1; k += gridDim.y) x_row(a, k, cbeg, cend, halo, sm);
+}
+
+// ---- z ---------------------------------------------------------------------
+struct SmemZ {
+  RowD row[kZTileMax + 1];
+};
+
+// Columns [cb*NC, cb*NC+NC), rows [z0, z1), z1 - z0 <= kZTileMax; every
+// thread of the CTA calls it.  hbot / htop: write the bottom / top wall halo
+// rows of these columns (cb == 0 also of the four x-halo columns).
+template <int NC>
+__device__ __forceinline__ void z_tile(const Args& a, int cb, int z0, int z1, bool hbot, bool htop, SmemZ& sm) {
+  for (int rr = threadIdx.x; rr <= z1 - z0; rr += NC) {
+    const int k = z0 + rr;
+    sm.row[rr] = row_consts(MW_AT(a.hyi, k, a.nz + 1), MW_AT(a.hyti, k, a.nz + 1), MW_AT(a.hypi, k, a.nz + 1));
+  }
+  __syncthreads();
+  const int c = cb * NC + threadIdx.x;  // interior column
+  if ((hbot || htop) && cb == 0 && threadIdx.x < 4)
+    write_z_halo_column(a, threadIdx.x < 2 ? threadIdx.x : a.nx + threadIdx.x, hbot, htop);
+  const unsigned mask = __ballot_sync(0xffffffffu, c < a.nx);
+  if (c < a.nx) {
+    const int col = c + kHs;
+    if (hbot || htop) write_z_halo_column(a, col, hbot, htop);
+    double w[4][4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) w[q][j] = zval(a, q, z0 - 2 + j, col);
+    double nxt[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) nxt[q] = zval(a, q, z0 + 2, col);
+    double Fp[4];
+    flux_z(w, sm.row[0], a.HV, z0 == 0, mask, Fp);
+    for (int k = z0; k < z1; ++k) {
+      const long long o = (long long)(k + kHs) * a.pitch + col;
+      double iv[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) iv[q] = MW_AT(a.init, q * a.plane + o, 4 * a.plane);
+      const double rho_k = w[DENS][2];  // forcing rho' at cell k (interpolate.py:248-250)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        w[q][0] = w[q][1];
+        w[q][1] = w[q][2];
+        w[q][2] = w[q][3];
+        w[q][3] = nxt[q];
+      }
+      if (k + 1 < z1) {  // the row the next iteration needs, loaded one step ahead
+#pragma unroll
+        for (int q = 0; q < 4; ++q) nxt[q] = zval(a, q, k + 3, col);
+      }
+      double Fn[4];
+      flux_z(w, sm.row[k + 1 - z0], a.HV, k + 1 == a.nz, mask, Fn);
+      double v[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) v[q] = fma(a.c, Fp[q] - Fn[q], iv[q]);
+      v[WMOM] = fma(a.gdt, rho_k, v[WMOM]);
+      if (a.srcw) v[WMOM] = fma(a.dt, MW_AT(a.srcw, (long long)k * a.nx + c, (long long)a.nx * a.nz), v[WMOM]);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) MW_AT(a.out, q * a.plane + o, 4 * a.plane) = v[q];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) Fp[q] = Fn[q];
+    }
+  }
+  __syncthreads();  // the row table is rewritten by the next tile
+}
+
+// Tiles of a.z_tile rows of [a.r0, a.r1), one per CTA row.
+__global__ void __launch_bounds__(kZT) k_stage_z_ieee(Args a, int tile0) {
+  __shared__ SmemZ sm;
+  const int tile = tile0 + blockIdx.y;  // grid.y is capped at 65535: one launch per 65535 tiles
+  const int z0 = a.r0 + tile * a.z_tile, z1 = min(z0 + a.z_tile, a.r1);
+  const bool halo = a.flags & MW_FLAG_WRITE_HALO;
+  z_tile<kZT>(a, blockIdx.x, z0, z1, halo && z0 == 0, halo && z1 == a.nz, sm);
+}
+
+}  // namespace ieee
+
+// One direction-stage in the IEEE-FP64 form over output rows [r0, r1) (the
+// whole grid: 0, nz); arguments validated by the caller.
+int launch_stage_ieee(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
+                      const double* hyi, const double* hyti, const double* hypi, const double* srcw,
+                      const double* init, double* forcing, double* out, double dt_stage, int direction,
+                      unsigned flags, int r0, int r1, cudaStream_t stream) {
+  using namespace ieee;
+  MW_REQUIRE(0 <= r0 && r0 < r1 && r1 <= nz, MW_ERR_INVALID_ARG, "row range [%d, %d) outside [0, %d)", r0, r1, nz);
+  const Geom g = make_geom(nx, nz);
+  Args a;
+  a.nx = nx;
+  a.nz = nz;
+  a.pitch = g.pitch;
+  a.plane = g.plane;
+  a.hyc = hyc;
+  a.hytc = hytc;
+  a.hyi = hyi;
+  a.hyti = hyti;
+  a.hypi = hypi;
+  a.srcw = srcw;
+  a.init = init;
+  a.forcing = forcing;
+  a.out = out;
+  a.flags = flags;
+  const double d = direction == MW_DIR_X ? dx : dz;
+  a.HV = 12.0 * kHvBeta * d / (16 * dt_full);  // -12 hv
+  a.c = dt_stage / (12.0 * d);
+  a.dt = dt_stage;
+  a.gdt = -dt_stage * kGrav;
+  const int nchunks = (nx + kXC - 1) / kXC;
+  a.chunks_per_block = (nchunks + kXBlocksPerRow - 1) / kXBlocksPerRow;
+  a.r0 = r0;
+  a.r1 = r1;
+  const int rows = r1 - r0;
+  a.z_tile = z_tile_rows(nx, rows, kZT, kZTileMax);
+  if (direction == MW_DIR_X) {
+    dim3 grid((nchunks + a.chunks_per_block - 1) / a.chunks_per_block, (unsigned)std::min(rows, 65535));
+    k_stage_x_ieee<<<grid, kXT, 0, stream>>>(a);
+  } else {
+    const int ntiles = (rows + a.z_tile - 1) / a.z_tile;
+    for (int t0 = 0; t0 < ntiles; t0 += 65535) {
+      dim3 grid((nx + kZT - 1) / kZT, (unsigned)std::min(ntiles - t0, 65535));
+      k_stage_z_ieee<<<grid, kZT, 0, stream>>>(a, t0);
+      if (t0 + 65535 < ntiles) {
+        const int st = check_launch("z IEEE-FP64 direction-stage launch");
+        if (st) return st;
+      }
+    }
+  }
+  return check_launch(direction == MW_DIR_X ? "x IEEE-FP64 direction-stage launch"
+                                            : "z IEEE-FP64 direction-stage launch");
+}
+
+#if MW_CHECK
+MW_OOB_COUNTER(oob_count_ieee_stage)
+#endif
+
+}  // namespace mw

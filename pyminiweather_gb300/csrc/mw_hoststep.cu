@@ -23,6 +23,10 @@ int launch_stage_split(int nx, int nz, double dx, double dz, double dt_full, con
                        const double* hyi, const double* hyti, const double* hypi, const double* srcw,
                        const double* init, double* forcing, double* out, double dt_stage, int direction,
                        unsigned flags, int r0, int r1, int fmt, cudaStream_t stream);
+int launch_stage_ieee(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
+                      const double* hyi, const double* hyti, const double* hypi, const double* srcw,
+                      const double* init, double* forcing, double* out, double dt_stage, int direction,
+                      unsigned flags, int r0, int r1, cudaStream_t stream);
 
 namespace {
 
@@ -116,7 +120,7 @@ extern "C" int mw_step_f64_host(int nx, int nz, double dx, double dz, double dt_
   const size_t bytes = sizeof(double) * 4 * (size_t)g.plane;
   cudaStream_t s = (cudaStream_t)stream;
   const int nb = std::max(1, std::min({nbands, kMaxBands, nz / 16}));
-  if (f64_mode != MW_F64_SPLIT || nb == 1) {  // no bands: copy in, step, copy out
+  if ((f64_mode != MW_F64_SPLIT && f64_mode != MW_F64_IEEE) || nb == 1) {  // no bands: copy in, step, copy out
     cudaError_t e = cudaMemcpyAsync(state, h_in, bytes, cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return fail(MW_ERR_CUDA, "copy in: %s", cudaGetErrorString(e));
     if ((st = mw_step_f64(nx, nz, dx, dz, dt_full, dt, hyc, hytc, hyi, hyti, hypi, src_w, state, state_tmp, scratch, 1,
@@ -129,9 +133,13 @@ extern "C" int mw_step_f64_host(int nx, int nz, double dx, double dz, double dt_
   CopyRes* c = nullptr;
   if ((st = resources(&c))) return st;
   double *S = state, *Tmp = state_tmp, *A = scratch;
-  // The first stage of a direction leaves s1 in the scratch array as
-  // double-FP32 pairs (format 1) for the second (format 2), as mw_step_f64 does.
+  // In the split form the first stage of a direction leaves s1 in the scratch
+  // array as double-FP32 pairs (format 1) for the second (format 2), as
+  // mw_step_f64 does; the IEEE-FP64 form stores FP64 throughout.
   auto stage = [&](const double* init, double* forcing, double* out, double dts, int dir, int r0, int r1) {
+    if (f64_mode == MW_F64_IEEE)
+      return launch_stage_ieee(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, src_w, init, forcing, out, dts,
+                               dir, flags, r0, r1, s);
     const int fmt = out == A ? 1 : (forcing == A ? 2 : 0);
     return launch_stage_split(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, src_w, init, forcing, out, dts,
                               dir, flags, r0, r1, fmt, s);

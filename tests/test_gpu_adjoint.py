@@ -94,7 +94,7 @@ def test_stage_vjp_split_matches_native(nx, nz, direction):
     assert torch.equal(got[:, :2], torch.zeros_like(got[:, :2])) and torch.equal(got[:, :, -2:], torch.zeros_like(got[:, :, -2:]))
 
 
-@pytest.mark.parametrize("mode", ["native", "split"])
+@pytest.mark.parametrize("mode", ["native", "fp64", "split"])
 def test_rollout_gradient_matches_autograd(mode):
     """Gradient of the upper-half (rho theta)' misfit after 12 steps w.r.t. all
     four initial fields: hand-written adjoint (checkpoints every 5 steps; FP64
@@ -122,19 +122,66 @@ def test_rollout_gradient_matches_autograd(mode):
     assert float(g[:, :2].abs().max()) == 0.0 and float(g[:, :, -2:].abs().max()) == 0.0
 
 
-def test_adjoint_vs_finite_differences_512x256():
-    """The differentiation configuration: 512 x 256 thermal, 200 steps,
-    checkpoints every 20; target from amplitude 3.5 K; 16 seeded directions,
-    central differences with eps = 1e-6."""
+def _config4(mode):
+    """The differentiation configuration: 512 x 256 thermal (amplitude 3 K),
+    200 steps, checkpoints every 20; target from amplitude 3.5 K; loss = the
+    upper-half (rho theta)' misfit.  Returns (p, f, target, x0, ctx)."""
     nx, nz, steps = 512, 256, 200
     p, f = _fields(nx, nz, amp=3.0)
-    p["f64_mode"] = "native"  # FD differences of the forward need its full FP64 rounding
+    p["f64_mode"] = mode
     _, ft = _fields(nx, nz, amp=3.5)
     reset_direction()
-    evolve(p, ft, None, dt=p["dt"], nsteps=steps)
+    evolve(dict(p, f64_mode="native"), ft, None, dt=p["dt"], nsteps=steps)
     target = ft.state.clone()
     ctx = RolloutContext(params=p, fields=f, nsteps=steps, ckpt_every=20)
-    x0 = f.state.clone().requires_grad_(True)
+    return p, f, target, f.state.clone().requires_grad_(True), ctx
+
+
+@pytest.mark.parametrize("mode", ["native", "fp64", "split"])
+def test_adjoint_vs_autograd_512x256_200_steps(mode):
+    """The differentiation configuration checked against autograd through the
+    pure-PyTorch step at its own size: 512 x 256, 200 steps, gradient with
+    respect to all four initial fields.  Autograd recomputes each 20-step
+    segment (torch.utils.checkpoint) to bound its memory.  Bar: 1e-9
+    normwise per field for the FP64 forms; the double-FP32 form's error is
+    printed and held to 1e-7."""
+    from torch.utils.checkpoint import checkpoint
+    p, f, target, x0, ctx = _config4(mode)
+    nx, nz, steps = f.nx, f.nz, ctx.nsteps
+    loss = upper_half_rhot_misfit(rollout(x0, ctx), target, nz)
+    (g,) = torch.autograd.grad(loss, x0)
+    bg = _bg(f)
+
+    def segment(s, rev, n):
+        return TS.evolve_interior(s, bg, p, n, reverse=rev)[0]
+
+    xi = f.state[:, 2:-2, 2:-2].clone().requires_grad_(True)
+    s, rev = xi, False
+    for k in range(0, steps, 20):
+        s = checkpoint(segment, s, rev, 20, use_reentrant=False)
+        rev = rev if 20 % 2 == 0 else not rev
+    d = s[3, nz // 2:, :] - target[3, 2 + nz // 2:2 + nz, 2:-2]
+    lr = (d * d).sum()
+    (gr,) = torch.autograd.grad(lr, xi)
+    print("%s: loss %.12e (hand-written forward) vs %.12e (PyTorch step)" % (mode, float(loss), float(lr)))
+    bar = 1e-7 if mode == "split" else 1e-9
+    for v in range(4):
+        err = float((g[v, 2:-2, 2:-2] - gr[v]).abs().max() / gr[v].abs().max())
+        print("%s field %d: adjoint vs autograd normwise %.2e" % (mode, v, err))
+        assert err <= bar
+    assert abs(float(loss) - float(lr)) <= 1e-8 * abs(float(lr))
+    assert float(g[:, :2].abs().max()) == 0.0 and float(g[:, :, -2:].abs().max()) == 0.0
+
+
+@pytest.mark.parametrize("mode", ["native", "fp64"])
+def test_adjoint_vs_finite_differences_512x256(mode):
+    """The differentiation configuration: 512 x 256 thermal, 200 steps,
+    checkpoints every 20; target from amplitude 3.5 K; 16 seeded directions,
+    central differences with eps = 1e-6, for both IEEE-FP64 forwards (the FD
+    quotient needs FP64 rounding in the forward: the split form's 2^-47 noise
+    divided by 2 eps would dominate it)."""
+    p, f, target, x0, ctx = _config4(mode)
+    nx, nz = f.nx, f.nz
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     loss = upper_half_rhot_misfit(rollout(x0, ctx), target, nz)
@@ -143,7 +190,8 @@ def test_adjoint_vs_finite_differences_512x256():
     (g,) = torch.autograd.grad(loss, x0)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
-    print("512x256, 200 steps: forward %.3f s, adjoint %.3f s (ratio %.2f)" % (t1 - t0, t2 - t1, (t2 - t1) / (t1 - t0)))
+    print("%s 512x256, 200 steps: forward %.3f s, adjoint %.3f s (ratio %.2f)" % (
+        mode, t1 - t0, t2 - t1, (t2 - t1) / (t1 - t0)))
 
     def L(x):
         with torch.no_grad():
@@ -159,5 +207,5 @@ def test_adjoint_vs_finite_differences_512x256():
         ad = float((g * v).sum())
         rel = abs(fd - ad) / abs(ad)
         worst = max(worst, rel)
-        print("direction %2d: adjoint %.10e  central FD %.10e  rel %.2e" % (k, ad, fd, rel))
+        print("%s direction %2d: adjoint %.10e  central FD %.10e  rel %.2e" % (mode, k, ad, fd, rel))
     assert worst <= 1e-6
