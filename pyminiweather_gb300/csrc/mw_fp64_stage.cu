@@ -37,6 +37,7 @@
 // are applied to the indices and values as they are loaded.  Every global
 // access goes through MW_AT (bounds-checked in the debug library).
 #include <algorithm>
+#include <atomic>
 
 #include "mw_common.cuh"
 #include "mw_ensemble.cuh"
@@ -49,6 +50,12 @@ constexpr int kXC = kXT - 1;        // cells per x chunk
 constexpr int kXBlocksPerRow = 4;   // x CTAs per row
 constexpr int kZT = 128;            // columns per z CTA
 constexpr int kZTileMax = 64;       // rows per z CTA
+#ifndef MW_IEEE_XWARP
+#define MW_IEEE_XWARP 1                 // x pass: barrier-free warp segments (0: CTA chunks)
+#endif
+#ifndef MW_IEEE_X_SEGS_PER_WARP
+#define MW_IEEE_X_SEGS_PER_WARP 16
+#endif
 
 // ---- constant tables ------------------------------------------------------
 constexpr double binom(double e, int n) {  // C(e, n)
@@ -91,9 +98,12 @@ __constant__ Coef c_coef = make_coef();
 __constant__ Deg c_deg = make_deg();
 
 // ---- FP64 building blocks --------------------------------------------------
-// 1/y: FP32 estimate refined by one cubic Newton step (3 FP64 operations).
-// |y| outside [2^-125, 2^126) (and Inf, NaN, 0) takes the FP64 division.
-__device__ __forceinline__ double rcp(double y) {
+// 1/y for the lanes in `mask`, which call it together: an FP32 estimate
+// refined by one cubic Newton step (3 FP64 operations).  |y| outside
+// [2^-125, 2^126) (and Inf, NaN, 0) takes the FP64 division, behind a
+// warp-uniform branch so that the division is never evaluated speculatively
+// on the other lanes.
+__device__ __forceinline__ double rcp(double y, unsigned mask) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(y);
   const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
   const unsigned ex = (hi >> 20) & 0x7ffu;
@@ -107,7 +117,10 @@ __device__ __forceinline__ double rcp(double y) {
   const double e = fma(-y, r0, 1.0);
   const double t = fma(e, e, e);
   double r = fma(r0, t, r0);
-  if (ex - (1023u - 125u) > 250u) r = 1.0 / y;
+  const bool out = ex - (1023u - 125u) > 250u;
+  if (__any_sync(mask, out)) {
+    if (out) r = 1.0 / y;
+  }
   return r;
 }
 
@@ -123,7 +136,9 @@ __device__ __forceinline__ double pgm1(double d, unsigned mask) {
   double g = c_coef.c[n];
   for (int k = n - 1; k >= 1; --k) g = fma(g, d, c_coef.c[k]);
   double f = d * g;
-  if (big) f = expm1(kGamma * log1p(d));
+  if (__any_sync(mask, big)) {
+    if (big) f = expm1(kGamma * log1p(d));
+  }
   return f;
 }
 
@@ -151,7 +166,7 @@ __device__ __forceinline__ void flux_x(const double s[4][4], const RowD& r, doub
   double A[4], D[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) interp(s[q][0], s[q][1], s[q][2], s[q][3], A[q], D[q]);
-  const double ri = rcp(A[DENS] + r.R12);
+  const double ri = rcp(A[DENS] + r.R12, mask);
   const double u = A[UMOM] * ri;
   const double f = pgm1(A[RHOT] * r.IRT12, mask);
   F[0] = fma(HV, D[DENS], A[UMOM]);
@@ -171,7 +186,7 @@ __device__ __forceinline__ void flux_z(const double s[4][4], const RowD& r, doub
     AW = 0.0;
     D[DENS] = 0.0;
   }
-  const double ri = rcp(A[DENS] + r.R12);
+  const double ri = rcp(A[DENS] + r.R12, mask);
   const double w = AW * ri;
   const double f = pgm1(A[RHOT] * r.IRT12, mask);
   F[0] = fma(HV, D[DENS], AW);
@@ -301,6 +316,127 @@ __global__ void __launch_bounds__(kXT) k_stage_x_ieee(Args a) {
   for (int k = a.r0 + blockIdx.y; k < a.r1; k += gridDim.y) x_row(a, k, cbeg, cend, halo, sm);
 }
 
+// x, warp segments: the CTA owns the contiguous range [g0, g1) of the
+// row-major list of 63-cell segments (nseg per row) and splits it evenly over
+// its eight warps, which walk their segments with no CTA barrier.  Lane l
+// evaluates the fluxes at interfaces x0+l and x0+32+l (two independent FP64
+// chains) from the segment's values staged in the warp's shared-memory slice,
+// and updates cells x0+l and x0+32+l (l < 31) from its own and the next
+// lane's fluxes.  The next segment's values are loaded one segment ahead; the
+// row constants (an FP64 pow per row) are tabled once per CTA.
+constexpr int kWI = 64;             // interfaces per warp segment
+constexpr int kWCells = kWI - 1;    // cells per warp segment
+constexpr int kXWarps = kXT / 32;
+constexpr int kXRowsMax = 64;       // rows of one CTA's range
+struct SmemXW {
+  double sS[kXWarps][4][kWI + 4];   // [warp][variable][cell x0-2 .. x0+64]
+  RowD row[kXRowsMax];
+};
+
+#ifndef MW_IEEE_X_MIN_BLOCKS
+#define MW_IEEE_X_MIN_BLOCKS 2
+#endif
+__global__ void __launch_bounds__(kXT, MW_IEEE_X_MIN_BLOCKS) k_stage_x_ieee_w(Args a, int nseg, long long total,
+                                                                               long long gbase) {
+  __shared__ SmemXW sm;
+  const long long g0 = gbase + total * blockIdx.x / gridDim.x, g1 = gbase + total * (blockIdx.x + 1) / gridDim.x;
+  if (g0 >= g1) return;
+  const int row0 = (int)(g0 / nseg), nrows = (int)((g1 - 1) / nseg) - row0 + 1;  // nrows <= kXRowsMax (host)
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const long long n = g1 - g0;
+  const long long w0 = g0 + n * w / kXWarps, w1 = g0 + n * (w + 1) / kXWarps;
+  const int n4 = a.nz + 2 * kHs;
+  const bool halo = a.flags & MW_FLAG_WRITE_HALO;
+  // values of the segment: cells x0-2+lane, x0+30+lane and (lanes 0..2) x0+62+lane
+  auto load = [&](long long g, double v[3][4]) {
+    const int k = (int)(g / nseg), x0 = (int)(g - (long long)k * nseg) * kWCells;
+    const long long row = (long long)(k + kHs) * a.pitch;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const int c = x0 - 2 + 32 * j + lane;
+      if ((j < 2 || lane < 3) && c <= a.nx + 1) {
+        const long long col = wrap_x(c, a.nx) + kHs;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[j][q] = __ldg(&MW_F(a, q * a.plane + row + col));
+      }
+    }
+  };
+  double v[3][4] = {};
+  if (w0 < w1) load(w0, v);
+  for (int r = threadIdx.x; r < nrows; r += kXT) {
+    const double rt = MW_AT(a.hytc, row0 + r + kHs, n4);
+    sm.row[r] = row_consts(MW_AT(a.hyc, row0 + r + kHs, n4), rt, kC0 * pow(rt, kGamma));
+  }
+  __syncthreads();
+  for (long long g = w0; g < w1; ++g) {
+    const int k = (int)(g / nseg), sg = (int)(g - (long long)k * nseg), x0 = sg * kWCells;
+    const long long row = (long long)(k + kHs) * a.pitch;
+    __syncwarp();  // the previous segment's taps are read
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      if (j < 2 || lane < 3)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) sm.sS[w][q][32 * j + lane] = v[j][q];
+    if (halo && sg == 0 && lane < 4) {  // columns 0, 1 <- nx, nx+1; nx+2, nx+3 <- 2, 3
+      const int dst = lane < 2 ? lane : a.nx + lane, src = lane < 2 ? a.nx + lane : lane;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) MW_F(a, q * a.plane + row + dst) = MW_F(a, q * a.plane + row + src);
+    }
+    if (g + 1 < w1) load(g + 1, v);
+    const int ia = x0 + lane, ib = x0 + 32 + lane;  // interfaces (and cells) of this lane
+    const bool ua = ia < a.nx, ub = lane < 31 && ib < a.nx;
+    double iva[4], ivb[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if (ua) iva[q] = MW_AT(a.init, q * a.plane + row + ia + kHs, 4 * a.plane);
+      if (ub) ivb[q] = MW_AT(a.init, q * a.plane + row + ib + kHs, 4 * a.plane);
+    }
+    __syncwarp();
+    const RowD rc = sm.row[k - row0];
+    double Fa[4] = {0, 0, 0, 0}, Fb[4] = {0, 0, 0, 0};
+    const unsigned ma = __ballot_sync(0xffffffffu, ia <= a.nx), mb = __ballot_sync(0xffffffffu, ib <= a.nx);
+    if (ia <= a.nx) {
+      double s[4][4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) s[q][j] = sm.sS[w][q][lane + j];
+      flux_x(s, rc, a.HV, ma, Fa);
+    }
+    if (ib <= a.nx) {
+      double s[4][4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) s[q][j] = sm.sS[w][q][32 + lane + j];
+      flux_x(s, rc, a.HV, mb, Fb);
+    }
+    // lane l needs the flux at interface x0+l+1: lane l+1's Fa, or for l = 31 lane 0's Fb
+    double Fa1[4], Fb1[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      Fa1[q] = __shfl_sync(0xffffffffu, lane == 0 ? Fb[q] : Fa[q], (lane + 1) & 31);
+      Fb1[q] = __shfl_down_sync(0xffffffffu, Fb[q], 1);
+    }
+    if (ua) {
+      double o[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) o[q] = fma(a.c, Fa[q] - Fa1[q], iva[q]);
+      if (a.srcw) o[WMOM] = fma(a.dt, MW_AT(a.srcw, (long long)k * a.nx + ia, (long long)a.nx * a.nz), o[WMOM]);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) MW_AT(a.out, q * a.plane + row + ia + kHs, 4 * a.plane) = o[q];
+    }
+    if (ub) {
+      double o[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) o[q] = fma(a.c, Fb[q] - Fb1[q], ivb[q]);
+      if (a.srcw) o[WMOM] = fma(a.dt, MW_AT(a.srcw, (long long)k * a.nx + ib, (long long)a.nx * a.nz), o[WMOM]);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) MW_AT(a.out, q * a.plane + row + ib + kHs, 4 * a.plane) = o[q];
+    }
+  }
+}
+
 // ---- z ---------------------------------------------------------------------
 struct SmemZ {
   RowD row[kZTileMax + 1];
@@ -375,6 +511,22 @@ __global__ void __launch_bounds__(kZT) k_stage_z_ieee(Args a, int tile0) {
   z_tile<kZT>(a, blockIdx.x, z0, z1, halo && z0 == 0, halo && z1 == a.nz, sm);
 }
 
+// CTAs of k_stage_x_ieee_w resident on the current device, cached per device.
+int x_resident_ctas(int* out) {
+  static std::atomic<int> cache[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return fail(MW_ERR_CUDA, "cudaGetDevice failed");
+  const bool cached = dev >= 0 && dev < 64;
+  if (cached && (*out = cache[dev].load(std::memory_order_relaxed)) > 0) return MW_OK;
+  int per_sm = 0, sms = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage_x_ieee_w, kXT, 0);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return fail(MW_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
+  *out = std::max(1, per_sm) * sms;
+  if (cached) cache[dev].store(*out, std::memory_order_relaxed);
+  return MW_OK;
+}
+
 }  // namespace ieee
 
 // One direction-stage in the IEEE-FP64 form over output rows [r0, r1) (the
@@ -412,7 +564,21 @@ int launch_stage_ieee(int nx, int nz, double dx, double dz, double dt_full, cons
   a.r1 = r1;
   const int rows = r1 - r0;
   a.z_tile = z_tile_rows(nx, rows, kZT, kZTileMax);
-  if (direction == MW_DIR_X) {
+  if (direction == MW_DIR_X && MW_IEEE_XWARP) {
+    // About MW_IEEE_X_SEGS_PER_WARP segments per warp in a whole number of
+    // resident waves of equal ranges (one wave, at least one segment per warp,
+    // for small grids); at most kXRowsMax rows per CTA range.
+    const int nseg = (nx + kWCells - 1) / kWCells;
+    const long long total = (long long)nseg * rows;
+    int resident = 0, st = x_resident_ctas(&resident);
+    if (st) return st;
+    long long grid = std::min<long long>(resident, (total + kXWarps - 1) / kXWarps);
+    grid = std::max<long long>(grid, total / (kXWarps * MW_IEEE_X_SEGS_PER_WARP));
+    if (grid > resident) grid = (grid + resident - 1) / resident * resident;
+    grid = std::max<long long>(grid, (rows + kXRowsMax - 3) / (kXRowsMax - 2));
+    MW_REQUIRE(grid <= 0x7fffffffLL, MW_ERR_SHAPE, "grid too large for the x direction-stage launch");
+    k_stage_x_ieee_w<<<(unsigned)grid, kXT, 0, stream>>>(a, nseg, total, (long long)r0 * nseg);
+  } else if (direction == MW_DIR_X) {
     dim3 grid((nchunks + a.chunks_per_block - 1) / a.chunks_per_block, (unsigned)std::min(rows, 65535));
     k_stage_x_ieee<<<grid, kXT, 0, stream>>>(a);
   } else {
