@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define MW_ABI_VERSION 3
+#define MW_ABI_VERSION 4
 
 enum mw_status {
   MW_OK = 0,
@@ -69,6 +69,14 @@ enum mw_f64_mode {
                                  are any (synchronises the stream to read the
                                  count, which is kept in the first 8 bytes of
                                  the scratch array: nothing is allocated) */
+
+#define MW_FLAG_PAIRS_OUT 8u /* mw_dirstage_f64, split form: store `out` as the double-FP32
+                              pairs mw_step_f64 keeps its first RK stage's result in
+                              (needs init == forcing) */
+#define MW_FLAG_PAIRS_IN 16u  /* mw_dirstage_f64, split form: read `forcing` as such pairs.
+                              With these two flags a caller can issue a split-form step
+                              stage by stage with the launches mw_step_f64 makes (to
+                              time them one by one); the pair arrays are not FP64 data */
 
 /* Background profile of the initial condition. */
 enum mw_background {
@@ -205,14 +213,15 @@ int mw_ensemble_plan(int n_members, const mw_ens_member* members, int z_tile, vo
  * and grid_z CTAs (0 = one full-occupancy wave); the FP64 call first writes
  * the plan's row-constant table (one more launch per call).  The direction order follows
  * *reverse as in mw_step_f64 (all members alike).  FP64 storage supports
- * f64_mode MW_F64_SPLIT. */
+ * f64_mode MW_F64_IEEE and MW_F64_SPLIT. */
 int mw_ensemble_step_f64(void* plan_device, const mw_ens_plan_info* info, const double* hy_dens_cell,
                          const double* hy_dens_theta_cell, const double* hy_dens_int, const double* hy_dens_theta_int,
                          const double* hy_pressure_int, double* state, double* state_tmp, double* scratch, int nsteps,
                          int* reverse, int f64_mode, unsigned flags, int grid_x, int grid_z, void* stream);
-/* Resident CTAs per SM of the persistent ensemble kernels (FP64 split or FP32
- * storage, x or z direction): a default grid is this times the SM count. */
-int mw_ensemble_occupancy(int f32_storage, int direction, int* blocks_per_sm);
+/* Resident CTAs per SM of the persistent ensemble kernels of one form (0: FP64
+ * storage, split form; 1: FP32 storage; 2: FP64 storage, IEEE-FP64 form) and
+ * direction: a default grid is this times the SM count. */
+int mw_ensemble_occupancy(int form, int direction, int* blocks_per_sm);
 int mw_ensemble_step_f32(void* plan_device, const mw_ens_plan_info* info, const double* hy_dens_cell,
                          const double* hy_dens_theta_cell, const double* hy_dens_int, const double* hy_dens_theta_int,
                          const double* hy_pressure_int, float* state, float* state_tmp, float* scratch, int nsteps,

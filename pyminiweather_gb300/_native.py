@@ -23,6 +23,8 @@ MW_F64_NATIVE, MW_F64_SPLIT, MW_F64_IEEE = 0, 1, 2
 MW_FLAG_WRITE_HALO = 1
 MW_FLAG_INDEX64 = 2
 MW_FLAG_CHECK_FINITE = 4
+MW_FLAG_PAIRS_OUT = 8
+MW_FLAG_PAIRS_IN = 16
 MW_BG_CONST_THETA, MW_BG_BVFREQ = 0, 1
 MW_MAX_BUBBLES = 8
 

@@ -686,8 +686,14 @@ extern "C" int mw_dirstage_f64(int nx, int nz, double dx, double dz, double dt_f
   MW_REQUIRE(valid_f64_mode(f64_mode), MW_ERR_INVALID_ARG, "unknown f64_mode %d",
              f64_mode);
   MW_REQUIRE(std::isfinite(dt_stage), MW_ERR_INVALID_ARG, "dt_stage must be finite");
+  const unsigned pairs = flags & (MW_FLAG_PAIRS_OUT | MW_FLAG_PAIRS_IN);
+  MW_REQUIRE(!pairs || (f64_mode == MW_F64_SPLIT && pairs != (MW_FLAG_PAIRS_OUT | MW_FLAG_PAIRS_IN)),
+             MW_ERR_INVALID_ARG, "MW_FLAG_PAIRS_OUT / _IN: split form only, one of the two");
+  MW_REQUIRE(!(flags & MW_FLAG_PAIRS_OUT) || init == forcing, MW_ERR_INVALID_ARG,
+             "MW_FLAG_PAIRS_OUT needs init == forcing (the first RK stage)");
+  const int fmt = (flags & MW_FLAG_PAIRS_OUT) ? 1 : ((flags & MW_FLAG_PAIRS_IN) ? 2 : 0);
   return stage_f64(nx, nz, dx, dz, dt_full, hyc, hytc, hyi, hyti, hypi, src_w, init, forcing, out, dt_stage,
-                   direction, f64_mode, flags, (cudaStream_t)stream);
+                   direction, f64_mode, flags & ~pairs, (cudaStream_t)stream, fmt);
 }
 
 extern "C" int mw_dirstage_f32(int nx, int nz, double dx, double dz, double dt_full, const double* hyc,

@@ -84,10 +84,14 @@ int num_sms(int* sms) {
   return MW_OK;
 }
 
-template <typename T, typename Launch, typename Occ>
+// fmts: storage format of the three RK stages' forcing / output (the split
+// form keeps s1 as pairs; the other forms store every stage as T).
+// row_table(table): writes the x row-constant table once per call (or nothing).
+template <typename T, typename Launch, typename Occ, typename RowTable>
 int ens_step(void* plan, const mw_ens_plan_info* info, const double* hyc, const double* hytc, const double* hyi,
              const double* hyti, const double* hypi, T* S, T* Tmp, T* A, int nsteps, int* reverse, unsigned flags,
-             int grid_x, int grid_z, cudaStream_t stream, Launch launch, Occ occupancy) {
+             int grid_x, int grid_z, cudaStream_t stream, Launch launch, Occ occupancy, const int fmts[3],
+             RowTable row_table) {
   MW_REQUIRE(plan && info, MW_ERR_INVALID_ARG, "plan and info must not be NULL");
   MW_REQUIRE(((uintptr_t)plan % 16) == 0, MW_ERR_ALIGN, "plan must be 16-byte aligned");
   MW_REQUIRE(hyc && hytc && hyi && hyti && hypi, MW_ERR_INVALID_ARG, "background buffers must not be NULL");
@@ -126,9 +130,7 @@ int ens_step(void* plan, const mw_ens_plan_info* info, const double* hyc, const 
   es.mconsts = (const char*)plan + ens_consts_off(*info);
   es.n_xrows = info->n_xrows;
   es.n_members = info->n_members;
-  if (std::is_same<T, double>::value && nsteps > 0 &&
-      (st = launch_ens_split_rowtable(hyc, hytc, info->n_xrows, (char*)plan + info->xrows_off, stream)))
-    return st;
+  if (nsteps > 0 && (st = row_table((char*)plan + info->xrows_off))) return st;
   for (int n = 0; n < nsteps; ++n) {
     const int dirs[2] = {*reverse ? MW_DIR_X : MW_DIR_Z, *reverse ? MW_DIR_Z : MW_DIR_X};
     for (int d = 0; d < 2; ++d) {
@@ -140,7 +142,6 @@ int ens_step(void* plan, const mw_ens_plan_info* info, const double* hyc, const 
       T* frc[3] = {S, A, Tmp};
       T* outs[3] = {A, Tmp, S};
       const int div[3] = {3, 2, 1};
-      const int fmts[3] = {1, 2, 0};  // split form: s1 kept in scratch as pairs (kToPair, kFromPair, kF64)
       for (int s = 0; s < 3; ++s) {
         es.init = ins[s];
         es.forcing = frc[s];
@@ -199,6 +200,10 @@ extern "C" int mw_ensemble_plan(int n_members, const mw_ens_member* members, int
         c.c_f = (float)(dts / d);
         c.dt_f = (float)dts;
         c.pad = 0.0f;
+        c.HV = 12.0 * kHvBeta * d / (16 * m.dt);  // as launch_stage_ieee forms them
+        c.c = dts / (12.0 * d);
+        c.dt = dts;
+        c.gdt = -dts * kGrav;
         MW_REQUIRE(std::isfinite(c.c12s), MW_ERR_INVALID_ARG,
                    "member %d: dt / (12 d) = %g is above the split form's range", e, dts / (12.0 * d));
       }
@@ -223,26 +228,40 @@ extern "C" int mw_ensemble_step_f64(void* plan_device, const mw_ens_plan_info* i
                                     const double* hytc, const double* hyi, const double* hyti, const double* hypi,
                                     double* state, double* state_tmp, double* scratch, int nsteps, int* reverse,
                                     int f64_mode, unsigned flags, int grid_x, int grid_z, void* stream) {
-  MW_REQUIRE(f64_mode == MW_F64_SPLIT, MW_ERR_INVALID_ARG,
-             "ensembles with FP64 storage run the split form (f64_mode MW_F64_SPLIT)");
+  MW_REQUIRE(f64_mode == MW_F64_SPLIT || f64_mode == MW_F64_IEEE, MW_ERR_INVALID_ARG,
+             "ensembles with FP64 storage run f64_mode MW_F64_IEEE or MW_F64_SPLIT");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (f64_mode == MW_F64_IEEE) {
+    const int fmts[3] = {0, 0, 0};
+    return ens_step<double>(plan_device, info, hyc, hytc, hyi, hyti, hypi, state, state_tmp, scratch, nsteps, reverse,
+                            flags, grid_x, grid_z, s,
+                            [](const EnsStageT<double>& es, int g) { return launch_ens_ieee(es, g); },
+                            [](int d, int* b) { return ens_ieee_occupancy(d, b); }, fmts,
+                            [&](void* t) { return launch_ens_ieee_rowtable(hyc, hytc, info->n_xrows, t, s); });
+  }
+  const int fmts[3] = {1, 2, 0};  // s1 kept in scratch as pairs (kToPair, kFromPair, kF64)
   return ens_step<double>(plan_device, info, hyc, hytc, hyi, hyti, hypi, state, state_tmp, scratch, nsteps, reverse,
-                          flags, grid_x, grid_z, (cudaStream_t)stream,
+                          flags, grid_x, grid_z, s,
                           [](const EnsStageT<double>& es, int g) { return launch_ens_split(es, g); },
-                          [](int d, int* b) { return ens_split_occupancy(d, b); });
+                          [](int d, int* b) { return ens_split_occupancy(d, b); }, fmts,
+                          [&](void* t) { return launch_ens_split_rowtable(hyc, hytc, info->n_xrows, t, s); });
 }
 
 extern "C" int mw_ensemble_step_f32(void* plan_device, const mw_ens_plan_info* info, const double* hyc,
                                     const double* hytc, const double* hyi, const double* hyti, const double* hypi,
                                     float* state, float* state_tmp, float* scratch, int nsteps, int* reverse,
                                     unsigned flags, int grid_x, int grid_z, void* stream) {
+  const int fmts[3] = {0, 0, 0};
   return ens_step<float>(plan_device, info, hyc, hytc, hyi, hyti, hypi, state, state_tmp, scratch, nsteps, reverse,
                          flags, grid_x, grid_z, (cudaStream_t)stream,
                          [](const EnsStageT<float>& es, int g) { return launch_ens_f32(es, g); },
-                         [](int d, int* b) { return ens_f32_occupancy(d, b); });
+                         [](int d, int* b) { return ens_f32_occupancy(d, b); }, fmts, [](void*) { return MW_OK; });
 }
 
-extern "C" int mw_ensemble_occupancy(int f32_storage, int direction, int* blocks_per_sm) {
+extern "C" int mw_ensemble_occupancy(int form, int direction, int* blocks_per_sm) {
   MW_REQUIRE(blocks_per_sm != nullptr, MW_ERR_INVALID_ARG, "blocks_per_sm must not be NULL");
   MW_REQUIRE(direction == MW_DIR_X || direction == MW_DIR_Z, MW_ERR_INVALID_ARG, "direction must be 0 or 1");
-  return f32_storage ? ens_f32_occupancy(direction, blocks_per_sm) : ens_split_occupancy(direction, blocks_per_sm);
+  MW_REQUIRE(form >= 0 && form <= 2, MW_ERR_INVALID_ARG, "form must be 0 (FP64 split), 1 (FP32) or 2 (IEEE FP64)");
+  if (form == 1) return ens_f32_occupancy(direction, blocks_per_sm);
+  return form == 2 ? ens_ieee_occupancy(direction, blocks_per_sm) : ens_split_occupancy(direction, blocks_per_sm);
 }

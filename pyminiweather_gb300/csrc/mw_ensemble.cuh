@@ -12,14 +12,16 @@ namespace mw {
 // when the plan is built, exactly as the single-grid launches form them.
 // Split form: (h, l) float pairs of 12 hv, 12 d, 12 dz g and dt_stage / (12 d),
 // and dt_stage / (12 d) * 2^896 in FP64.  FP32 form: hv, dt_stage / d and
-// dt_stage rounded to float.  Entry (member * 2 + (direction == z)) * 3 + stage
+// dt_stage rounded to float.  IEEE-FP64 form: -12 hv, dt_stage / (12 d),
+// dt_stage and -dt_stage g.  Entry (member * 2 + (direction == z)) * 3 + stage
 // (stage 0, 1, 2: dt/3, dt/2, dt).
 struct EnsMemberConsts {
   float hv12[2], d12[2], gz12[2], c12[2];
   double c12s;
   float hv_f, c_f, dt_f, pad;
+  double HV, c, dt, gdt;
 };
-static_assert(sizeof(EnsMemberConsts) == 56, "EnsMemberConsts layout");
+static_assert(sizeof(EnsMemberConsts) == 88, "EnsMemberConsts layout");
 
 // Arguments of one ensemble direction-stage launch (T = state storage type).
 template <typename T>
@@ -59,17 +61,20 @@ int launch_ens_split(const EnsStage& es, int grid);
 int ens_split_occupancy(int direction, int* blocks_per_sm);
 int launch_ens_f32(const EnsStageT<float>& es, int grid);
 int ens_f32_occupancy(int direction, int* blocks_per_sm);
+int launch_ens_ieee(const EnsStage& es, int grid);
+int ens_ieee_occupancy(int direction, int* blocks_per_sm);
 
 constexpr int kEnsZTileMax = 64;
 constexpr int kEnsZCols = 64;  // columns per z work item (one CTA of kEnsZCols threads)
-constexpr size_t kEnsRowBytes = 32;  // one row's background constants (four double-FP32 pairs)
+constexpr size_t kEnsRowBytes = 32;  // one row's background constants (four double-FP32 pairs, or four FP64)
 
 constexpr int kEnsConstsPerMember = 6;
 inline size_t ens_consts_off(const mw_ens_plan_info& info) {
   return (info.xrows_off + kEnsRowBytes * (size_t)info.n_xrows + 15) & ~(size_t)15;
 }
 
-// Row-constant table of the split ensemble x kernels: entry j from hyc[j], hytc[j].
+// Row-constant tables of the split / IEEE-FP64 ensemble x kernels: entry j from hyc[j], hytc[j].
 int launch_ens_split_rowtable(const double* hyc, const double* hytc, long long n, void* table, cudaStream_t stream);
+int launch_ens_ieee_rowtable(const double* hyc, const double* hytc, long long n, void* table, cudaStream_t stream);
 
 }  // namespace mw

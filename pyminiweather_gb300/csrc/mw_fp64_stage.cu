@@ -333,21 +333,16 @@ struct SmemXW {
   RowD row[kXRowsMax];
 };
 
-#ifndef MW_IEEE_X_MIN_BLOCKS
-#define MW_IEEE_X_MIN_BLOCKS 2
-#endif
-__global__ void __launch_bounds__(kXT, MW_IEEE_X_MIN_BLOCKS) k_stage_x_ieee_w(Args a, int nseg, long long total,
-                                                                               long long gbase) {
-  __shared__ SmemXW sm;
-  const long long g0 = gbase + total * blockIdx.x / gridDim.x, g1 = gbase + total * (blockIdx.x + 1) / gridDim.x;
-  if (g0 >= g1) return;
-  const int row0 = (int)(g0 / nseg), nrows = (int)((g1 - 1) / nseg) - row0 + 1;  // nrows <= kXRowsMax (host)
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const long long n = g1 - g0;
-  const long long w0 = g0 + n * w / kXWarps, w1 = g0 + n * (w + 1) / kXWarps;
-  const int n4 = a.nz + 2 * kHs;
-  const bool halo = a.flags & MW_FLAG_WRITE_HALO;
-  // values of the segment: cells x0-2+lane, x0+30+lane and (lanes 0..2) x0+62+lane
+// Walks the segments [g0, g1) of the row-major list of kWCells-cell segments
+// (nseg per row); row_at(k) gives the constants of row k.  Every lane of the
+// warp calls it; prologue() runs once, after the first segment's loads are
+// issued (so that their latency overlaps it), also when the range is empty
+// (it may contain a CTA barrier).  sS is the warp's shared-memory slice.
+template <typename RowAt, typename Prologue>
+__device__ __forceinline__ void x_warp_walk(const Args& a, int nseg, long long g0, long long g1, RowAt row_at,
+                                            bool halo, double (*sS)[kWI + 4], Prologue prologue) {
+  const int lane = threadIdx.x & 31;
+  // values of segment g: cells x0-2+lane, x0+30+lane and (lanes 0..2) x0+62+lane
   auto load = [&](long long g, double v[3][4]) {
     const int k = (int)(g / nseg), x0 = (int)(g - (long long)k * nseg) * kWCells;
     const long long row = (long long)(k + kHs) * a.pitch;
@@ -362,13 +357,9 @@ __global__ void __launch_bounds__(kXT, MW_IEEE_X_MIN_BLOCKS) k_stage_x_ieee_w(Ar
     }
   };
   double v[3][4] = {};
-  if (w0 < w1) load(w0, v);
-  for (int r = threadIdx.x; r < nrows; r += kXT) {
-    const double rt = MW_AT(a.hytc, row0 + r + kHs, n4);
-    sm.row[r] = row_consts(MW_AT(a.hyc, row0 + r + kHs, n4), rt, kC0 * pow(rt, kGamma));
-  }
-  __syncthreads();
-  for (long long g = w0; g < w1; ++g) {
+  if (g0 < g1) load(g0, v);
+  prologue();
+  for (long long g = g0; g < g1; ++g) {
     const int k = (int)(g / nseg), sg = (int)(g - (long long)k * nseg), x0 = sg * kWCells;
     const long long row = (long long)(k + kHs) * a.pitch;
     __syncwarp();  // the previous segment's taps are read
@@ -376,13 +367,13 @@ __global__ void __launch_bounds__(kXT, MW_IEEE_X_MIN_BLOCKS) k_stage_x_ieee_w(Ar
     for (int j = 0; j < 3; ++j)
       if (j < 2 || lane < 3)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) sm.sS[w][q][32 * j + lane] = v[j][q];
-    if (halo && sg == 0 && lane < 4) {  // columns 0, 1 <- nx, nx+1; nx+2, nx+3 <- 2, 3
+        for (int q = 0; q < 4; ++q) sS[q][32 * j + lane] = v[j][q];
+    if (halo && sg == 0 && lane < 4) {  // columns 0, 1 <- nx, nx+1; nx+2, nx+3 <- 2, 3 (ics/bcs.py:35-39)
       const int dst = lane < 2 ? lane : a.nx + lane, src = lane < 2 ? a.nx + lane : lane;
 #pragma unroll
       for (int q = 0; q < 4; ++q) MW_F(a, q * a.plane + row + dst) = MW_F(a, q * a.plane + row + src);
     }
-    if (g + 1 < w1) load(g + 1, v);
+    if (g + 1 < g1) load(g + 1, v);
     const int ia = x0 + lane, ib = x0 + 32 + lane;  // interfaces (and cells) of this lane
     const bool ua = ia < a.nx, ub = lane < 31 && ib < a.nx;
     double iva[4], ivb[4];
@@ -392,7 +383,7 @@ __global__ void __launch_bounds__(kXT, MW_IEEE_X_MIN_BLOCKS) k_stage_x_ieee_w(Ar
       if (ub) ivb[q] = MW_AT(a.init, q * a.plane + row + ib + kHs, 4 * a.plane);
     }
     __syncwarp();
-    const RowD rc = sm.row[k - row0];
+    const RowD rc = row_at(k);
     double Fa[4] = {0, 0, 0, 0}, Fb[4] = {0, 0, 0, 0};
     const unsigned ma = __ballot_sync(0xffffffffu, ia <= a.nx), mb = __ballot_sync(0xffffffffu, ib <= a.nx);
     if (ia <= a.nx) {
@@ -400,7 +391,7 @@ __global__ void __launch_bounds__(kXT, MW_IEEE_X_MIN_BLOCKS) k_stage_x_ieee_w(Ar
 #pragma unroll
       for (int q = 0; q < 4; ++q)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) s[q][j] = sm.sS[w][q][lane + j];
+        for (int j = 0; j < 4; ++j) s[q][j] = sS[q][lane + j];
       flux_x(s, rc, a.HV, ma, Fa);
     }
     if (ib <= a.nx) {
@@ -408,7 +399,7 @@ __global__ void __launch_bounds__(kXT, MW_IEEE_X_MIN_BLOCKS) k_stage_x_ieee_w(Ar
 #pragma unroll
       for (int q = 0; q < 4; ++q)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) s[q][j] = sm.sS[w][q][32 + lane + j];
+        for (int j = 0; j < 4; ++j) s[q][j] = sS[q][32 + lane + j];
       flux_x(s, rc, a.HV, mb, Fb);
     }
     // lane l needs the flux at interface x0+l+1: lane l+1's Fa, or for l = 31 lane 0's Fb
@@ -435,6 +426,31 @@ __global__ void __launch_bounds__(kXT, MW_IEEE_X_MIN_BLOCKS) k_stage_x_ieee_w(Ar
       for (int q = 0; q < 4; ++q) MW_AT(a.out, q * a.plane + row + ib + kHs, 4 * a.plane) = o[q];
     }
   }
+}
+
+#ifndef MW_IEEE_X_MIN_BLOCKS
+#define MW_IEEE_X_MIN_BLOCKS 2
+#endif
+// Single grid: the CTA owns the contiguous range [g0, g1) of segments of rows
+// [r0, r1) and splits it evenly over its warps; the row constants (an FP64 pow
+// per row) are tabled once per CTA while the warps' first loads are in flight.
+__global__ void __launch_bounds__(kXT, MW_IEEE_X_MIN_BLOCKS) k_stage_x_ieee_w(Args a, int nseg, long long total,
+                                                                               long long gbase) {
+  __shared__ SmemXW sm;
+  const long long g0 = gbase + total * blockIdx.x / gridDim.x, g1 = gbase + total * (blockIdx.x + 1) / gridDim.x;
+  if (g0 >= g1) return;
+  const int row0 = (int)(g0 / nseg), nrows = (int)((g1 - 1) / nseg) - row0 + 1;  // nrows <= kXRowsMax (host)
+  const int w = threadIdx.x >> 5;
+  const long long n = g1 - g0;
+  const int n4 = a.nz + 2 * kHs;
+  x_warp_walk(a, nseg, g0 + n * w / kXWarps, g0 + n * (w + 1) / kXWarps, [&](int k) { return sm.row[k - row0]; },
+              a.flags & MW_FLAG_WRITE_HALO, sm.sS[w], [&]() {
+                for (int r = threadIdx.x; r < nrows; r += kXT) {
+                  const double rt = MW_AT(a.hytc, row0 + r + kHs, n4);
+                  sm.row[r] = row_consts(MW_AT(a.hyc, row0 + r + kHs, n4), rt, kC0 * pow(rt, kGamma));
+                }
+                __syncthreads();
+              });
 }
 
 // ---- z ---------------------------------------------------------------------
@@ -511,6 +527,81 @@ __global__ void __launch_bounds__(kZT) k_stage_z_ieee(Args a, int tile0) {
   z_tile<kZT>(a, blockIdx.x, z0, z1, halo && z0 == 0, halo && z1 == a.nz, sm);
 }
 
+// ---- ensembles -------------------------------------------------------------
+// One persistent launch per direction-stage walks a work list over all members
+// (x items: member rows; z items: member column-block tiles).  Each member's
+// stage constants were formed on the host with the plan, exactly as
+// launch_stage_ieee forms them for a single grid, and the x row constants
+// come from a table the step call writes once (no FP64 pow per row).
+__device__ __forceinline__ Args member_args(const EnsStage& es, int e) {
+  const mw_ens_member m = MW_AT(es.members, e, es.n_members);
+  Args a;
+  a.nx = m.nx;
+  a.nz = m.nz;
+  a.pitch = m.nx + 2 * kHs;
+  a.plane = (long long)(m.nz + 2 * kHs) * a.pitch;
+  a.hyc = es.hyc + m.cell_off;
+  a.hytc = es.hytc + m.cell_off;
+  a.hyi = es.hyi + m.int_off;
+  a.hyti = es.hyti + m.int_off;
+  a.hypi = es.hypi + m.int_off;
+  a.srcw = nullptr;
+  a.init = es.init + m.state_off;
+  a.forcing = es.forcing + m.state_off;
+  a.out = es.out + m.state_off;
+  a.flags = es.flags;
+  const EnsMemberConsts& c = MW_AT(reinterpret_cast<const EnsMemberConsts*>(es.mconsts), mconsts_index(es, e),
+                                   (long long)kEnsConstsPerMember * es.n_members);
+  a.HV = c.HV;
+  a.c = c.c;
+  a.dt = c.dt;
+  a.gdt = c.gdt;
+  a.chunks_per_block = 0;
+  a.z_tile = es.z_tile;
+  a.r0 = 0;
+  a.r1 = m.nz;
+  return a;
+}
+
+static_assert(sizeof(RowD) == kEnsRowBytes, "row-constant table entry size");
+
+__global__ void k_ens_row_table_ieee(const double* hyc, const double* hytc, long long n, RowD* table) {
+  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x) {
+    const double rt = MW_AT(hytc, j, n);
+    MW_AT(table, j, n) = row_consts(MW_AT(hyc, j, n), rt, kC0 * pow(rt, kGamma));
+  }
+}
+
+// x items are rows (member, row), one per warp: the warp walks the row's
+// segments as the single-grid kernel does.
+__global__ void __launch_bounds__(kXT, MW_IEEE_X_MIN_BLOCKS) k_ens_x_ieee(EnsStage es) {
+  __shared__ SmemXW sm;
+  const int w = threadIdx.x >> 5;
+  const int nw = gridDim.x * kXWarps;
+  for (int it = blockIdx.x * kXWarps + w; it < es.n_items; it += nw) {
+    const int2 item = MW_AT(es.items, it, es.n_items);  // (member, row)
+    const Args a = member_args(es, item.x);
+    const int nseg = (a.nx + kWCells - 1) / kWCells;
+    const RowD r = MW_AT(reinterpret_cast<const RowD*>(es.xrows),
+                         MW_AT(es.members, item.x, es.n_members).cell_off + item.y + kHs, es.n_xrows);
+    x_warp_walk(a, nseg, (long long)item.y * nseg, (long long)(item.y + 1) * nseg, [&](int) { return r; },
+                a.flags & MW_FLAG_WRITE_HALO, sm.sS[w], []() {});
+  }
+}
+
+__global__ void __launch_bounds__(kEnsZCols) k_ens_z_ieee(EnsStage es) {
+  __shared__ SmemZ sm;
+  for (int it = blockIdx.x; it < es.n_items; it += gridDim.x) {
+    const int2 item = MW_AT(es.items, it, es.n_items);  // (member, column block + ncb * tile)
+    const Args a = member_args(es, item.x);
+    const int ncb = (a.nx + kEnsZCols - 1) / kEnsZCols;
+    const int cb = item.y % ncb, tile = item.y / ncb;
+    const int z0 = tile * es.z_tile, z1 = min(z0 + es.z_tile, a.nz);
+    const bool halo = a.flags & MW_FLAG_WRITE_HALO;
+    z_tile<kEnsZCols>(a, cb, z0, z1, halo && z0 == 0, halo && z1 == a.nz, sm);
+  }
+}
+
 // CTAs of k_stage_x_ieee_w resident on the current device, cached per device.
 int x_resident_ctas(int* out) {
   static std::atomic<int> cache[64];
@@ -528,6 +619,34 @@ int x_resident_ctas(int* out) {
 }
 
 }  // namespace ieee
+
+int launch_ens_ieee(const EnsStage& es, int grid) {
+  using namespace ieee;
+  if (es.n_items == 0) return MW_OK;
+  if (es.direction == MW_DIR_X)
+    k_ens_x_ieee<<<grid, kXT, 0, es.stream>>>(es);
+  else
+    k_ens_z_ieee<<<grid, kEnsZCols, 0, es.stream>>>(es);
+  return check_launch("ensemble IEEE-FP64 stage launch");
+}
+
+int ens_ieee_occupancy(int direction, int* blocks_per_sm) {
+  using namespace ieee;
+  cudaError_t e = direction == MW_DIR_X
+                      ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_ens_x_ieee, kXT, 0)
+                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_ens_z_ieee, kEnsZCols, 0);
+  if (e != cudaSuccess) return fail(MW_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
+  return MW_OK;
+}
+
+int launch_ens_ieee_rowtable(const double* hyc, const double* hytc, long long n, void* table, cudaStream_t stream) {
+  using namespace ieee;
+  if (n <= 0) return MW_OK;
+  MW_REQUIRE(((uintptr_t)table % 16) == 0, MW_ERR_ALIGN, "row table misaligned");
+  const long long blocks = std::min<long long>((n + 127) / 128, 4096);
+  k_ens_row_table_ieee<<<(unsigned)blocks, 128, 0, stream>>>(hyc, hytc, n, (RowD*)table);
+  return check_launch("ensemble row-table launch");
+}
 
 // One direction-stage in the IEEE-FP64 form over output rows [r0, r1) (the
 // whole grid: 0, nz); arguments validated by the caller.

@@ -9,7 +9,8 @@ orders) in a CUDA graph; `autotune()` picks the z tile height and the
 persistent grid sizes by timing candidates on the ensemble itself.
 
 Each member runs the arithmetic of `solve.evolve` on its own grid (the same
-tile code); FP64 members agree with single-grid runs to rounding level, FP32
+tile code); FP64 members (f64_mode "fp64", IEEE FP64, the default, or
+"split") agree with single-grid runs of the same form to rounding level, FP32
 members to FP32 rounding.  Members take no forcing term (no gravity-wave case).
 """
 from __future__ import annotations
@@ -59,12 +60,13 @@ def thermal_ensemble(n: int = 256, seed: int = 0, nx_range: Tuple[int, int] = (6
 class Ensemble:
     """Members [(params, bubbles or None)] in shared flat buffers on one GPU."""
 
-    def __init__(self, members: Sequence[tuple], dtype=torch.float64, f64_mode: str = "split", device=None,
+    def __init__(self, members: Sequence[tuple], dtype=torch.float64, f64_mode: str = "fp64", device=None,
                  z_tile: int = 64):
         if dtype not in (torch.float64, torch.float32):
             raise TypeError("dtype must be torch.float64 or torch.float32")
-        if dtype == torch.float64 and f64_mode != "split":
-            raise ValueError("ensembles with FP64 storage run the split form")
+        if dtype == torch.float64 and f64_mode not in ("fp64", "split"):
+            raise ValueError("ensembles with FP64 storage run f64_mode 'fp64' (IEEE FP64) or 'split'")
+        self.f64_mode = f64_mode if dtype == torch.float64 else None
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         if self.device.type != "cuda":
             raise ValueError("ensembles live on a CUDA device")
@@ -155,18 +157,24 @@ class Ensemble:
                 _native.ptr(self.state_tmp), _native.ptr(self.scratch), int(nsteps), ctypes.byref(rv)]
         stream = _native.stream_handle(self.device)
         if self.dtype == torch.float64:
-            _native.call("mw_ensemble_step_f64", *args, _native.MW_F64_SPLIT, _native.MW_FLAG_WRITE_HALO,
+            _native.call("mw_ensemble_step_f64", *args, _native.F64_MODES[self.f64_mode], _native.MW_FLAG_WRITE_HALO,
                          self.grid_x, self.grid_z, stream)
         else:
             _native.call("mw_ensemble_step_f32", *args, _native.MW_FLAG_WRITE_HALO, self.grid_x, self.grid_z, stream)
         self.reverse = rv.value
+
+    def _form(self) -> int:
+        """The kernel form of mw_ensemble_occupancy: 0 FP64 split, 1 FP32, 2 IEEE FP64."""
+        if self.dtype == torch.float32:
+            return 1
+        return 2 if self.f64_mode == "fp64" else 0
 
     def default_grids(self) -> Tuple[int, int]:
         sms = torch.cuda.get_device_properties(self.device).multi_processor_count
         out = []
         for d in (_native.MW_DIR_X, _native.MW_DIR_Z):
             b = ctypes.c_int(0)
-            _native.call("mw_ensemble_occupancy", int(self.dtype == torch.float32), d, ctypes.byref(b))
+            _native.call("mw_ensemble_occupancy", self._form(), d, ctypes.byref(b))
             out.append(max(1, b.value) * sms)
         return out[0], out[1]
 
@@ -202,7 +210,7 @@ class Ensemble:
     def autotune(self, z_tiles=(16, 32, 64), steps: int = 2, verbose: bool = False) -> dict:
         """Pick the z tile height and the persistent grid sizes by timing
         candidates on this ensemble (state restored afterwards)."""
-        key = (self.dtype, tuple((p["nx"], p["nz"]) for p in self.params),
+        key = (self.dtype, self.f64_mode, tuple((p["nx"], p["nz"]) for p in self.params),
                torch.cuda.get_device_name(self.device))
         if key in _TUNING_CACHE:
             self._apply(_TUNING_CACHE[key])

@@ -35,7 +35,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_status_strings_and_version():
     L = _native.load()
-    assert L.mw_abi_version() == 3
+    assert L.mw_abi_version() == 4
     for code in range(8):
         assert L.mw_status_string(code)
     assert L.mw_status_string(99) == b"unknown status"
@@ -65,6 +65,19 @@ def test_dirstage_validation():
     assert dirstage(init=0) == INVALID
     assert dirstage(direction=2) == INVALID
     assert dirstage(mode=5) == INVALID
+    assert dirstage(mode=3) == INVALID
+    L = _native.load()
+    bg = [P(FAKE)] * 5
+    # the pair-format flags: split form only, one at a time, PAIRS_OUT with init == forcing
+    st = L.mw_dirstage_f64(16, 8, 1.0, 1.0, 0.1, *bg, None, P(FAKE * 10), P(FAKE * 20), P(FAKE * 30), 0.1, 0, 2, 8,
+                           None)
+    assert st == INVALID
+    st = L.mw_dirstage_f64(16, 8, 1.0, 1.0, 0.1, *bg, None, P(FAKE * 10), P(FAKE * 20), P(FAKE * 30), 0.1, 0, 1, 8,
+                           None)
+    assert st == INVALID and b"init == forcing" in L.mw_last_error()
+    st = L.mw_dirstage_f64(16, 8, 1.0, 1.0, 0.1, *bg, None, P(FAKE * 10), P(FAKE * 20), P(FAKE * 30), 0.1, 0, 1, 24,
+                           None)
+    assert st == INVALID
     assert dirstage(init=FAKE * 10 + 4) == ALIGN
     assert dirstage(out=FAKE * 20) == ALIAS  # out == forcing
     assert dirstage(out=FAKE * 20 + 64) == ALIAS  # out overlaps forcing

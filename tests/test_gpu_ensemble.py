@@ -24,8 +24,8 @@ def small_members(seed=1):
     return out
 
 
-def single_run(p, bubbles, steps, dtype=torch.float64):
-    q = dict(p, f64_mode="split")
+def single_run(p, bubbles, steps, dtype=torch.float64, mode="fp64"):
+    q = dict(p, f64_mode=mode)
     f = initialize_fields(q, dtype=dtype)
     init(f, q, None, bubbles=bubbles)
     reset_direction()
@@ -40,35 +40,37 @@ def single_run(p, bubbles, steps, dtype=torch.float64):
 MEMBER_TOL = {torch.float64: 1e-12, torch.float32: 1e-5}
 
 
-@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
-def test_members_match_single_grid_runs(dtype):
+@pytest.mark.parametrize("dtype,mode", [(torch.float64, "fp64"), (torch.float64, "split"), (torch.float32, "fp64")])
+def test_members_match_single_grid_runs(dtype, mode):
     mem = small_members()
-    ens = Ensemble(mem, dtype=dtype)
+    ens = Ensemble(mem, dtype=dtype, f64_mode=mode)
     ens.step(10)
     for e, (p, bub) in enumerate(mem):
         got = ens.member_state(e).to(torch.float64).cpu().numpy()
-        ref = single_run(p, bub, 10, dtype)
+        ref = single_run(p, bub, 10, dtype, mode)
         err = max(normwise(got, ref, interior=False))
-        print("member %d %dx%d: max normwise vs single grid %.2e identical %s" % (
-            e, p["nx"], p["nz"], err, np.array_equal(got, ref)))
+        print("%s member %d %dx%d: max normwise vs single grid %.2e identical %s" % (
+            mode, e, p["nx"], p["nz"], err, np.array_equal(got, ref)))
         assert err <= MEMBER_TOL[dtype]
 
 
-def test_members_vs_oracle():
+@pytest.mark.parametrize("mode", ["fp64", "split"])
+def test_members_vs_oracle(mode):
     mem = small_members(seed=2)[:3]
-    ens = Ensemble(mem)
+    ens = Ensemble(mem, f64_mode=mode)
     ens.step(100)
     for e, (p, bub) in enumerate(mem):
         o = O.OracleSim(O.make_params(p["nx"], p["nz"], "thermal"), bubbles=bub)
         o.evolve(100)
         err = normwise(ens.member_state(e).cpu().numpy(), o.state)
-        print("member %d vs oracle after 100 steps: %s" % (e, ["%.2e" % v for v in err]))
+        print("%s member %d vs oracle after 100 steps: %s" % (mode, e, ["%.2e" % v for v in err]))
         assert max(err) <= TOL_STEP
 
 
-def test_graph_replay_equals_eager_steps():
+@pytest.mark.parametrize("mode", ["fp64", "split"])
+def test_graph_replay_equals_eager_steps(mode):
     mem = small_members(seed=3)
-    a, b = Ensemble(mem), Ensemble(mem)
+    a, b = Ensemble(mem, f64_mode=mode), Ensemble(mem, f64_mode=mode)
     replay = a.graph()
     for _ in range(3):
         replay()
@@ -91,12 +93,14 @@ def test_autotune_does_not_change_results():
 
 def test_uneven_thermal_ensemble_256():
     """The batching configuration: 256 thermal members, nx log-uniform in
-    [64, 1024], 100 steps, FP64 and FP32; three members are re-run alone."""
+    [64, 1024], 100 steps, FP64 (IEEE; and the split form) and FP32; three
+    members are re-run alone."""
     mem = thermal_ensemble(256, seed=0)
     e64 = Ensemble(mem, dtype=torch.float64)
+    e64s = Ensemble(mem, dtype=torch.float64, f64_mode="split")
     e32 = Ensemble(mem, dtype=torch.float32)
     m0 = [e64.member_stats(e)[0] for e in range(len(mem))]
-    for ens in (e64, e32):
+    for ens in (e64, e64s, e32):
         ens.autotune(steps=1)
         replay = ens.graph()
         for _ in range(50):
@@ -114,5 +118,8 @@ def test_uneven_thermal_ensemble_256():
     assert worst32 <= 1e-4
     for e in (0, 100, 255):
         p, bub = mem[e]
-        ref = single_run(p, bub, 100)
-        assert max(normwise(e64.member_state(e).cpu().numpy(), ref)) <= MEMBER_TOL[torch.float64]
+        for ens, mode in ((e64, "fp64"), (e64s, "split")):
+            ref = single_run(p, bub, 100, mode=mode)
+            assert max(normwise(ens.member_state(e).cpu().numpy(), ref)) <= MEMBER_TOL[torch.float64]
+        # the two FP64 forms agree with each other to the benchmark's tolerance
+        assert max(normwise(e64s.member_state(e).cpu().numpy(), e64.member_state(e).cpu().numpy())) <= TOL_STEP
