@@ -43,17 +43,23 @@ struct VjpArgs {
 
 __device__ __forceinline__ int wrap_x(int j, int nx) { return j < 0 ? j + nx : (j >= nx ? j - nx : j); }
 
+// Bounds-checked element access (MW_AT) to the arrays of one stage adjoint.
+#define MW_VF(a, off) MW_AT((a).forcing, (off), 4 * (a).plane)
+#define MW_VC(a, p, k) MW_AT((a).p, (k), (a).nz + 2 * kHs)  // cell-centre background
+#define MW_VI(a, p, k) MW_AT((a).p, (k), (a).nz + 1)        // interface background
+#define MW_WS(a, off) MW_AT((a).ws, (off), 8 * (a).nif)
+
 __device__ __forceinline__ double zval(const VjpArgs& a, int q, int k, int col) {
-  if (k >= 0 && k < a.nz) return a.forcing[q * a.plane + (long long)(k + kHs) * a.pitch + col];
+  if (k >= 0 && k < a.nz) return MW_VF(a, q * a.plane + (long long)(k + kHs) * a.pitch + col);
   if (q == WMOM) return 0.0;
   const int src = k < 0 ? kHs : a.nz + kHs - 1;
-  const double s = a.forcing[q * a.plane + (long long)src * a.pitch + col];
-  if (q == UMOM) return s / a.hyc[src] * a.hyc[k + kHs];
+  const double s = MW_VF(a, q * a.plane + (long long)src * a.pitch + col);
+  if (q == UMOM) return s / MW_VC(a, hyc, src) * MW_VC(a, hyc, k + kHs);
   return s;
 }
 
 __device__ __forceinline__ double gval(const VjpArgs& a, int q, int k, int i) {
-  return a.gout[q * a.plane + (long long)(k + kHs) * a.pitch + i + kHs];
+  return MW_AT(a.gout, q * a.plane + (long long)(k + kHs) * a.pitch + i + kHs, 4 * a.plane);
 }
 
 // tap weights of the interpolation (data/fields.py:94-97, convolution order
@@ -76,15 +82,15 @@ __global__ void k_vjp_iface(VjpArgs a) {
       const long long row = (long long)(k + kHs) * a.pitch;
       for (int j = 0; j < 4; ++j) {
         const long long col = wrap_x(i - 2 + j, a.nx) + kHs;
-        for (int q = 0; q < 4; ++q) s[q][j] = a.forcing[q * a.plane + row + col];
+        for (int q = 0; q < 4; ++q) s[q][j] = MW_VF(a, q * a.plane + row + col);
       }
       for (int q = 0; q < 4; ++q) {
         const double gr = i < a.nx ? gval(a, q, k, i) : 0.0;
         const double gl = i > 0 ? gval(a, q, k, i - 1) : 0.0;
         Fb[q] = a.dt_stage / a.d * (gr - gl);
       }
-      hy_r = a.hyc[k + kHs];
-      hy_rt = a.hytc[k + kHs];
+      hy_r = MW_VC(a, hyc, k + kHs);
+      hy_rt = MW_VC(a, hytc, k + kHs);
     } else {
       const int k = (int)(idx / a.nx), c = (int)(idx % a.nx);
       for (int j = 0; j < 4; ++j)
@@ -94,8 +100,8 @@ __global__ void k_vjp_iface(VjpArgs a) {
         const double gl = k > 0 ? gval(a, q, k - 1, c) : 0.0;
         Fb[q] = a.dt_stage / a.d * (gr - gl);
       }
-      hy_r = a.hyi[k];
-      hy_rt = a.hyti[k];
+      hy_r = MW_VI(a, hyi, k);
+      hy_rt = MW_VI(a, hyti, k);
       wall = (k == 0) || (k == a.nz);
     }
     double A[4];
@@ -124,8 +130,8 @@ __global__ void k_vjp_iface(VjpArgs a) {
       Db[DENS] = 0.0;
     }
     for (int q = 0; q < 4; ++q) {
-      a.ws[q * n + idx] = Ab[q];
-      a.ws[(4 + q) * n + idx] = Db[q];
+      MW_WS(a, q * n + idx) = Ab[q];
+      MW_WS(a, (4 + q) * n + idx) = Db[q];
     }
   }
 }
@@ -140,7 +146,7 @@ __global__ void k_vjp_gather(VjpArgs a) {
     const int kk = (int)(idx / a.pitch), ii = (int)(idx % a.pitch);
     const int k = kk - kHs, i = ii - kHs;
     if (k < 0 || k >= a.nz || i < 0 || i >= a.nx) {
-      for (int q = 0; q < 4; ++q) a.gdst[q * a.plane + idx] = 0.0;
+      for (int q = 0; q < 4; ++q) MW_AT(a.gdst, q * a.plane + idx, 4 * a.plane) = 0.0;
       continue;
     }
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
@@ -150,7 +156,7 @@ __global__ void k_vjp_gather(VjpArgs a) {
           const int f = i + 2 - j + m * a.nx;  // interface whose tap j is cell i
           if (f < 0 || f > a.nx) continue;
           const long long o = (long long)k * (a.nx + 1) + f;
-          for (int q = 0; q < 4; ++q) acc[q] += kC[j] * a.ws[q * n + o] + kE[j] * a.ws[(4 + q) * n + o];
+          for (int q = 0; q < 4; ++q) acc[q] += kC[j] * MW_WS(a, q * n + o) + kE[j] * MW_WS(a, (4 + q) * n + o);
         }
     } else {
       // taps t = f - 2 + j of interface f in [0, nz]; t maps to row k directly,
@@ -159,13 +165,13 @@ __global__ void k_vjp_gather(VjpArgs a) {
         if (f < 0 || f > a.nz) continue;
         const int j = k - f + 2;
         const long long o = (long long)f * a.nx + i;
-        for (int q = 0; q < 4; ++q) acc[q] += kC[j] * a.ws[q * n + o] + kE[j] * a.ws[(4 + q) * n + o];
+        for (int q = 0; q < 4; ++q) acc[q] += kC[j] * MW_WS(a, q * n + o) + kE[j] * MW_WS(a, (4 + q) * n + o);
       }
       auto halo_taps = [&](int t, double wq[4]) {  // weight of halo row t on row k
         const int src = t < 0 ? 0 : a.nz - 1;
         wq[DENS] = wq[RHOT] = (k == src) ? 1.0 : 0.0;
         wq[WMOM] = 0.0;
-        wq[UMOM] = (k == src) ? a.hyc[t + kHs] / a.hyc[src + kHs] : 0.0;
+        wq[UMOM] = (k == src) ? MW_VC(a, hyc, t + kHs) / MW_VC(a, hyc, src + kHs) : 0.0;
       };
       const int halo_rows[4] = {-2, -1, a.nz, a.nz + 1};
       for (int h = 0; h < 4; ++h) {
@@ -178,7 +184,7 @@ __global__ void k_vjp_gather(VjpArgs a) {
           if (f < 0 || f > a.nz) continue;
           const long long o = (long long)f * a.nx + i;
           for (int q = 0; q < 4; ++q)
-            acc[q] += wq[q] * (kC[j] * a.ws[q * n + o] + kE[j] * a.ws[(4 + q) * n + o]);
+            acc[q] += wq[q] * (kC[j] * MW_WS(a, q * n + o) + kE[j] * MW_WS(a, (4 + q) * n + o));
         }
       }
       acc[DENS] -= a.dt_stage * kGrav * gval(a, WMOM, k, i);
@@ -186,10 +192,10 @@ __global__ void k_vjp_gather(VjpArgs a) {
     for (int q = 0; q < 4; ++q) {
       const long long o = q * a.plane + idx;
       double v = acc[q];
-      if (a.add_gout) v += a.gout[o];
-      if (a.base_a) v += a.base_a[o];
-      if (a.base_b) v += a.base_b[o];
-      a.gdst[o] = v;
+      if (a.add_gout) v += MW_AT(a.gout, o, 4 * a.plane);
+      if (a.base_a) v += MW_AT(a.base_a, o, 4 * a.plane);
+      if (a.base_b) v += MW_AT(a.base_b, o, 4 * a.plane);
+      MW_AT(a.gdst, o, 4 * a.plane) = v;
     }
   }
 }
@@ -206,6 +212,10 @@ long long n_interfaces(int nx, int nz, int dir) {
 }
 
 }  // namespace
+
+#if MW_CHECK
+MW_OOB_COUNTER(oob_count_adjoint)
+#endif
 
 // mw_adjoint_split.cu
 int launch_vjp_row_table(int nx, int nz, const double* hyc, const double* hytc, const double* hyi, const double* hyti,

@@ -109,7 +109,7 @@ __global__ void k_init_state(int nx, int nz, double dx, double dz, int bg, doubl
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q)
-      state[q * plane + (long long)k * NX + i] = (T)add_(add_(acc[q][0], acc[q][1]), acc[q][2]);
+      MW_AT(state, q * plane + (long long)k * NX + i, 4 * plane) = (T)add_(add_(acc[q][0], acc[q][1]), acc[q][2]);
   }
 }
 
@@ -122,15 +122,15 @@ __global__ void k_init_background(int nz, double dz, int bg, double* hyc, double
     double hr, ht;
     hydro(bg, z, &hr, &ht);
     const double sumw = add_(add_(c_qw[0], c_qw[1]), c_qw[2]);
-    hyc[k] = mul_(hr, sumw);
+    MW_AT(hyc, k, NZ) = mul_(hr, sumw);
     const double a = mul_(ht, hr);
-    hytc[k] = add_(add_(mul_(a, c_qw[0]), mul_(a, c_qw[1])), mul_(a, c_qw[2]));
+    MW_AT(hytc, k, NZ) = add_(add_(mul_(a, c_qw[0]), mul_(a, c_qw[1])), mul_(a, c_qw[2]));
     if (k <= nz) {
       const double ze = linspace_at(0.0, (nz + 1) * dz, nz + 1, k);
       hydro(bg, ze, &hr, &ht);
-      hyi[k] = hr;
-      hyti[k] = mul_(hr, ht);
-      hypi[k] = mul_(kC0, pow(mul_(hr, ht), kGamma));
+      MW_AT(hyi, k, nz + 1) = hr;
+      MW_AT(hyti, k, nz + 1) = mul_(hr, ht);
+      MW_AT(hypi, k, nz + 1) = mul_(kC0, pow(mul_(hr, ht), kGamma));
     }
   }
 }
@@ -144,7 +144,7 @@ __global__ void k_gravity_source(int nx, int nz, double xlen, double zlen, const
     const int k = (int)(idx / nx), i = (int)(idx % nx);
     const double z = linspace_at(dz / 2.0, zlen + dz / 2.0, nz, k);
     const double x = linspace_at(dx / 2.0, xlen + dx / 2.0, nx, i);
-    src[idx] = mul_(ellipse_cos2(x, z, B), hyc[k + kHs]);
+    MW_AT(src, idx, n) = mul_(ellipse_cos2(x, z, B), MW_AT(hyc, k + kHs, nz + 2 * kHs));
   }
 }
 
@@ -199,13 +199,13 @@ __global__ void __launch_bounds__(kStatThreads) k_stats_partial(int nx, int nz, 
   const int k0 = blockIdx.x * rpb, k1 = min(k0 + rpb, nz);
   for (int k = k0; k < k1; ++k) {
     const int kk = k + kHs;
-    const double hr = hyc[kk], hrt = hytc[kk];
+    const double hr = MW_AT(hyc, kk, nz + 2 * kHs), hrt = MW_AT(hytc, kk, nz + 2 * kHs);
     for (int i = threadIdx.x; i < nx; i += kStatThreads) {
       const long long o = (long long)kk * NX + i + kHs;
-      const double rho = add_(load_state(state + o), hr);
-      const double u = div_(load_state(state + plane + o), rho);
-      const double w = div_(load_state(state + 2 * plane + o), rho);
-      const double th = div_(add_(load_state(state + 3 * plane + o), hrt), rho);
+      const double rho = add_(load_state(&MW_AT(state, o, 4 * plane)), hr);
+      const double u = div_(load_state(&MW_AT(state, plane + o, 4 * plane)), rho);
+      const double w = div_(load_state(&MW_AT(state, 2 * plane + o, 4 * plane)), rho);
+      const double th = div_(add_(load_state(&MW_AT(state, 3 * plane + o, 4 * plane)), hrt), rho);
       const double p = mul_(kC0, pow(mul_(rho, th), kGamma));
       const double t = div_(th, pow(div_(kP0, p), kRd / kCp));
       const double ke = mul_(rho, add_(mul_(u, u), mul_(w, w)));
@@ -216,8 +216,8 @@ __global__ void __launch_bounds__(kStatThreads) k_stats_partial(int nx, int nz, 
   }
   block_sum2<kStatThreads>(m, e, sm, se);
   if (threadIdx.x == 0) {
-    part[2 * blockIdx.x] = m;
-    part[2 * blockIdx.x + 1] = e;
+    MW_AT(part, 2 * blockIdx.x, 2 * gridDim.x) = m;
+    MW_AT(part, 2 * blockIdx.x + 1, 2 * gridDim.x) = e;
   }
 }
 
@@ -225,12 +225,12 @@ __global__ void __launch_bounds__(kStatMaxBlocks) k_stats_final(int nblocks, dou
                                                                 double* out2) {
   __shared__ double sm[kStatMaxBlocks / 32], se[kStatMaxBlocks / 32];
   const int t = threadIdx.x;
-  double m = t < nblocks ? part[2 * t] : 0.0;
-  double e = t < nblocks ? part[2 * t + 1] : 0.0;
+  double m = t < nblocks ? MW_AT(part, 2 * t, 2 * nblocks) : 0.0;
+  double e = t < nblocks ? MW_AT(part, 2 * t + 1, 2 * nblocks) : 0.0;
   block_sum2<kStatMaxBlocks>(m, e, sm, se);
   if (t == 0) {
-    out2[0] = mul_(mul_(m, dx), dz);
-    out2[1] = mul_(mul_(e, dx), dz);
+    MW_AT(out2, 0, 2) = mul_(mul_(m, dx), dz);
+    MW_AT(out2, 1, 2) = mul_(mul_(e, dx), dz);
   }
 }
 
@@ -270,12 +270,13 @@ __global__ void k_solution_vars(int nx, int nz, const double* hyc, const double*
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n; idx += (long long)gridDim.x * blockDim.x) {
     const int k = (int)(idx / nx), i = (int)(idx % nx);
     const long long o = (long long)(k + kHs) * NX + i + kHs;
-    const double hr = hyc[k + kHs], hrt = hytc[k + kHs];
-    const double d = state[o];
-    out[idx] = d;
-    out[n + idx] = div_(state[plane + o], add_(hr, d));
-    out[2 * n + idx] = div_(state[2 * plane + o], add_(hr, d));
-    out[3 * n + idx] = sub_(div_(add_(state[3 * plane + o], hrt), add_(hr, d)), div_(hrt, hr));
+    const double hr = MW_AT(hyc, k + kHs, nz + 2 * kHs), hrt = MW_AT(hytc, k + kHs, nz + 2 * kHs);
+    const double d = MW_AT(state, o, 4 * plane);
+    MW_AT(out, idx, 4 * n) = d;
+    MW_AT(out, n + idx, 4 * n) = div_(MW_AT(state, plane + o, 4 * plane), add_(hr, d));
+    MW_AT(out, 2 * n + idx, 4 * n) = div_(MW_AT(state, 2 * plane + o, 4 * plane), add_(hr, d));
+    MW_AT(out, 3 * n + idx, 4 * n) = sub_(div_(add_(MW_AT(state, 3 * plane + o, 4 * plane), hrt), add_(hr, d)),
+                                          div_(hrt, hr));
   }
 }
 
@@ -289,23 +290,25 @@ __global__ void k_set_bc(int nx, int nz, const double* hyc, double* f, int dir) 
     for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
          idx += (long long)gridDim.x * blockDim.x) {
       const int q = (int)(idx / nz), k = (int)(idx % nz);
-      double* row = f + q * plane + (long long)(k + kHs) * NX;
-      row[0] = row[nx];
-      row[1] = row[nx + 1];
-      row[nx + kHs] = row[kHs];
-      row[nx + kHs + 1] = row[kHs + 1];
+      const long long row = q * plane + (long long)(k + kHs) * NX;
+      auto at = [&](int c) -> double& { return MW_AT(f, row + c, 4 * plane); };
+      at(0) = at(nx);
+      at(1) = at(nx + 1);
+      at(nx + kHs) = at(kHs);
+      at(nx + kHs + 1) = at(kHs + 1);
     }
   } else {  // ics/bcs.py:92-148, all nx+4 columns
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < NX; c += gridDim.x * blockDim.x) {
-      auto at = [&](int q, int r) -> double& { return f[q * plane + (long long)r * NX + c]; };
+      auto at = [&](int q, int r) -> double& { return MW_AT(f, q * plane + (long long)r * NX + c, 4 * plane); };
+      auto hc = [&](int r) { return MW_AT(hyc, r, nz + 2 * kHs); };
       at(WMOM, 0) = 0.0;
       at(WMOM, 1) = 0.0;
       at(WMOM, nz + kHs) = 0.0;
       at(WMOM, nz + kHs + 1) = 0.0;
-      at(UMOM, 0) = mul_(div_(at(UMOM, kHs), hyc[kHs]), hyc[0]);
-      at(UMOM, 1) = mul_(div_(at(UMOM, kHs), hyc[kHs]), hyc[1]);
-      at(UMOM, nz + kHs) = mul_(div_(at(UMOM, nz + kHs - 1), hyc[nz + kHs - 1]), hyc[nz + kHs]);
-      at(UMOM, nz + kHs + 1) = mul_(div_(at(UMOM, nz + kHs - 1), hyc[nz + kHs - 1]), hyc[nz + kHs + 1]);
+      at(UMOM, 0) = mul_(div_(at(UMOM, kHs), hc(kHs)), hc(0));
+      at(UMOM, 1) = mul_(div_(at(UMOM, kHs), hc(kHs)), hc(1));
+      at(UMOM, nz + kHs) = mul_(div_(at(UMOM, nz + kHs - 1), hc(nz + kHs - 1)), hc(nz + kHs));
+      at(UMOM, nz + kHs + 1) = mul_(div_(at(UMOM, nz + kHs - 1), hc(nz + kHs - 1)), hc(nz + kHs + 1));
       for (int q = 0; q < 4; q += 3) {  // DENS and RHOT
         at(q, 0) = at(q, kHs);
         at(q, 1) = at(q, kHs);
@@ -335,15 +338,13 @@ __global__ void k_interpolate(int nx, int nz, const double* s, double* vals, dou
     const int q = (int)(idx / ((long long)nk * ni));
     const int r = (int)((idx / ni) % nk), i = (int)(idx % ni);
     double t[4];
-    if (dir == MW_DIR_X) {
-      const double* row = s + q * plane + (long long)(r + kHs) * NX + i;
-      t[0] = row[0]; t[1] = row[1]; t[2] = row[2]; t[3] = row[3];
-    } else {
-      const double* col = s + q * plane + (long long)r * NX + i + kHs;
-      t[0] = col[0]; t[1] = col[NX]; t[2] = col[2 * NX]; t[3] = col[3 * NX];
-    }
-    vals[idx] = interp4_rn(t[0], t[1], t[2], t[3]);
-    d3[idx] = diff3_rn(t[0], t[1], t[2], t[3]);
+    const long long base = dir == MW_DIR_X ? q * plane + (long long)(r + kHs) * NX + i
+                                           : q * plane + (long long)r * NX + i + kHs;
+    const long long step = dir == MW_DIR_X ? 1 : NX;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) t[j] = MW_AT(s, base + j * step, 4 * plane);
+    MW_AT(vals, idx, n) = interp4_rn(t[0], t[1], t[2], t[3]);
+    MW_AT(d3, idx, n) = diff3_rn(t[0], t[1], t[2], t[3]);
   }
 }
 
@@ -367,35 +368,36 @@ __global__ void k_flux(FluxArgs a) {
     const int r = (int)(idx / ni), i = (int)(idx % ni);
     double v[4], d[4];
     for (int q = 0; q < 4; ++q) {
-      v[q] = a.vals[q * vplane + idx];
-      d[q] = a.d3[q * vplane + idx];
+      v[q] = MW_AT(a.vals, q * vplane + idx, 4 * vplane);
+      d[q] = MW_AT(a.d3, q * vplane + idx, 4 * vplane);
     }
     const long long fo = (long long)r * (a.nx + 1) + i;
+    auto F = [&](int q) -> double& { return MW_AT(a.flux, q * fplane + fo, 4 * fplane); };
     if (a.dir == MW_DIR_X) {  // interpolate.py:105-129
-      const double rho = add_(v[DENS], a.hyc[r + kHs]);
+      const double rho = add_(v[DENS], MW_AT(a.hyc, r + kHs, a.nz + 2 * kHs));
       const double u = div_(v[UMOM], rho);
       const double w = div_(v[WMOM], rho);
-      const double t = div_(add_(v[RHOT], a.hytc[r + kHs]), rho);
+      const double t = div_(add_(v[RHOT], MW_AT(a.hytc, r + kHs, a.nz + 2 * kHs)), rho);
       const double p = mul_(kC0, pow(mul_(rho, t), kGamma));
-      a.flux[0 * fplane + fo] = sub_(mul_(rho, u), mul_(a.hv, d[DENS]));
-      a.flux[1 * fplane + fo] = sub_(add_(mul_(rho, mul_(u, u)), p), mul_(a.hv, d[UMOM]));
-      a.flux[2 * fplane + fo] = sub_(mul_(mul_(rho, u), w), mul_(a.hv, d[WMOM]));
-      a.flux[3 * fplane + fo] = sub_(mul_(mul_(rho, u), t), mul_(a.hv, d[RHOT]));
+      F(0) = sub_(mul_(rho, u), mul_(a.hv, d[DENS]));
+      F(1) = sub_(add_(mul_(rho, mul_(u, u)), p), mul_(a.hv, d[UMOM]));
+      F(2) = sub_(mul_(mul_(rho, u), w), mul_(a.hv, d[WMOM]));
+      F(3) = sub_(mul_(mul_(rho, u), t), mul_(a.hv, d[RHOT]));
     } else {  // interpolate.py:153-186
-      const double rho = add_(v[DENS], a.hyi[r]);
+      const double rho = add_(v[DENS], MW_AT(a.hyi, r, a.nz + 1));
       const double u = div_(v[UMOM], rho);
       double w = div_(v[WMOM], rho);
-      const double t = div_(add_(v[RHOT], a.hyti[r]), rho);
-      const double p = sub_(mul_(kC0, pow(mul_(rho, t), kGamma)), a.hypi[r]);
+      const double t = div_(add_(v[RHOT], MW_AT(a.hyti, r, a.nz + 1)), rho);
+      const double p = sub_(mul_(kC0, pow(mul_(rho, t), kGamma)), MW_AT(a.hypi, r, a.nz + 1));
       if (r == 0 || r == a.nz) {
         w = 0.0;
         d[DENS] = 0.0;
-        a.d3[DENS * vplane + idx] = 0.0;
+        MW_AT(a.d3, DENS * vplane + idx, 4 * vplane) = 0.0;
       }
-      a.flux[0 * fplane + fo] = sub_(mul_(rho, w), mul_(a.hv, d[DENS]));
-      a.flux[1 * fplane + fo] = sub_(mul_(mul_(rho, w), u), mul_(a.hv, d[UMOM]));
-      a.flux[2 * fplane + fo] = sub_(add_(mul_(rho, mul_(w, w)), p), mul_(a.hv, d[WMOM]));
-      a.flux[3 * fplane + fo] = sub_(mul_(mul_(rho, w), t), mul_(a.hv, d[RHOT]));
+      F(0) = sub_(mul_(rho, w), mul_(a.hv, d[DENS]));
+      F(1) = sub_(mul_(mul_(rho, w), u), mul_(a.hv, d[UMOM]));
+      F(2) = sub_(add_(mul_(rho, mul_(w, w)), p), mul_(a.hv, d[WMOM]));
+      F(3) = sub_(mul_(mul_(rho, w), t), mul_(a.hv, d[RHOT]));
     }
   }
 }
@@ -412,11 +414,11 @@ __global__ void k_tend(int nx, int nz, double d, const double* flux, const doubl
     const long long f0 = (long long)k * (nx + 1) + i;
     const long long f1 = dir == MW_DIR_X ? f0 + 1 : f0 + (nx + 1);
     for (int q = 0; q < 4; ++q) {
-      double t = div_(-sub_(flux[q * fplane + f1], flux[q * fplane + f0]), d);
+      double t = div_(-sub_(MW_AT(flux, q * fplane + f1, 4 * fplane), MW_AT(flux, q * fplane + f0, 4 * fplane)), d);
       if (q == WMOM && dir == MW_DIR_Z)
-        t = sub_(t, mul_(forcing[DENS * splane + (long long)(k + kHs) * NX + i + kHs], kGrav));
-      if (q == WMOM && srcw) t = add_(t, srcw[idx]);
-      tend[q * tplane + idx] = t;
+        t = sub_(t, mul_(MW_AT(forcing, DENS * splane + (long long)(k + kHs) * NX + i + kHs, 4 * splane), kGrav));
+      if (q == WMOM && srcw) t = add_(t, MW_AT(srcw, idx, tplane));
+      MW_AT(tend, q * tplane + idx, 4 * tplane) = t;
     }
   }
 }
@@ -431,7 +433,7 @@ __global__ void k_update(int nx, int nz, const double* init, const double* tend,
     const long long r = idx % tplane;
     const int k = (int)(r / nx), i = (int)(r % nx);
     const long long o = q * splane + (long long)(k + kHs) * NX + i + kHs;
-    out[o] = add_(init[o], mul_(dt, tend[idx]));
+    MW_AT(out, o, 4 * splane) = add_(MW_AT(init, o, 4 * splane), mul_(dt, MW_AT(tend, idx, 4 * tplane)));
   }
 }
 
@@ -439,7 +441,8 @@ __global__ void k_add_source(int nx, int nz, const double* srcw, double* tend) {
   const long long tplane = (long long)nz * nx;
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < tplane;
        idx += (long long)gridDim.x * blockDim.x)
-    tend[WMOM * tplane + idx] = add_(tend[WMOM * tplane + idx], srcw[idx]);
+    MW_AT(tend, WMOM * tplane + idx, 4 * tplane) =
+        add_(MW_AT(tend, WMOM * tplane + idx, 4 * tplane), MW_AT(srcw, idx, tplane));
 }
 
 inline unsigned grid_for(long long n, int threads) {
@@ -642,7 +645,7 @@ __global__ void k_count_nonfinite(int nx, int nz, const T* s, unsigned long long
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
     const long long q = e / ((long long)nz * nx), r = e - q * nz * nx;
     const int k = (int)(r / nx), i = (int)(r - (long long)k * nx);
-    const T v = s[q * plane + (long long)(k + kHs) * pitch + i + kHs];
+    const T v = MW_AT(s, q * plane + (long long)(k + kHs) * pitch + i + kHs, 4 * plane);
     c += !isfinite(v);
   }
   for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
@@ -688,6 +691,10 @@ int check_finite_blocking(int nx, int nz, const T* state, void* counter8, cudaSt
 }
 template int check_finite_blocking<double>(int, int, const double*, void*, cudaStream_t);
 template int check_finite_blocking<float>(int, int, const float*, void*, cudaStream_t);
+
+#if MW_CHECK
+MW_OOB_COUNTER(oob_count_aux)
+#endif
 }  // namespace mw
 
 extern "C" int mw_count_nonfinite_f64(int nx, int nz, const double* state, unsigned long long* count, void* stream) {

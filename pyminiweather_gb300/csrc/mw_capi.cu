@@ -61,6 +61,9 @@ namespace mw {
 int oob_count_split_stage(unsigned long long* out, bool reset);
 int oob_count_adjoint_split(unsigned long long* out, bool reset);
 int oob_count_ieee_stage(unsigned long long* out, bool reset);
+int oob_count_dirstage(unsigned long long* out, bool reset);
+int oob_count_aux(unsigned long long* out, bool reset);
+int oob_count_adjoint(unsigned long long* out, bool reset);
 namespace {
 __global__ void k_oob_selftest(double* p, int n) { MW_AT(p, n, n) = 1.0; }  // one index past the end
 }  // namespace
@@ -74,7 +77,9 @@ extern "C" int mw_debug_oob_count(unsigned long long* count, int reset) {
 #if MW_CHECK
   int st;
   if ((st = mw::oob_count_split_stage(count, reset != 0)) || (st = mw::oob_count_adjoint_split(count, reset != 0)) ||
-      (st = mw::oob_count_ieee_stage(count, reset != 0)) || (st = mw::oob_count_capi(count, reset != 0)))
+      (st = mw::oob_count_ieee_stage(count, reset != 0)) || (st = mw::oob_count_dirstage(count, reset != 0)) ||
+      (st = mw::oob_count_aux(count, reset != 0)) || (st = mw::oob_count_adjoint(count, reset != 0)) ||
+      (st = mw::oob_count_capi(count, reset != 0)))
     return st;
   return MW_OK;
 #else

@@ -22,7 +22,7 @@ namespace mw {
 
 #if MW_CHECK
 static __device__ unsigned long long g_oob_count;           // per translation unit
-static __device__ __align__(16) unsigned char g_oob_sink[64];  // stands in for out-of-range elements
+static __device__ __align__(16) unsigned char g_oob_sink[128];  // stands in for out-of-range elements
 
 template <typename T, typename I>
 __device__ __forceinline__ T& checked_at(T* p, I i, long long n) {

@@ -57,6 +57,14 @@ struct StageArgs {
   float dt_f;       // dt_stage
 };
 
+// Bounds-checked element access (MW_AT) to the arrays of one stage.
+#define MW_SF(a, off) MW_AT((a).forcing, (off), 4 * (a).plane)
+#define MW_SI(a, off) MW_AT((a).init, (off), 4 * (a).plane)
+#define MW_SO(a, off) MW_AT((a).out, (off), 4 * (a).plane)
+#define MW_BC(a, p, k) MW_AT((a).p, (k), (a).nz + 2 * kHs)  // cell-centre background
+#define MW_BI(a, p, k) MW_AT((a).p, (k), (a).nz + 1)        // interface background
+#define MW_SW(a, off) MW_AT((a).srcw, (off), (long long)(a).nx * (a).nz)
+
 template <typename T>
 __host__ __device__ inline void set_f32_constants(StageArgs<T>& a, int direction) {
   a.hv_f = float(a.hv);
@@ -199,11 +207,11 @@ __device__ __forceinline__ int wrap_x(int j, int nx) { return j < 0 ? j + nx : (
 // [-2, nz+1] of the halo-indexed column col.
 template <typename T>
 __device__ __forceinline__ T zval(const StageArgs<T>& a, int q, int k, int col) {
-  if (k >= 0 && k < a.nz) return a.forcing[q * a.plane + (long long)(k + kHs) * a.pitch + col];
+  if (k >= 0 && k < a.nz) return MW_SF(a, q * a.plane + (long long)(k + kHs) * a.pitch + col);
   if (q == WMOM) return T(0);
   const int src = k < 0 ? kHs : a.nz + kHs - 1;  // halo-indexed source row
-  T s = a.forcing[q * a.plane + (long long)src * a.pitch + col];
-  if (q == UMOM) return T((double)s / a.hyc[src] * a.hyc[k + kHs]);
+  T s = MW_SF(a, q * a.plane + (long long)src * a.pitch + col);
+  if (q == UMOM) return T((double)s / MW_BC(a, hyc, src) * MW_BC(a, hyc, k + kHs));
   return s;
 }
 
@@ -216,7 +224,7 @@ __device__ __forceinline__ void write_z_halo_column(const StageArgs<T>& a, int c
 #pragma unroll
     for (int r = 0; r < 4; ++r) vals[r] = zval(a, q, rows[r], col);
 #pragma unroll
-    for (int r = 0; r < 4; ++r) a.forcing[q * a.plane + (long long)(rows[r] + kHs) * a.pitch + col] = vals[r];
+    for (int r = 0; r < 4; ++r) MW_SF(a, q * a.plane + (long long)(rows[r] + kHs) * a.pitch + col) = vals[r];
   }
 }
 
@@ -259,13 +267,13 @@ __device__ __forceinline__ void x_rowrun_t(const StageArgs<T>& a, int k, int cbe
   const int t = threadIdx.x;
   const long long row = (long long)(k + kHs) * a.pitch;
   if constexpr (MODE != MODE_NATIVE64) {
-    if (t == 0) sm.row = rowf_x(a.hyc[k + kHs], a.hytc[k + kHs]);
+    if (t == 0) sm.row = rowf_x(MW_BC(a, hyc, k + kHs), MW_BC(a, hytc, k + kHs));
   }
   if (halo && t < 4) {
     const int dst[4] = {0, 1, a.nx + kHs, a.nx + kHs + 1};
     const int src[4] = {a.nx, a.nx + 1, kHs, kHs + 1};
 #pragma unroll
-    for (int q = 0; q < 4; ++q) a.forcing[q * a.plane + row + dst[t]] = a.forcing[q * a.plane + row + src[t]];
+    for (int q = 0; q < 4; ++q) MW_SF(a, q * a.plane + row + dst[t]) = MW_SF(a, q * a.plane + row + src[t]);
   }
   __syncthreads();
   for (int chunk = cbeg; chunk < cend; ++chunk) {
@@ -276,7 +284,7 @@ __device__ __forceinline__ void x_rowrun_t(const StageArgs<T>& a, int k, int cbe
     T iv[4];
     if (upd) {  // issued before the flux so the load latency is covered
 #pragma unroll
-      for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
+      for (int q = 0; q < 4; ++q) iv[q] = MW_SI(a, q * a.plane + o);
     }
     if (i <= a.nx) {
       T s[4][4];
@@ -284,11 +292,11 @@ __device__ __forceinline__ void x_rowrun_t(const StageArgs<T>& a, int k, int cbe
       for (int j = 0; j < 4; ++j) {
         const long long col = wrap_x(i - 2 + j, a.nx) + kHs;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) s[q][j] = __ldg(a.forcing + q * a.plane + row + col);
+        for (int q = 0; q < 4; ++q) s[q][j] = __ldg(&MW_SF(a, q * a.plane + row + col));
       }
       T F[4];
       if constexpr (MODE == MODE_NATIVE64) {
-        flux_x_native(s, a.hyc[k + kHs], a.hytc[k + kHs], a.hv, F);
+        flux_x_native(s, MW_BC(a, hyc, k + kHs), MW_BC(a, hytc, k + kHs), a.hv, F);
       } else {
         flux_x_f32(s, sm.row, a.hv_f, F);
       }
@@ -301,17 +309,17 @@ __device__ __forceinline__ void x_rowrun_t(const StageArgs<T>& a, int k, int cbe
         double tend[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) tend[q] = -(sm.sF[q][t + 1] - sm.sF[q][t]) / a.dx;
-        if (a.srcw) tend[WMOM] = tend[WMOM] + a.srcw[(long long)k * a.nx + i];
+        if (a.srcw) tend[WMOM] = tend[WMOM] + MW_SW(a, (long long)k * a.nx + i);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = iv[q] + a.dt_stage * tend[q];
+        for (int q = 0; q < 4; ++q) MW_SO(a, q * a.plane + o) = iv[q] + a.dt_stage * tend[q];
       } else {
         const float c = a.c_f, dt = a.dt_f;
         float inc[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) inc[q] = (sm.sF[q][t] - sm.sF[q][t + 1]) * c;
-        if (a.srcw) inc[WMOM] += dt * split::d2f(a.srcw[(long long)k * a.nx + i]);
+        if (a.srcw) inc[WMOM] += dt * split::d2f(MW_SW(a, (long long)k * a.nx + i));
 #pragma unroll
-        for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = iv[q] + inc[q];
+        for (int q = 0; q < 4; ++q) MW_SO(a, q * a.plane + o) = iv[q] + inc[q];
       }
     }
     __syncthreads();
@@ -328,7 +336,7 @@ __device__ __forceinline__ void z_tile_t(const StageArgs<T>& a, int cb, int z0, 
   if constexpr (MODE != MODE_NATIVE64) {
     for (int r = threadIdx.x; r <= z1 - z0; r += NC) {
       const int k = z0 + r;
-      sm.row[r] = rowf_z(a.hyi[k], a.hyti[k], a.hypi[k]);
+      sm.row[r] = rowf_z(MW_BI(a, hyi, k), MW_BI(a, hyti, k), MW_BI(a, hypi, k));
     }
     __syncthreads();
   }
@@ -348,7 +356,7 @@ __device__ __forceinline__ void z_tile_t(const StageArgs<T>& a, int cb, int z0, 
     auto flux_at = [&](int k, T F[4]) {
       const bool wall = (k == 0) || (k == a.nz);
       if constexpr (MODE == MODE_NATIVE64) {
-        flux_z_native(w, a.hyi[k], a.hyti[k], a.hypi[k], a.hv, wall, F);
+        flux_z_native(w, MW_BI(a, hyi, k), MW_BI(a, hyti, k), MW_BI(a, hypi, k), a.hv, wall, F);
       } else {
         flux_z_f32(w, sm.row[k - z0], a.hv_f, wall, F);
       }
@@ -362,7 +370,7 @@ __device__ __forceinline__ void z_tile_t(const StageArgs<T>& a, int cb, int z0, 
       const long long o = (long long)(k + kHs) * a.pitch + col;
       T iv[4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
+      for (int q = 0; q < 4; ++q) iv[q] = MW_SI(a, q * a.plane + o);
       const T rho_k = w[DENS][2];  // forcing rho' at cell k (interpolate.py:248-250)
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
@@ -382,18 +390,18 @@ __device__ __forceinline__ void z_tile_t(const StageArgs<T>& a, int cb, int z0, 
 #pragma unroll
         for (int q = 0; q < 4; ++q) tend[q] = -(Fn[q] - Fp[q]) / a.dz;
         tend[WMOM] = tend[WMOM] - rho_k * kGrav;
-        if (a.srcw) tend[WMOM] = tend[WMOM] + a.srcw[(long long)k * a.nx + c];
+        if (a.srcw) tend[WMOM] = tend[WMOM] + MW_SW(a, (long long)k * a.nx + c);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = iv[q] + a.dt_stage * tend[q];
+        for (int q = 0; q < 4; ++q) MW_SO(a, q * a.plane + o) = iv[q] + a.dt_stage * tend[q];
       } else {
         const float cz = a.c_f, dt = a.dt_f;
         float inc[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) inc[q] = (Fp[q] - Fn[q]) * cz;
         inc[WMOM] -= dt * (rho_k * float(kGrav));
-        if (a.srcw) inc[WMOM] += dt * split::d2f(a.srcw[(long long)k * a.nx + c]);
+        if (a.srcw) inc[WMOM] += dt * split::d2f(MW_SW(a, (long long)k * a.nx + c));
 #pragma unroll
-        for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = iv[q] + inc[q];
+        for (int q = 0; q < 4; ++q) MW_SO(a, q * a.plane + o) = iv[q] + inc[q];
       }
 #pragma unroll
       for (int q = 0; q < 4; ++q) Fp[q] = Fn[q];
@@ -424,7 +432,7 @@ __global__ void __launch_bounds__(kZThreads) k_stage_z(StageArgs<T> a, int tile0
 // ---------------------------------------------------------------------------
 // Ensemble (FP32 storage): one persistent launch per stage over all members.
 __device__ StageArgs<float> member_args_f32(const EnsStageT<float>& es, int e) {
-  const mw_ens_member m = es.members[e];
+  const mw_ens_member m = MW_AT(es.members, e, es.n_members);
   StageArgs<float> a;
   a.nx = m.nx;
   a.nz = m.nz;
@@ -447,7 +455,8 @@ __device__ StageArgs<float> member_args_f32(const EnsStageT<float>& es, int e) {
   a.chunks_per_block = 0;
   a.z_tile = es.z_tile;
   // hv_f, c_f, dt_f from the plan (formed on the host as set_f32_constants forms them)
-  const EnsMemberConsts& c = reinterpret_cast<const EnsMemberConsts*>(es.mconsts)[mconsts_index(es, e)];
+  const EnsMemberConsts& c = MW_AT(reinterpret_cast<const EnsMemberConsts*>(es.mconsts), mconsts_index(es, e),
+                                   (long long)kEnsConstsPerMember * es.n_members);
   a.hv_f = c.hv_f;
   a.c_f = c.c_f;
   a.dt_f = c.dt_f;
@@ -462,12 +471,12 @@ constexpr int kF32WCells = 31;
 
 __device__ __forceinline__ void x_row_warp_f32(const StageArgs<float>& a, int k, bool halo) {
   const int lane = threadIdx.x & 31;
-  const RowF r = rowf_x(a.hyc[k + kHs], a.hytc[k + kHs]);
+  const RowF r = rowf_x(MW_BC(a, hyc, k + kHs), MW_BC(a, hytc, k + kHs));
   const long long row = (long long)(k + kHs) * a.pitch;
   if (halo && lane < 4) {  // columns 0, 1 <- nx, nx+1; nx+2, nx+3 <- 2, 3
     const int dst = lane < 2 ? lane : a.nx + lane, src = lane < 2 ? a.nx + lane : lane;
 #pragma unroll
-    for (int q = 0; q < 4; ++q) a.forcing[q * a.plane + row + dst] = a.forcing[q * a.plane + row + src];
+    for (int q = 0; q < 4; ++q) MW_SF(a, q * a.plane + row + dst) = MW_SF(a, q * a.plane + row + src);
   }
   for (int x0 = 0; x0 < a.nx; x0 += kF32WCells) {
     const int i = x0 + lane;
@@ -476,7 +485,7 @@ __device__ __forceinline__ void x_row_warp_f32(const StageArgs<float>& a, int k,
     float iv[4];
     if (upd) {
 #pragma unroll
-      for (int q = 0; q < 4; ++q) iv[q] = a.init[q * a.plane + o];
+      for (int q = 0; q < 4; ++q) iv[q] = MW_SI(a, q * a.plane + o);
     }
     float F[4] = {0.f, 0.f, 0.f, 0.f};
     if (i <= a.nx) {
@@ -485,7 +494,7 @@ __device__ __forceinline__ void x_row_warp_f32(const StageArgs<float>& a, int k,
       for (int j = 0; j < 4; ++j) {
         const long long col = wrap_x(i - 2 + j, a.nx) + kHs;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) s4[q][j] = __ldg(a.forcing + q * a.plane + row + col);
+        for (int q = 0; q < 4; ++q) s4[q][j] = __ldg(&MW_SF(a, q * a.plane + row + col));
       }
       flux_x_f32(s4, r, a.hv_f, F);
     }
@@ -494,7 +503,7 @@ __device__ __forceinline__ void x_row_warp_f32(const StageArgs<float>& a, int k,
     for (int q = 0; q < 4; ++q) Fn[q] = __shfl_down_sync(0xffffffffu, F[q], 1);
     if (upd) {
 #pragma unroll
-      for (int q = 0; q < 4; ++q) a.out[q * a.plane + o] = iv[q] + (F[q] - Fn[q]) * a.c_f;
+      for (int q = 0; q < 4; ++q) MW_SO(a, q * a.plane + o) = iv[q] + (F[q] - Fn[q]) * a.c_f;
     }
   }
 }
@@ -502,7 +511,7 @@ __device__ __forceinline__ void x_row_warp_f32(const StageArgs<float>& a, int k,
 __global__ void __launch_bounds__(kXThreads) k_ens_x_f32(EnsStageT<float> es) {
   const int nw = gridDim.x * (kXThreads / 32);
   for (int it = blockIdx.x * (kXThreads / 32) + (threadIdx.x >> 5); it < es.n_items; it += nw) {
-    const int2 item = es.items[it];  // (member, row)
+    const int2 item = MW_AT(es.items, it, es.n_items);  // (member, row)
     const StageArgs<float> a = member_args_f32(es, item.x);
     x_row_warp_f32(a, item.y, a.flags & MW_FLAG_WRITE_HALO);
   }
@@ -511,7 +520,7 @@ __global__ void __launch_bounds__(kXThreads) k_ens_x_f32(EnsStageT<float> es) {
 __global__ void __launch_bounds__(kEnsZCols) k_ens_z_f32(EnsStageT<float> es) {
   __shared__ SmemZT sm;
   for (int it = blockIdx.x; it < es.n_items; it += gridDim.x) {
-    const int2 item = es.items[it];
+    const int2 item = MW_AT(es.items, it, es.n_items);
     const StageArgs<float> a = member_args_f32(es, item.x);
     const int ncb = (a.nx + kEnsZCols - 1) / kEnsZCols;
     const int cb = item.y % ncb, tile = item.y / ncb;
@@ -672,6 +681,10 @@ static int validate_step(int nx, int nz, double dx, double dz, double dt, const 
              MW_ERR_ALIAS, "state, state_tmp and scratch must be three separate arrays");
   return MW_OK;
 }
+
+#if MW_CHECK
+MW_OOB_COUNTER(oob_count_dirstage)
+#endif
 
 }  // namespace mw
 

@@ -66,7 +66,8 @@ int ens_ieee_occupancy(int direction, int* blocks_per_sm);
 
 constexpr int kEnsZTileMax = 64;
 constexpr int kEnsZCols = 64;  // columns per z work item (one CTA of kEnsZCols threads)
-constexpr size_t kEnsRowBytes = 32;  // one row's background constants (four double-FP32 pairs, or four FP64)
+constexpr size_t kEnsRowBytes = 40;  // one row's background constants: four double-FP32 pairs (split form,
+                                     // 32 B used) or five FP64 values (IEEE-FP64 form)
 
 constexpr int kEnsConstsPerMember = 6;
 inline size_t ens_consts_off(const mw_ens_plan_info& info) {

@@ -124,22 +124,39 @@ __device__ __forceinline__ double rcp(double y, unsigned mask) {
   return r;
 }
 
-// (1 + d)^gamma - 1 for the lanes in `mask`, which call it together: the
-// binomial series to the degree the largest |d| among them needs (a
-// warp-uniform loop), or expm1(gamma log1p(d)) for |d| >= 1/8, Inf and NaN.
-__device__ __forceinline__ double pgm1(double d, unsigned mask) {
+// Row constants, scaled by 12 like the interpolated values.
+struct RowD {
+  double R12;    // 12 background rho
+  double RT12;   // 12 background rho theta
+  double IRT12;  // 1 / (12 background rho theta)
+  double P12;    // 12 background pressure C0 (rho theta)^gamma
+  double PC1;    // P12 C(gamma, 1) IRT12: the pressure perturbation per unit of 12 (rho theta)' to first order
+};
+__device__ __forceinline__ RowD row_consts(double r, double rt, double P) {
+  const double irt = 1.0 / (12.0 * rt);
+  return {12.0 * r, 12.0 * rt, irt, 12.0 * P, 12.0 * P * c_coef.c[1] * irt};
+}
+
+// P12 ((1 + d)^gamma - 1) + add, d = AT IRT12, for the lanes in `mask`, which
+// call it together: the binomial series to the degree the largest |d| among
+// them needs (a warp-uniform loop), or expm1(gamma log1p(d)) for |d| >= 1/8,
+// Inf and NaN.  At degree 1 (|d| < 2^-52 on every lane, e.g. a region at
+// rest) the series is P12 C1 d = AT PC1: one FMA in all.
+__device__ __forceinline__ double pressure(double AT, const RowD& r, double add, unsigned mask) {
+  const double d = AT * r.IRT12;
   const unsigned ex = ((unsigned)((unsigned long long)__double_as_longlong(d) >> 52)) & 0x7ffu;
   const bool big = ex >= 1020u;  // |d| >= 2^-3
   const unsigned exm = __reduce_max_sync(mask, big ? 0u : ex);
   const int s = min(1022 - (int)exm, 64);  // |d| < 2^-s for every series lane
   const int n = c_deg.n[s];
+  if (n == 1 && !__any_sync(mask, big)) return fma(AT, r.PC1, add);
   double g = c_coef.c[n];
   for (int k = n - 1; k >= 1; --k) g = fma(g, d, c_coef.c[k]);
   double f = d * g;
   if (__any_sync(mask, big)) {
     if (big) f = expm1(kGamma * log1p(d));
   }
-  return f;
+  return fma(r.P12, f, add);
 }
 
 // 12 x the 4-point interpolation and the third difference of one variable
@@ -147,17 +164,6 @@ __device__ __forceinline__ double pgm1(double d, unsigned mask) {
 __device__ __forceinline__ void interp(double s0, double s1, double s2, double s3, double& A, double& D) {
   A = fma(7.0, s1 + s2, -(s0 + s3));
   D = fma(3.0, s1 - s2, s3 - s0);
-}
-
-// Row constants, scaled by 12 like the interpolated values.
-struct RowD {
-  double R12;    // 12 background rho
-  double RT12;   // 12 background rho theta
-  double IRT12;  // 1 / (12 background rho theta)
-  double P12;    // 12 background pressure C0 (rho theta)^gamma
-};
-__device__ __forceinline__ RowD row_consts(double r, double rt, double P) {
-  return {12.0 * r, 12.0 * rt, 1.0 / (12.0 * rt), 12.0 * P};
 }
 
 // x flux times 12 (interpolate.py:82-129): with u = (rho u)' / rho,
@@ -168,9 +174,8 @@ __device__ __forceinline__ void flux_x(const double s[4][4], const RowD& r, doub
   for (int q = 0; q < 4; ++q) interp(s[q][0], s[q][1], s[q][2], s[q][3], A[q], D[q]);
   const double ri = rcp(A[DENS] + r.R12, mask);
   const double u = A[UMOM] * ri;
-  const double f = pgm1(A[RHOT] * r.IRT12, mask);
   F[0] = fma(HV, D[DENS], A[UMOM]);
-  F[1] = fma(A[UMOM], u, fma(r.P12, f, HV * D[UMOM]));
+  F[1] = fma(A[UMOM], u, pressure(A[RHOT], r, HV * D[UMOM], mask));
   F[2] = fma(u, A[WMOM], HV * D[WMOM]);
   F[3] = fma(u, A[RHOT] + r.RT12, HV * D[RHOT]);
 }
@@ -188,10 +193,9 @@ __device__ __forceinline__ void flux_z(const double s[4][4], const RowD& r, doub
   }
   const double ri = rcp(A[DENS] + r.R12, mask);
   const double w = AW * ri;
-  const double f = pgm1(A[RHOT] * r.IRT12, mask);
   F[0] = fma(HV, D[DENS], AW);
   F[1] = fma(w, A[UMOM], HV * D[UMOM]);
-  F[2] = fma(AW, w, fma(r.P12, f, HV * D[WMOM]));
+  F[2] = fma(AW, w, pressure(A[RHOT], r, HV * D[WMOM], mask));
   F[3] = fma(w, A[RHOT] + r.RT12, HV * D[RHOT]);
 }
 
@@ -563,7 +567,7 @@ __device__ __forceinline__ Args member_args(const EnsStage& es, int e) {
   return a;
 }
 
-static_assert(sizeof(RowD) == kEnsRowBytes, "row-constant table entry size");
+static_assert(sizeof(RowD) <= kEnsRowBytes, "row-constant table entry size");
 
 __global__ void k_ens_row_table_ieee(const double* hyc, const double* hytc, long long n, RowD* table) {
   for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x) {

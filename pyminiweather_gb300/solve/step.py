@@ -117,13 +117,22 @@ def evolve(params: Dict, fields, mesh=None, dt: float = 1e-4, nsteps: int = 1) -
     reverse_direction = bool(rv.value)
 
 
+# Row bands of the host-buffer step (GB300, 8192 x 4096 collision, measured):
+# the split form is bound by the copies and hides its compute best in 32
+# bands (9.3 ms per step); the IEEE-FP64 form is bound by its compute, which
+# loses efficiency in small launches, and is fastest in 8 (24.2 ms against
+# 26.2 ms in 32 and 30.1 ms unbanded).
+HOST_STEP_BANDS = {"split": 32, "fp64": 8}
+
+
 def evolve_host(params: Dict, fields, h_in: torch.Tensor, h_out: torch.Tensor, dt: float = 1e-4,
-                nbands: int = 32) -> None:
+                nbands: int = None) -> None:
     """One time step of a state held in host memory: h_in (a CPU tensor of the
     state's shape, ideally pinned) is copied into fields.state, the step runs as
     evolve() would run it, and the new state is copied into h_out (may be
-    h_in).  The FP64 split form overlaps the copies with the step by row bands
-    (mw_step_f64_host); other forms copy, step and copy.  Returns once the work
+    h_in).  The FP64 forms "fp64" and "split" overlap the copies with the step
+    by row bands (mw_step_f64_host; nbands None: the form's default,
+    HOST_STEP_BANDS); other forms copy, step and copy.  Returns once the work
     is enqueued on the current stream; synchronise before reading h_out."""
     global reverse_direction
     for name, h in (("h_in", h_in), ("h_out", h_out)):
@@ -144,6 +153,8 @@ def evolve_host(params: Dict, fields, h_in: torch.Tensor, h_out: torch.Tensor, d
     flags = params.get("step_flags", _native.MW_FLAG_WRITE_HALO)
     if params.get("check_finite"):  # blocking: raises MiniWeatherError (status 7) on NaN / Inf
         flags |= _native.MW_FLAG_CHECK_FINITE
+    if nbands is None:
+        nbands = HOST_STEP_BANDS.get(params.get("f64_mode", DEFAULT_F64_MODE), 1)
     _native.call("mw_step_f64_host", fields.nx, fields.nz, float(params["dx"]), float(params["dz"]),
                  float(params["dt"]), float(dt), *hb, _native.ptr(fields.src_w), ctypes.c_void_p(h_in.data_ptr()),
                  ctypes.c_void_p(h_out.data_ptr()), _native.ptr(fields.state), _native.ptr(fields.state_tmp),
