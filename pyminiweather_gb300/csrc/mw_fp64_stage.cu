@@ -4,125 +4,57 @@
 //
 // Every floating-point operation on state values is an FP64 add, multiply or
 // FMA (no FP32 arithmetic on them, no double-FP32 pairs).  On GB300 the FP64
-// pipe retires about 1.9 operations per clock per SM, so one FP64
-// warp-instruction occupies it for ~17 SM clocks, in which the SM can issue
-// ~67 other warp-instructions: the kernels are bound by their FP64 operation
-// count, and integer work (conversions, index arithmetic, table look-ups) is
-// nearly free.  Against the reference's formulas (one pow, three divides and
-// ~50 operations per interface, interpolate.py:82-186) each interface costs
-// ~39 + n FP64 operations and each cell update 8:
+// pipe retires 2 operations per clock per SM, so one FP64 warp-instruction
+// occupies it for 16 SM clocks, in which the SM can issue 64 other
+// warp-instructions: the kernels are bound by their FP64 operation count, and
+// integer work (conversions, index arithmetic, table look-ups) is nearly free.
+// Against the reference's formulas (one pow, three divides and ~50 operations
+// per interface, interpolate.py:82-186) each interface costs ~37 + n FP64
+// operations and each cell update 8 (ncu: 49.7 per cell-stage in x, 50.7 in
+// z on the collision case):
 //   - quantities are carried scaled by 12, so the 4-point interpolation is
 //     A = 7 (s1 + s2) - (s0 + s3) and needs no division; the third
 //     difference is D = (s3 - s0) + 3 (s1 - s2): 6 operations per variable;
-//   - one reciprocal per interface: an FP32 hardware estimate of 1/rho
-//     (operand and result converted by integer operations) refined by one
-//     cubic Newton step in FP64, r = r0 (1 + e + e^2), e = 1 - rho r0
-//     (relative error e^3 <= 2^-66 before rounding): 3 FP64 operations;
+//   - one reciprocal per interface, 3 FP64 operations (ieee::rcp);
 //   - pressure enters as the perturbation P_row ((1 + delta)^gamma - 1),
 //     delta = (rho theta)' / (rho theta)_bg, P_row = C0 (rho theta)_bg^gamma:
 //     exactly the reference's p - hy_pressure_int in z (hy_pressure_int is
 //     C0 hy_dens_theta_int^gamma, ics/initial.py:105); in x the row constant
 //     cancels in the flux difference.  (1 + delta)^gamma - 1 is its binomial
 //     series summed by Horner's rule to the degree n that the warp's largest
-//     |delta| needs for a truncation below 2^-54 relative (n = 2..4 in smooth
-//     regions, 15 for |delta| < 1/8), and expm1(gamma log1p(delta)) beyond;
+//     |delta| needs for a truncation below 2^-54 relative (one FMA in a
+//     region at rest, up to 15 terms for |delta| < 1/8), and
+//     expm1(gamma log1p(delta)) beyond;
 //   - the stage update is out = init + c (F(i) - F(i+1)), c = dt / (12 d):
 //     2 operations per value.
 //
-// x pass: a CTA walks a run of 255-cell chunks of one row; thread t evaluates
-// the flux at interface x0+t into shared memory, and after one barrier
-// updates cell x0+t.  z pass: one thread per column marching a tile of rows
-// with a rolling 4-row window, so each interface flux is evaluated once.
-// Halo cells are never read: the periodic-x and wall-z rules of ics/bcs.py
-// are applied to the indices and values as they are loaded.  Every global
-// access goes through MW_AT (bounds-checked in the debug library).
+// x pass: warps walk 63-cell segments of the rows with no CTA barrier, lane l
+// evaluating the fluxes at interfaces x0+l and x0+32+l (two independent FP64
+// chains) from values staged in the warp's shared-memory slice.  z pass: one
+// thread per column marching a tile of rows with a rolling 4-row window, so
+// each interface flux is evaluated once.  Halo cells are never read: the
+// periodic-x and wall-z rules of ics/bcs.py are applied to the indices and
+// values as they are loaded.  Every global access goes through MW_AT
+// (bounds-checked in the debug library).
 #include <algorithm>
 #include <atomic>
 
 #include "mw_common.cuh"
 #include "mw_ensemble.cuh"
+#include "mw_fp64_math.cuh"
 
 namespace mw {
 namespace ieee {
 
-constexpr int kXT = 256;            // interfaces per x chunk
-constexpr int kXC = kXT - 1;        // cells per x chunk
-constexpr int kXBlocksPerRow = 4;   // x CTAs per row
+constexpr int kXT = 256;            // threads per x CTA
 constexpr int kZT = 128;            // columns per z CTA
 constexpr int kZTileMax = 64;       // rows per z CTA
-#ifndef MW_IEEE_XWARP
-#define MW_IEEE_XWARP 1                 // x pass: barrier-free warp segments (0: CTA chunks)
-#endif
 #ifndef MW_IEEE_X_SEGS_PER_WARP
 #define MW_IEEE_X_SEGS_PER_WARP 16
 #endif
 
-// ---- constant tables ------------------------------------------------------
-constexpr double binom(double e, int n) {  // C(e, n)
-  double c = 1.0;
-  for (int k = 0; k < n; ++k) c = c * (e - k) / (k + 1);
-  return c;
-}
-constexpr double cabs(double v) { return v < 0 ? -v : v; }
-
-constexpr int kMaxDeg = 15;
-struct Coef {
-  double c[kMaxDeg + 1];
-};
-constexpr Coef make_coef() {
-  Coef t{};
-  for (int n = 0; n <= kMaxDeg; ++n) t.c[n] = binom(kGamma, n);
-  return t;
-}
-// deg[s]: the Horner degree for |delta| < 2^-s (s >= 3): the smallest n with
-// |C(gamma, n+1) / C(gamma, 1)| 2^(-s n) <= 2^-54.
-struct Deg {
-  unsigned char n[65];
-};
-constexpr Deg make_deg() {
-  Deg t{};
-  for (int s = 0; s <= 64; ++s) {
-    int n = kMaxDeg;
-    if (s >= 3) {
-      for (n = 1; n < kMaxDeg; ++n) {
-        double b = cabs(binom(kGamma, n + 1) / binom(kGamma, 1));
-        for (int j = 0; j < s * n && b > 0.0; ++j) b *= 0.5;
-        if (b <= 5.551115123125783e-17) break;  // 2^-54
-      }
-    }
-    t.n[s] = (unsigned char)n;
-  }
-  return t;
-}
-__constant__ Coef c_coef = make_coef();
-__constant__ Deg c_deg = make_deg();
-
-// ---- FP64 building blocks --------------------------------------------------
-// 1/y for the lanes in `mask`, which call it together: an FP32 estimate
-// refined by one cubic Newton step (3 FP64 operations).  |y| outside
-// [2^-125, 2^126) (and Inf, NaN, 0) takes the FP64 division, behind a
-// warp-uniform branch so that the division is never evaluated speculatively
-// on the other lanes.
-__device__ __forceinline__ double rcp(double y, unsigned mask) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(y);
-  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
-  const unsigned ex = (hi >> 20) & 0x7ffu;
-  // float with y's sign, rebiased exponent and leading 23 significand bits
-  const unsigned fb = ((__funnelshift_l(lo, hi, 3) + 0x40000000u) & 0x7fffffffu) | (hi & 0x80000000u);
-  float rf;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(__uint_as_float(fb)));
-  const unsigned rb = __float_as_uint(rf);
-  const unsigned rhi = (((rb >> 3) & 0x0fffffffu) + (896u << 20)) | (rb & 0x80000000u);
-  const double r0 = __longlong_as_double((long long)(((unsigned long long)rhi << 32) | (rb << 29)));
-  const double e = fma(-y, r0, 1.0);
-  const double t = fma(e, e, e);
-  double r = fma(r0, t, r0);
-  const bool out = ex - (1023u - 125u) > 250u;
-  if (__any_sync(mask, out)) {
-    if (out) r = 1.0 / y;
-  }
-  return r;
-}
+// (1 + d)^gamma: the pressure perturbation.
+__constant__ Series c_pow_g = make_series(kGamma);
 
 // Row constants, scaled by 12 like the interpolated values.
 struct RowD {
@@ -134,7 +66,7 @@ struct RowD {
 };
 __device__ __forceinline__ RowD row_consts(double r, double rt, double P) {
   const double irt = 1.0 / (12.0 * rt);
-  return {12.0 * r, 12.0 * rt, irt, 12.0 * P, 12.0 * P * c_coef.c[1] * irt};
+  return {12.0 * r, 12.0 * rt, irt, 12.0 * P, 12.0 * P * c_pow_g.c[1] * irt};
 }
 
 // P12 ((1 + d)^gamma - 1) + add, d = AT IRT12, for the lanes in `mask`, which
@@ -144,15 +76,10 @@ __device__ __forceinline__ RowD row_consts(double r, double rt, double P) {
 // rest) the series is P12 C1 d = AT PC1: one FMA in all.
 __device__ __forceinline__ double pressure(double AT, const RowD& r, double add, unsigned mask) {
   const double d = AT * r.IRT12;
-  const unsigned ex = ((unsigned)((unsigned long long)__double_as_longlong(d) >> 52)) & 0x7ffu;
-  const bool big = ex >= 1020u;  // |d| >= 2^-3
-  const unsigned exm = __reduce_max_sync(mask, big ? 0u : ex);
-  const int s = min(1022 - (int)exm, 64);  // |d| < 2^-s for every series lane
-  const int n = c_deg.n[s];
+  bool big;
+  const int n = series_degree(d, mask, c_pow_g, big);
   if (n == 1 && !__any_sync(mask, big)) return fma(AT, r.PC1, add);
-  double g = c_coef.c[n];
-  for (int k = n - 1; k >= 1; --k) g = fma(g, d, c_coef.c[k]);
-  double f = d * g;
+  double f = d * series_g(d, n, c_pow_g);
   if (__any_sync(mask, big)) {
     if (big) f = expm1(kGamma * log1p(d));
   }
@@ -162,7 +89,7 @@ __device__ __forceinline__ double pressure(double AT, const RowD& r, double add,
 // 12 x the 4-point interpolation and the third difference of one variable
 // (the stencils of interpolate.py:33-43 and 69-79).
 __device__ __forceinline__ void interp(double s0, double s1, double s2, double s3, double& A, double& D) {
-  A = fma(7.0, s1 + s2, -(s0 + s3));
+  A = interp12(s0, s1, s2, s3);
   D = fma(3.0, s1 - s2, s3 - s0);
 }
 
@@ -217,7 +144,6 @@ struct Args {
   double c;     // dt_stage / (12 d)
   double dt;    // dt_stage (source terms)
   double gdt;   // -dt_stage grav (z)
-  int chunks_per_block;
   int z_tile;
   int r0, r1;   // output rows [r0, r1)
 };
@@ -254,72 +180,6 @@ __device__ __forceinline__ void write_z_halo_column(const Args& a, int col, bool
 }
 
 // ---- x ---------------------------------------------------------------------
-struct SmemX {
-  double sF[4][kXT];
-  RowD row;
-};
-
-// Row k, chunks [cbeg, cend) of kXC cells; every thread of the CTA calls it.
-__device__ __forceinline__ void x_row(const Args& a, int k, int cbeg, int cend, bool halo, SmemX& sm) {
-  const int t = threadIdx.x;
-  const long long row = (long long)(k + kHs) * a.pitch;
-  const int n4 = a.nz + 2 * kHs;
-  if (t == 0) {
-    const double rt = MW_AT(a.hytc, k + kHs, n4);
-    sm.row = row_consts(MW_AT(a.hyc, k + kHs, n4), rt, kC0 * pow(rt, kGamma));
-  }
-  if (halo && t < 4) {  // columns 0, 1 <- nx, nx+1; nx+2, nx+3 <- 2, 3 (ics/bcs.py:35-39)
-    const int dst = t < 2 ? t : a.nx + t, src = t < 2 ? a.nx + t : t;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) MW_F(a, q * a.plane + row + dst) = MW_F(a, q * a.plane + row + src);
-  }
-  __syncthreads();
-  const RowD r = sm.row;
-  for (int chunk = cbeg; chunk < cend; ++chunk) {
-    const int i = chunk * kXC + t;  // interface i, between cells i-1 and i
-    const bool upd = t < kXC && i < a.nx;
-    const long long o = row + i + kHs;
-    double iv[4];
-    if (upd) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) iv[q] = MW_AT(a.init, q * a.plane + o, 4 * a.plane);
-    }
-    const unsigned mask = __ballot_sync(0xffffffffu, i <= a.nx);
-    if (i <= a.nx) {
-      double s[4][4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const long long col = wrap_x(i - 2 + j, a.nx) + kHs;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) s[q][j] = __ldg(&MW_F(a, q * a.plane + row + col));
-      }
-      double F[4];
-      flux_x(s, r, a.HV, mask, F);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) sm.sF[q][t] = F[q];
-    }
-    __syncthreads();
-    if (upd) {
-      double v[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) v[q] = fma(a.c, sm.sF[q][t] - sm.sF[q][t + 1], iv[q]);
-      if (a.srcw) v[WMOM] = fma(a.dt, MW_AT(a.srcw, (long long)k * a.nx + i, (long long)a.nx * a.nz), v[WMOM]);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) MW_AT(a.out, q * a.plane + o, 4 * a.plane) = v[q];
-    }
-    __syncthreads();
-  }
-}
-
-__global__ void __launch_bounds__(kXT) k_stage_x_ieee(Args a) {
-  __shared__ SmemX sm;
-  const int nchunks = (a.nx + kXC - 1) / kXC;
-  const int cbeg = blockIdx.x * a.chunks_per_block;
-  const int cend = min(cbeg + a.chunks_per_block, nchunks);
-  const bool halo = (a.flags & MW_FLAG_WRITE_HALO) && blockIdx.x == 0;
-  for (int k = a.r0 + blockIdx.y; k < a.r1; k += gridDim.y) x_row(a, k, cbeg, cend, halo, sm);
-}
-
 // x, warp segments: the CTA owns the contiguous range [g0, g1) of the
 // row-major list of 63-cell segments (nseg per row) and splits it evenly over
 // its eight warps, which walk their segments with no CTA barrier.  Lane l
@@ -560,7 +420,6 @@ __device__ __forceinline__ Args member_args(const EnsStage& es, int e) {
   a.c = c.c;
   a.dt = c.dt;
   a.gdt = c.gdt;
-  a.chunks_per_block = 0;
   a.z_tile = es.z_tile;
   a.r0 = 0;
   a.r1 = m.nz;
@@ -681,13 +540,11 @@ int launch_stage_ieee(int nx, int nz, double dx, double dz, double dt_full, cons
   a.c = dt_stage / (12.0 * d);
   a.dt = dt_stage;
   a.gdt = -dt_stage * kGrav;
-  const int nchunks = (nx + kXC - 1) / kXC;
-  a.chunks_per_block = (nchunks + kXBlocksPerRow - 1) / kXBlocksPerRow;
   a.r0 = r0;
   a.r1 = r1;
   const int rows = r1 - r0;
   a.z_tile = z_tile_rows(nx, rows, kZT, kZTileMax);
-  if (direction == MW_DIR_X && MW_IEEE_XWARP) {
+  if (direction == MW_DIR_X) {
     // About MW_IEEE_X_SEGS_PER_WARP segments per warp in a whole number of
     // resident waves of equal ranges (one wave, at least one segment per warp,
     // for small grids); at most kXRowsMax rows per CTA range.
@@ -701,9 +558,6 @@ int launch_stage_ieee(int nx, int nz, double dx, double dz, double dt_full, cons
     grid = std::max<long long>(grid, (rows + kXRowsMax - 3) / (kXRowsMax - 2));
     MW_REQUIRE(grid <= 0x7fffffffLL, MW_ERR_SHAPE, "grid too large for the x direction-stage launch");
     k_stage_x_ieee_w<<<(unsigned)grid, kXT, 0, stream>>>(a, nseg, total, (long long)r0 * nseg);
-  } else if (direction == MW_DIR_X) {
-    dim3 grid((nchunks + a.chunks_per_block - 1) / a.chunks_per_block, (unsigned)std::min(rows, 65535));
-    k_stage_x_ieee<<<grid, kXT, 0, stream>>>(a);
   } else {
     const int ntiles = (rows + a.z_tile - 1) / a.z_tile;
     for (int t0 = 0; t0 < ntiles; t0 += 65535) {

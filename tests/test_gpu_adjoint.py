@@ -30,12 +30,13 @@ def _bg(f):
     return [a for a in f.backgrounds()]
 
 
-@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("mode", [0, 1, 2])
 @pytest.mark.parametrize("direction", [0, 1])
 def test_stage_vjp_matches_autograd(direction, mode):
     """One direction-stage: g_forcing = dt (dL/dforcing)^T g_out, against
-    torch autograd of the pure-PyTorch tendency, in FP64 (mode 0) and
-    double-FP32 (mode 1) arithmetic."""
+    torch autograd of the pure-PyTorch tendency, in FP64 with the reference's
+    formulas (mode 0), double-FP32 (mode 1) and IEEE FP64 with the fewest
+    operations (mode 2)."""
     torch.manual_seed(0)
     p, f = _fields(40, 24, "collision")
     evolve(dict(p, f64_mode="native"), f, None, dt=p["dt"], nsteps=3)  # a developed state
@@ -64,9 +65,10 @@ def test_stage_vjp_matches_autograd(direction, mode):
 @pytest.mark.parametrize("nx,nz", [(2, 1), (3, 2), (29, 5), (30, 31), (61, 58), (130, 3)])
 @pytest.mark.parametrize("direction", [0, 1])
 def test_stage_vjp_split_matches_native(nx, nz, direction):
-    """The double-FP32 stage adjoint against the FP64 one on ragged grids
-    (segment edges, one-row and two-column grids, both walls in one segment),
-    with bases and accumulation of g_out."""
+    """The double-FP32 and the fewest-operation IEEE-FP64 stage adjoints
+    against the reference-formula FP64 one on ragged grids (segment edges,
+    one-row and two-column grids, both walls in one segment), with bases and
+    accumulation of g_out."""
     p, f = _fields(nx, nz, "collision")
     evolve(dict(p, f64_mode="native"), f, None, dt=p["dt"], nsteps=2)
     s = f.state.clone()
@@ -78,20 +80,22 @@ def test_stage_vjp_split_matches_native(nx, nz, direction):
                      device=s.device)
     hb = [_native.ptr(a) for a in f.backgrounds()]
     outs = []
-    for mode in (0, 1):
+    for mode in (0, 1, 2):
         out = torch.full_like(s, 7.0)
         _native.call("mw_dirstage_vjp_f64", nx, nz, p["dx"], p["dz"], p["dt"], *hb, _native.ptr(s), _native.ptr(g),
                      _native.ptr(ba), _native.ptr(bb), 1, _native.ptr(out), p["dt"] / 3, direction, mode,
                      _native.ptr(ws), ws.numel() * 8, _native.stream_handle())
         outs.append(out)
     torch.cuda.synchronize()
-    ref, got = outs
+    ref = outs[0]
     inc_ref = ref[:, 2:-2, 2:-2] - (g + ba + bb)[:, 2:-2, 2:-2]
-    inc_got = got[:, 2:-2, 2:-2] - (g + ba + bb)[:, 2:-2, 2:-2]
-    for v in range(4):
-        err = float((inc_got[v] - inc_ref[v]).abs().max() / inc_ref[v].abs().max().clamp_min(1e-300))
-        assert err <= 1e-11, (nx, nz, direction, v, err)
-    assert torch.equal(got[:, :2], torch.zeros_like(got[:, :2])) and torch.equal(got[:, :, -2:], torch.zeros_like(got[:, :, -2:]))
+    for mode, got in ((1, outs[1]), (2, outs[2])):
+        inc_got = got[:, 2:-2, 2:-2] - (g + ba + bb)[:, 2:-2, 2:-2]
+        for v in range(4):
+            err = float((inc_got[v] - inc_ref[v]).abs().max() / inc_ref[v].abs().max().clamp_min(1e-300))
+            assert err <= (1e-11 if mode == 1 else 1e-13), (nx, nz, direction, mode, v, err)
+        assert torch.equal(got[:, :2], torch.zeros_like(got[:, :2]))
+        assert torch.equal(got[:, :, -2:], torch.zeros_like(got[:, :, -2:]))
 
 
 @pytest.mark.parametrize("mode", ["native", "fp64", "split"])
