@@ -302,6 +302,12 @@ int mw_gravity_source_f64(int nx, int nz, double xlen, double zlen, const double
 int mw_debug_oob_count(unsigned long long* count, int reset);
 int mw_debug_oob_selftest(void* stream);
 
+/* Bounded waits: the kernels that wait on an mbarrier for asynchronous copies
+ * (the FP32 z pass) give up after a bounded number of rounds instead of
+ * hanging, abandon their tile and count it here; *count receives the count
+ * (reset to 0 if asked).  Zero unless a copy failed to arrive. */
+int mw_debug_wait_timeouts(unsigned long long* count, int reset);
+
 /* Count the non-finite (NaN, +-Inf) interior values of a (4, nz+4, nx+4)
  * state into *count (a device counter, added to, not reset); no host sync. */
 int mw_count_nonfinite_f64(int nx, int nz, const double* state, unsigned long long* count, void* stream);

@@ -15,6 +15,10 @@
 // rolling 4-row register window, so every forcing value is loaded once per
 // tile and every interface flux is evaluated once; rows are coalesced across
 // the warp.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <atomic>
 #include <mutex>
 
 #include "mw_common.cuh"
@@ -430,7 +434,189 @@ __global__ void __launch_bounds__(kZThreads) k_stage_z(StageArgs<T> a, int tile0
 }
 
 // ---------------------------------------------------------------------------
-// Ensemble (FP32 storage): one persistent launch per stage over all members.
+// FP32 z pass fed by the tensor memory accelerator (cp.async.bulk.tensor +
+// mbarrier).  The same march as k_stage_z<float, MODE_F32>, but the forcing
+// and init rows reach shared memory through a ring of kBulkStages blocks of
+// kBulkRows rows: per block and array one 3-D tensor copy of the CTA's
+// 132-column segment of kBulkRows rows of the four variables (halo-indexed
+// columns [128 cb, 128 cb + 132): a 16-byte-aligned start, so the grid needs
+// nx % 4 == 0, nx >= 128 and 16-byte-aligned arrays).  Thread 0 issues a
+// block's copies and their byte count on the block's mbarrier; the consumers
+// wait on it (bounded: a copy that never lands counts a timeout and the tile
+// is abandoned, never a hang) and, once every thread has finished a block,
+// thread 0 refills its slot with the block kBulkStages further on.  Forcing
+// rows outside [0, nz) are never copied: the wall rule builds them from the
+// register window.
+constexpr int kBulkRows = 4;
+constexpr int kBulkStages = 4;
+constexpr int kBulkCols = kZThreads + 4;  // 132 floats = 528 bytes, a multiple of 16
+constexpr long long kBulkSpin = 1LL << 20;  // try_wait rounds before a wait gives up
+constexpr unsigned kBulkBoxBytes = 4u * kBulkRows * kBulkCols * 4;  // one array's box: 4 variables x rows x columns
+
+static __device__ unsigned long long g_bulk_timeouts;
+
+struct SmemZBulk {
+  float f[kBulkStages][4][kBulkRows][kBulkCols];  // forcing rows
+  float i[kBulkStages][4][kBulkRows][kBulkCols];  // init rows
+  RowF row[kEnsZTileMax + 1];
+  unsigned long long full[kBulkStages];
+};
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Waits for the phase of the given parity to complete, at most kBulkSpin rounds.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+  for (long long it = 0; it < kBulkSpin; ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__global__ void __launch_bounds__(kZThreads) k_stage_z_f32_bulk(StageArgs<float> a, int tile0,
+                                                                 const __grid_constant__ CUtensorMap tmf,
+                                                                 const __grid_constant__ CUtensorMap tmi) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  SmemZBulk& sm = *reinterpret_cast<SmemZBulk*>(smem_raw);
+  const int tile = tile0 + blockIdx.y;
+  const int z0 = tile * a.z_tile, z1 = min(z0 + a.z_tile, a.nz), zt = z1 - z0;
+  const int cb = blockIdx.x, t = threadIdx.x;
+  const int c = cb * kZThreads + t;                 // interior column of this thread
+  const long long col0 = (long long)cb * kZThreads;  // first halo-indexed column of the segments
+  const int nblk = (zt + 4 + kBulkRows - 1) / kBulkRows;  // forcing rows z0-2 .. z1+1
+  for (int r = t; r <= zt; r += kZThreads) {
+    const int k = z0 + r;
+    sm.row[r] = rowf_z(MW_BI(a, hyi, k), MW_BI(a, hyti, k), MW_BI(a, hypi, k));
+  }
+  if (t == 0) {
+    for (int s = 0; s < kBulkStages; ++s)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&sm.full[s])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  // block b: forcing rows j = z0 - 2 + 4b + r and init rows k = z0 + 4b + r, r < kBulkRows, each a
+  // 132-column x 4-row x 4-variable box of one tensor copy (rows beyond the array read as zero;
+  // forcing rows outside [0, nz) are never used)
+  auto issue = [&](int b) {
+    const int s = b % kBulkStages;
+    const unsigned bar = smem_addr(&sm.full[s]);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(2u * kBulkBoxBytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_addr(&sm.f[s][0][0][0])),
+        "l"(reinterpret_cast<unsigned long long>(&tmf)), "r"((int)col0), "r"(z0 + kBulkRows * b), "r"(0), "r"(bar)
+        : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_addr(&sm.i[s][0][0][0])),
+        "l"(reinterpret_cast<unsigned long long>(&tmi)), "r"((int)col0), "r"(z0 + kHs + kBulkRows * b), "r"(0),
+        "r"(bar)
+        : "memory");
+  };
+  int issued = 0, waited = 0;  // thread 0: blocks issued; every thread: blocks waited for
+  if (t == 0)
+    for (; issued < min(kBulkStages, nblk); ++issued) issue(issued);
+  auto wait_block = [&](int b) {
+    const bool ok = mbar_wait_bounded(&sm.full[b % kBulkStages], (b / kBulkStages) & 1);
+    waited = b + 1;
+    return ok;
+  };
+  bool ok = __syncthreads_and(wait_block(0));
+  if (ok && (a.flags & MW_FLAG_WRITE_HALO) && tile == 0 && cb == 0 && t < 4) {
+    const int hcol[4] = {0, 1, a.nx + kHs, a.nx + kHs + 1};
+    write_z_halo_column(a, hcol[t]);
+  }
+  const bool act = c < a.nx;
+  if (ok && act && (a.flags & MW_FLAG_WRITE_HALO) && tile == 0) write_z_halo_column(a, c + kHs);
+  // forcing value of variable q at relative row rel (row z0 - 2 + rel), the
+  // wall rule applied from the last interior row value `edge` outside [0, nz)
+  auto fsm = [&](int q, int rel) {
+    return sm.f[(rel / kBulkRows) % kBulkStages][q][rel % kBulkRows][t + 2];
+  };
+  auto wall = [&](int q, int k, float edge) {  // k outside [0, nz); edge = value of the nearest interior row
+    if (q == WMOM) return 0.0f;
+    if (q == UMOM) {
+      const int src = k < 0 ? kHs : a.nz + kHs - 1;
+      return float((double)edge / MW_BC(a, hyc, src) * MW_BC(a, hyc, k + kHs));
+    }
+    return edge;
+  };
+  float w[4][4], last[4];  // window rows z0-2 .. z0+1; last: the latest interior row loaded
+  if (ok) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float e0 = fsm(q, max(0, 2 - z0));  // row max(0, z0 - 2)... the bottom row when z0 < 2
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int k = z0 - 2 + j;
+        w[q][j] = (k >= 0 && k < a.nz) ? fsm(q, j) : wall(q, k, k < 0 ? e0 : fsm(q, a.nz - 1 - (z0 - 2)));
+      }
+      last[q] = fsm(q, min(3, a.nz - 1 - (z0 - 2)));
+    }
+  }
+  float Fp[4] = {0.f, 0.f, 0.f, 0.f};
+  if (ok) flux_z_f32(w, sm.row[0], a.hv_f, z0 == 0, Fp);
+  for (int i = 0; ok && i < zt; ++i) {
+    if (i % kBulkRows == 0) {
+      const int b = i / kBulkRows;
+      ok = __syncthreads_and(b + 1 < nblk ? wait_block(b + 1) : true);  // also: block b - 1 is done
+      if (!ok) break;
+      if (t == 0 && b >= 1 && issued < nblk) issue(issued++);
+    }
+    const int k = z0 + i;
+    float iv[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) iv[q] = sm.i[(i / kBulkRows) % kBulkStages][q][i % kBulkRows][t + 2];
+    const float rho_k = w[DENS][2];
+    const int kn = k + 2;  // the row entering the window
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      float v;
+      if (kn < a.nz) {
+        v = fsm(q, i + 4);
+        last[q] = v;
+      } else {
+        v = wall(q, kn, last[q]);
+      }
+      w[q][0] = w[q][1];
+      w[q][1] = w[q][2];
+      w[q][2] = w[q][3];
+      w[q][3] = v;
+    }
+    float Fn[4];
+    flux_z_f32(w, sm.row[i + 1], a.hv_f, k + 1 == a.nz, Fn);
+    if (act) {
+      const long long o = (long long)(k + kHs) * a.pitch + c + kHs;
+      float inc[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) inc[q] = (Fp[q] - Fn[q]) * a.c_f;
+      inc[WMOM] -= a.dt_f * (rho_k * float(kGrav));
+      if (a.srcw) inc[WMOM] += a.dt_f * split::d2f(MW_SW(a, (long long)k * a.nx + c));
+#pragma unroll
+      for (int q = 0; q < 4; ++q) MW_SO(a, q * a.plane + o) = iv[q] + inc[q];
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) Fp[q] = Fn[q];
+  }
+  if (!ok) {
+    // a copy never completed: count it, and let no copy of this CTA land after
+    // it exits (each remaining wait again bounded)
+    if (t == 0) {
+      atomicAdd(&g_bulk_timeouts, 1ULL);
+      for (int b = waited; b < issued; ++b) mbar_wait_bounded(&sm.full[b % kBulkStages], (b / kBulkStages) & 1);
+    }
+  }
+}
+
 __device__ StageArgs<float> member_args_f32(const EnsStageT<float>& es, int e) {
   const mw_ens_member m = MW_AT(es.members, e, es.n_members);
   StageArgs<float> a;
@@ -548,6 +734,67 @@ int ens_f32_occupancy(int direction, int* blocks_per_sm) {
 
 // ---------------------------------------------------------------------------
 // host side
+#ifndef MW_F32_BULK
+#define MW_F32_BULK 1  // FP32 z pass: rows staged by bulk copies where the layout allows (0: plain loads)
+#endif
+
+// cuTensorMapEncodeTiled, from the driver through the runtime (no link-time
+// dependency on the driver library).
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static std::atomic<void*> fn{nullptr};
+  void* f = fn.load(std::memory_order_relaxed);
+  if (f) return (PFN_cuTensorMapEncodeTiled_v12000)f;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess)
+    return nullptr;
+  fn.store(f, std::memory_order_relaxed);
+  return (PFN_cuTensorMapEncodeTiled_v12000)f;
+}
+
+// The (4, nz+4, nx+4) FP32 array as a 3-D tensor (columns, rows, variables)
+// read in boxes of 132 columns x kBulkRows rows x 4 variables.
+static int bulk_tensor_map(const float* p, int nx, int nz, CUtensorMap* tm) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return fail(MW_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+  const cuuint64_t pitch = (cuuint64_t)nx + 2 * kHs, rows = (cuuint64_t)nz + 2 * kHs;
+  const cuuint64_t dims[3] = {pitch, rows, 4};
+  const cuuint64_t strides[2] = {pitch * sizeof(float), pitch * rows * sizeof(float)};
+  const cuuint32_t box[3] = {(cuuint32_t)kBulkCols, (cuuint32_t)kBulkRows, 4};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)p, dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(MW_ERR_CUDA, "tensor map encoding failed (%d)", (int)r);
+  return MW_OK;
+}
+
+// The bulk kernel's shared memory exceeds the 48 KB default: raise its limit
+// once per device.
+static int bulk_z_setup() {
+  static std::atomic<int> done[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return fail(MW_ERR_CUDA, "cudaGetDevice failed");
+  if (dev >= 0 && dev < 64 && done[dev].load(std::memory_order_relaxed)) return MW_OK;
+  const cudaError_t e = cudaFuncSetAttribute(k_stage_z_f32_bulk, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)sizeof(SmemZBulk));
+  if (e != cudaSuccess) return fail(MW_ERR_CUDA, "bulk z kernel shared memory: %s", cudaGetErrorString(e));
+  if (dev >= 0 && dev < 64) done[dev].store(1, std::memory_order_relaxed);
+  return MW_OK;
+}
+
+int bulk_wait_timeouts(unsigned long long* out, bool reset) {
+  unsigned long long v = 0;
+  cudaError_t e = cudaMemcpyFromSymbol(&v, g_bulk_timeouts, sizeof(v));
+  if (e == cudaSuccess && reset) {
+    const unsigned long long z = 0;
+    e = cudaMemcpyToSymbol(g_bulk_timeouts, &z, sizeof(z));
+  }
+  if (e != cudaSuccess) return fail(MW_ERR_CUDA, "wait-timeout counter: %s", cudaGetErrorString(e));
+  *out = v;
+  return MW_OK;
+}
+
 template <typename T>
 static int validate_stage(int nx, int nz, double dx, double dz, double dt_full, const double* hyc, const double* hytc,
                           const double* hyi, const double* hyti, const double* hypi, const T* init, const T* forcing,
@@ -603,9 +850,29 @@ static int launch_stage(int nx, int nz, double dx, double dz, double dt_full, co
     k_stage_x<T, MODE><<<grid, kXThreads, 0, stream>>>(a);
   } else {
     const int ntiles = (nz + a.z_tile - 1) / a.z_tile;
+    bool bulk = false;
+    CUtensorMap tmf, tmi;
+    if constexpr (MODE == MODE_F32) {
+      // the bulk copies start at 16-byte boundaries of 4-float-aligned rows
+      bulk = MW_F32_BULK && nx % 4 == 0 && nx >= kZThreads && ((uintptr_t)init % 16) == 0 &&
+             ((uintptr_t)forcing % 16) == 0;
+      if (bulk) {
+        int st = bulk_z_setup();
+        if (!st) st = bulk_tensor_map((const float*)forcing, nx, nz, &tmf);
+        if (!st) st = bulk_tensor_map((const float*)init, nx, nz, &tmi);
+        if (st) return st;
+      }
+    }
     for (int t0 = 0; t0 < ntiles; t0 += 65535) {
       dim3 grid((nx + kZThreads - 1) / kZThreads, (unsigned)min(ntiles - t0, 65535));
-      k_stage_z<T, MODE><<<grid, kZThreads, 0, stream>>>(a, t0);
+      if constexpr (MODE == MODE_F32) {
+        if (bulk)
+          k_stage_z_f32_bulk<<<grid, kZThreads, sizeof(SmemZBulk), stream>>>(a, t0, tmf, tmi);
+        else
+          k_stage_z<T, MODE><<<grid, kZThreads, 0, stream>>>(a, t0);
+      } else {
+        k_stage_z<T, MODE><<<grid, kZThreads, 0, stream>>>(a, t0);
+      }
       if (t0 + 65535 < ntiles) {
         const int st = check_launch("z direction-stage launch");
         if (st) return st;
@@ -689,6 +956,11 @@ MW_OOB_COUNTER(oob_count_dirstage)
 }  // namespace mw
 
 using namespace mw;
+
+extern "C" int mw_debug_wait_timeouts(unsigned long long* count, int reset) {
+  MW_REQUIRE(count != nullptr, MW_ERR_INVALID_ARG, "count must not be NULL");
+  return mw::bulk_wait_timeouts(count, reset != 0);
+}
 
 extern "C" int mw_dirstage_f64(int nx, int nz, double dx, double dz, double dt_full, const double* hyc,
                                const double* hytc, const double* hyi, const double* hyti, const double* hypi,

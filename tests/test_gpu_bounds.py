@@ -45,7 +45,8 @@ DRIVER = textwrap.dedent("""
     assert n.value == 1, n.value  # the planted index was caught (and diverted)
     for nx, nz, ic in [(2, 1, "collision"), (3, 2, "thermal"), (37, 13, "collision"), (31, 5, "gravity"),
                        (62, 17, "density-current"), (130, 70, "collision"), (257, 129, "gravity"),
-                       (96, 320, "thermal")]:  # 16 host-step bands, the end ones half as tall
+                       (96, 320, "thermal"),  # 16 host-step bands, the end ones half as tall
+                       (256, 40, "collision")]:  # the FP32 z pass fed by tensor copies (nx % 4 == 0, nx >= 128)
         p = make_params(nx, nz, ic)
         hb = None
         for mode in ("fp64", "split", "native"):
@@ -114,6 +115,9 @@ DRIVER = textwrap.dedent("""
                      _native.ptr(f.state), _native.ptr(f.state_tmp), p["dt"] / 3, 1, mode, 1, S)
     print("OOB", count())
     assert n.value == 0, n.value
+    t = ctypes.c_ulonglong(1)
+    _native.call("mw_debug_wait_timeouts", ctypes.byref(t), 0)
+    assert t.value == 0, t.value
 """)
 
 

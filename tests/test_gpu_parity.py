@@ -230,6 +230,11 @@ def test_fp32_form_error_and_mass():
         assert l2[IDS.DENS] <= 1e-4 and l2[IDS.RHOT] <= 1e-4
     m1 = compute_stats(p, f)[0]
     assert abs(m1 - m0) / m0 <= 1e-9
+    # the z pass waited on its bulk copies (nx % 4 == 0) and never gave up a wait
+    import ctypes
+    n = ctypes.c_ulonglong(1)
+    _native.call("mw_debug_wait_timeouts", ctypes.byref(n), 0)
+    assert n.value == 0
 
 
 def test_fullsize_200_steps_vs_oracle():
