@@ -306,12 +306,11 @@ __global__ void __launch_bounds__(kXT, MW_IEEE_X_MIN_BLOCKS) k_stage_x_ieee_w(Ar
   const int row0 = (int)(g0 / nseg), nrows = (int)((g1 - 1) / nseg) - row0 + 1;  // nrows <= kXRowsMax (host)
   const int w = threadIdx.x >> 5;
   const long long n = g1 - g0;
-  const int n4 = a.nz + 2 * kHs;
   x_warp_walk(a, nseg, g0 + n * w / kXWarps, g0 + n * (w + 1) / kXWarps, [&](int k) { return sm.row[k - row0]; },
               a.flags & MW_FLAG_WRITE_HALO, sm.sS[w], [&]() {
                 for (int r = threadIdx.x; r < nrows; r += kXT) {
-                  const double rt = MW_AT(a.hytc, row0 + r + kHs, n4);
-                  sm.row[r] = row_consts(MW_AT(a.hyc, row0 + r + kHs, n4), rt, kC0 * pow(rt, kGamma));
+                  const double rt = MW_AT(a.hytc, row0 + r + kHs, a.nz + 2 * kHs);
+                  sm.row[r] = row_consts(MW_AT(a.hyc, row0 + r + kHs, a.nz + 2 * kHs), rt, kC0 * pow(rt, kGamma));
                 }
                 __syncthreads();
               });
