@@ -464,19 +464,21 @@ __global__ void __launch_bounds__(kEnsZCols) k_ens_z_ieee(EnsStage es) {
   }
 }
 
-// CTAs of k_stage_x_ieee_w resident on the current device, cached per device.
-int x_resident_ctas(int* out) {
-  static std::atomic<int> cache[64];
+// CTAs of k_stage_x_ieee_w (which 0) / k_stage_z_ieee (which 1) resident on
+// the current device, cached per device.
+int resident_ctas(int which, int* out) {
+  static std::atomic<int> cache[2][64];
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return fail(MW_ERR_CUDA, "cudaGetDevice failed");
   const bool cached = dev >= 0 && dev < 64;
-  if (cached && (*out = cache[dev].load(std::memory_order_relaxed)) > 0) return MW_OK;
+  if (cached && (*out = cache[which][dev].load(std::memory_order_relaxed)) > 0) return MW_OK;
   int per_sm = 0, sms = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage_x_ieee_w, kXT, 0);
+  cudaError_t e = which == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage_x_ieee_w, kXT, 0)
+                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage_z_ieee, kZT, 0);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return fail(MW_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
   *out = std::max(1, per_sm) * sms;
-  if (cached) cache[dev].store(*out, std::memory_order_relaxed);
+  if (cached) cache[which][dev].store(*out, std::memory_order_relaxed);
   return MW_OK;
 }
 
@@ -542,14 +544,24 @@ int launch_stage_ieee(int nx, int nz, double dx, double dz, double dt_full, cons
   a.r0 = r0;
   a.r1 = r1;
   const int rows = r1 - r0;
-  a.z_tile = z_tile_rows(nx, rows, kZT, kZTileMax);
+  if (direction == MW_DIR_Z) {
+    // rows per z CTA: at most kZTileMax, fewer when the launch would otherwise
+    // leave resident CTA slots empty (the bands of the host-buffer step), at
+    // least 8 (each tile re-reads 4 window rows)
+    int resident = 0, st = resident_ctas(1, &resident);
+    if (st) return st;
+    const long long ncb = (nx + kZT - 1) / kZT;
+    a.z_tile = (int)std::max(8LL, std::min<long long>(kZTileMax, (long long)rows * ncb / resident));
+  } else {
+    a.z_tile = kZTileMax;
+  }
   if (direction == MW_DIR_X) {
     // About MW_IEEE_X_SEGS_PER_WARP segments per warp in a whole number of
     // resident waves of equal ranges (one wave, at least one segment per warp,
     // for small grids); at most kXRowsMax rows per CTA range.
     const int nseg = (nx + kWCells - 1) / kWCells;
     const long long total = (long long)nseg * rows;
-    int resident = 0, st = x_resident_ctas(&resident);
+    int resident = 0, st = resident_ctas(0, &resident);
     if (st) return st;
     long long grid = std::min<long long>(resident, (total + kXWarps - 1) / kXWarps);
     grid = std::max<long long>(grid, total / (kXWarps * MW_IEEE_X_SEGS_PER_WARP));
