@@ -55,6 +55,7 @@ STATE_VALUES_PER_CELL_STEP = 2 * sum(VALUES_PER_STAGE)  # 64
 FP64_OPS_PER_CLOCK_PER_SM = 2.0
 
 DTYPES = {
+    "fp32": "f32 perturbation fields (FP64 backgrounds, IC and reductions)",
     "fp64": "f64",
     "native": "f64",
     "split": "f64 storage and update, double-FP32 interior arithmetic (~47-bit significand, FP32 exponent range; "
@@ -64,7 +65,7 @@ KERNELS = {
     "fp64": {0: "k_stage_x_ieee_w", 1: "k_stage_z_ieee"},
     "split": {0: "k_stage_x_split", 1: "k_stage_z_split"},
     "native": {0: "k_stage_x<double,NATIVE64>", 1: "k_stage_z<double,NATIVE64>"},
-    "fp32": {0: "k_stage_x<float,F32>", 1: "k_stage_z<float,F32>"},
+    "fp32": {0: "k_stage_x<float,F32>", 1: "k_stage_z_f32_bulk"},
 }
 
 
@@ -77,8 +78,9 @@ def parse_args():
     ap.add_argument("--nx", type=int, default=8192)
     ap.add_argument("--nz", type=int, default=4096)
     ap.add_argument("--ic", default="collision")
-    ap.add_argument("--mode", default="fp64", choices=["fp64", "split", "native"],
-                    help="FP64 form of the headline (default: fp64, IEEE FP64)")
+    ap.add_argument("--mode", default="fp64", choices=["fp64", "split", "native", "fp32"],
+                    help="form of the headline: an FP64 form (default: fp64, IEEE FP64) or fp32 (the "
+                         "precision form; for profiling)")
     ap.add_argument("--no-extras", action="store_true", help="headline only (no other forms, e2e or CPU legs)")
     ap.add_argument("--cpu-steps", type=int, default=2, help="time steps in the oracle CPU-baseline sample")
     return ap.parse_args()
@@ -599,8 +601,10 @@ def run_gb300(args):
     peak, peak_kind = load_peaks()
     table = load_profile_table()
     cells = args.nx * args.nz
-    p = make_params(args.nx, args.nz, args.ic, args.mode)
-    f = initialize_fields(p, dtype=torch.float64)
+    f32 = args.mode == "fp32"
+    p = make_params(args.nx, args.nz, args.ic, "fp64" if f32 else args.mode)
+    f = initialize_fields(p, dtype=torch.float32 if f32 else torch.float64)
+    vbytes = 4 if f32 else 8
     init(f, p)
     torch.cuda.synchronize()
     m0 = compute_stats(p, f)[0]
@@ -612,36 +616,44 @@ def run_gb300(args):
     ms = replica_max(torch, ms, dist, "cuda")
     m1 = compute_stats(p, f)[0]
     value = job_value(world, cells, args.steps, ms)
+    if f32 and not args.no_extras:
+        raise SystemExit("--mode fp32 is a profiling headline: use it with --no-extras")
+    if not args.no_extras:
+        # end to end through the public API with host buffers (on the headline's fields)
+        init(f, p)
+        clocks_e = ClockSampler(device_id_for_smi(torch, dev))
+        clocks_e.start()
+        ms_e, nbytes = e2e_run(torch, p, f, args.steps, 1, dist)
+        clk_e = clocks_e.stop()
+        ms_e = replica_max(torch, ms_e, dist, "cuda")
+        e2e_line = {"value": job_value(world, cells, args.steps, ms_e), "unit": UNIT,
+                    "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                    "ms_per_step": ms_e / args.steps, "api": "pyminiweather_gb300.solve.evolve_host",
+                    "f64_mode": args.mode, "clocks": clk_e}
     # per-kernel durations: the step's six launches issued one by one through
     # the C ABI (same kernels, same arrays, same storage formats), an event after each
     init(f, p)
     per = stage_pass(torch, _native, p, f, args.steps, args.warmup, dist)
-    rl = roofline(per, cells, 8, peak, peak_kind, KERNELS[args.mode], table, clk.get("sm_mhz"))
+    rl = roofline(per, cells, vbytes, peak, peak_kind, KERNELS[args.mode], table, clk.get("sm_mhz"))
     rl["kernel_timing"] = "the public step's six launches issued one by one (mw_dirstage_f64), CUDA events on the " \
                           "launching stream"
-    step_gbs = cells * STATE_VALUES_PER_CELL_STEP * 8 / (ms / args.steps * 1e-3) / 1e9
+    step_gbs = cells * STATE_VALUES_PER_CELL_STEP * vbytes / (ms / args.steps * 1e-3) / 1e9
     rl["public_step"] = {"achieved": round(step_gbs, 1), "frac": round(step_gbs / peak, 4),
-                         "note": "512 algorithmic B per cell-step over the public step's time"}
+                         "note": "%d algorithmic B per cell-step over the public step's time"
+                                 % (STATE_VALUES_PER_CELL_STEP * vbytes)}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": DTYPES[args.mode],
             "data": "synthetic (the reference's analytic collision initial condition)",
             "config": config_dict(args), "f64_mode": args.mode,
             "roofline": rl, "clocks": clk, "gpu_launches": 6 * args.steps,
-            "mass_drift": (m1 - m0) / m0, "bytes_per_cell_step": STATE_VALUES_PER_CELL_STEP * 8}
+            "mass_drift": (m1 - m0) / m0, "bytes_per_cell_step": STATE_VALUES_PER_CELL_STEP * vbytes}
     if rl.get("fp64_pipe"):
         line["limiter"] = "FP64 pipe (%.0f %% of its peak in the dominant kernel; HBM %.0f %%)" % (
             100 * rl["fp64_pipe"]["frac"], 100 * rl["frac"])
-
     if not args.no_extras:
-        # end to end through the public API with host buffers (on the headline's fields)
-        init(f, p)
-        ms_e, nbytes = e2e_run(torch, p, f, args.steps, 1, dist)
-        ms_e = replica_max(torch, ms_e, dist, "cuda")
-        line["e2e"] = {"value": job_value(world, cells, args.steps, ms_e), "unit": UNIT,
-                       "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
-                       "ms_per_step": ms_e / args.steps, "api": "pyminiweather_gb300.solve.evolve_host",
-                       "f64_mode": args.mode}
+        line["e2e"] = e2e_line
+
     del f
     torch.cuda.empty_cache()
     if not args.no_extras and world == 1:
