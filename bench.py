@@ -65,7 +65,7 @@ KERNELS = {
     "fp64": {0: "k_stage_x_ieee_w", 1: "k_stage_z_ieee"},
     "split": {0: "k_stage_x_split", 1: "k_stage_z_split"},
     "native": {0: "k_stage_x<double,NATIVE64>", 1: "k_stage_z<double,NATIVE64>"},
-    "fp32": {0: "k_stage_x<float,F32>", 1: "k_stage_z_f32_bulk"},
+    "fp32": {0: "k_stage_x_f32_bulk", 1: "k_stage_z_f32_bulk"},
 }
 
 
@@ -188,12 +188,17 @@ def device_id_for_smi(torch, dev):
         return str(dev)
 
 
+ARM_PARTS = {"0xd4f": "Arm Neoverse V2", "0xd40": "Arm Neoverse V1", "0xd0c": "Arm Neoverse N1",
+             "0xd8e": "Arm Neoverse N3", "0xd84": "Arm Neoverse V3"}
+
+
 def cpu_model():
     try:
         with open("/proc/cpuinfo") as fh:
             for line in fh:
                 if line.lower().startswith(("model name", "cpu part")):
-                    return line.split(":", 1)[1].strip()
+                    name = line.split(":", 1)[1].strip()
+                    return "%s (%s, %s)" % (ARM_PARTS[name], name, platform.machine()) if name in ARM_PARTS else name
     except Exception:
         pass
     return platform.processor() or platform.machine()

@@ -141,7 +141,8 @@ int mw_step_f64(int nx, int nz, double dx, double dz, double dt_full, double dt,
  * at most nz / 16); the results are those of copy-in, mw_step_f64, copy-out
  * bit for bit.
  * h_in / h_out should be page-locked for the copies to run asynchronously.
- * Calls on one device share internal copy streams and are serialised. */
+ * Calls on one device share internal copy and compute streams (the x stages
+ * of a band run on one beside the caller's) and are serialised. */
 int mw_step_f64_host(int nx, int nz, double dx, double dz, double dt_full, double dt, const double* hy_dens_cell,
                      const double* hy_dens_theta_cell, const double* hy_dens_int, const double* hy_dens_theta_int,
                      const double* hy_pressure_int, const double* src_w, const double* h_in, double* h_out,

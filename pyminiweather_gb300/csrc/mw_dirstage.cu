@@ -522,12 +522,12 @@ __global__ void __launch_bounds__(kZThreads) k_stage_z_f32_bulk(StageArgs<float>
         "r"(bar)
         : "memory");
   };
-  int issued = 0, waited = 0;  // thread 0: blocks issued; every thread: blocks waited for
+  int issued = 0, waited = 0;  // thread 0: blocks issued; every thread: blocks whose copies it saw land
   if (t == 0)
     for (; issued < min(kBulkStages, nblk); ++issued) issue(issued);
   auto wait_block = [&](int b) {
     const bool ok = mbar_wait_bounded(&sm.full[b % kBulkStages], (b / kBulkStages) & 1);
-    waited = b + 1;
+    if (ok) waited = b + 1;
     return ok;
   };
   bool ok = __syncthreads_and(wait_block(0));
@@ -614,6 +614,138 @@ __global__ void __launch_bounds__(kZThreads) k_stage_z_f32_bulk(StageArgs<float>
       atomicAdd(&g_bulk_timeouts, 1ULL);
       for (int b = waited; b < issued; ++b) mbar_wait_bounded(&sm.full[b % kBulkStages], (b / kBulkStages) & 1);
     }
+  }
+}
+
+// FP32 x pass fed by the tensor memory accelerator.  The row-major list of
+// kBXCells-cell chunks is split into equal ranges, one per CTA; per chunk one
+// 3-D tensor copy per array of kBXCols columns x 1 row x 4 variables
+// (halo-indexed columns [x0, x0 + kBXCols): cells x0 - 2 .. x0 + kBXCells + 1,
+// starting at a 16-byte boundary since x0 is a multiple of 4) lands in a ring of
+// kBXStages slots.  Thread t evaluates the flux at interface x0 + t from the
+// slot (taps outside [0, nx), at the two ends of a row, are read from global
+// memory with the periodic rule: the halo columns are never trusted) into a
+// double-buffered flux array; after one CTA barrier per chunk, thread t
+// updates cell x0 + t, and thread 0 refills the slot of the previous chunk.
+// Waits are bounded as in the z pass.
+constexpr int kBXCells = 252;
+constexpr int kBXCols = kBXCells + 4;  // 256 floats = 1 KB per variable
+constexpr int kBXStages = 4;
+constexpr unsigned kBXBoxBytes = 4u * kBXCols * 4;  // one array's box: 4 variables x 256 floats
+static_assert(kBXCells % 4 == 0 && kBXCells + 1 <= kXThreads, "x chunk layout");
+
+struct SmemXBulk {
+  float f[kBXStages][4][kBXCols];  // forcing
+  float i[kBXStages][4][kBXCols];  // init
+  float sF[2][4][kXThreads];       // interface fluxes, by chunk parity
+  unsigned long long full[kBXStages];
+};
+
+__global__ void __launch_bounds__(kXThreads) k_stage_x_f32_bulk(StageArgs<float> a, long long total, int cpr,
+                                                                 const __grid_constant__ CUtensorMap tmf,
+                                                                 const __grid_constant__ CUtensorMap tmi) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  SmemXBulk& sm = *reinterpret_cast<SmemXBulk*>(smem_raw);
+  const int t = threadIdx.x;
+  const long long j0 = total * blockIdx.x / gridDim.x, j1 = total * (blockIdx.x + 1) / gridDim.x;
+  const int n = (int)(j1 - j0);  // chunks of this CTA (uniform)
+  if (n <= 0) return;
+  if (t == 0) {
+    for (int s = 0; s < kBXStages; ++s)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&sm.full[s])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  // (row, chunk in row) of the next chunk to issue (thread 0) and of the chunk being computed,
+  // advanced incrementally (no 64-bit division per chunk)
+  int ik = (int)(j0 / cpr), ic = (int)(j0 % cpr);
+  int k = ik, cc = ic;
+  auto issue = [&](int b) {  // chunk j0 + b into slot b % kBXStages (thread 0, in order of b)
+    const int x0 = ic * kBXCells, kk = ik;
+    if (++ic == cpr) {
+      ic = 0;
+      ++ik;
+    }
+    const int s = b % kBXStages;
+    const unsigned bar = smem_addr(&sm.full[s]);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(2u * kBXBoxBytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_addr(&sm.f[s][0][0])),
+        "l"(reinterpret_cast<unsigned long long>(&tmf)), "r"(x0), "r"(kk + kHs), "r"(0), "r"(bar)
+        : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_addr(&sm.i[s][0][0])),
+        "l"(reinterpret_cast<unsigned long long>(&tmi)), "r"(x0), "r"(kk + kHs), "r"(0), "r"(bar)
+        : "memory");
+  };
+  int issued = 0, waited = 0;  // thread 0: chunks issued / chunks whose copies have landed
+  if (t == 0)
+    for (; issued < min(kBXStages, n); ++issued) issue(issued);
+  const bool halo = a.flags & MW_FLAG_WRITE_HALO;
+  const float c = a.c_f, dt = a.dt_f;
+  int rk = -1;
+  RowF rc;
+  bool ok = true;
+  for (int b = 0; b < n; ++b) {
+    if (b > 0 && ++cc == cpr) {
+      cc = 0;
+      ++k;
+    }
+    const int x0 = cc * kBXCells;
+    const int s = b % kBXStages, fb = b & 1;
+    const long long row = (long long)(k + kHs) * a.pitch;
+    if (k != rk) {
+      rk = k;
+      rc = rowf_x(MW_BC(a, hyc, k + kHs), MW_BC(a, hytc, k + kHs));
+    }
+    const bool w_ok = mbar_wait_bounded(&sm.full[s], (b / kBXStages) & 1);
+    if (w_ok) waited = b + 1;
+    const int i = x0 + t;  // interface between cells i - 1 and i
+    if (w_ok && t <= kBXCells && i <= a.nx) {
+      float sv[4][4];
+      if (i >= 2 && i + 1 < a.nx) {
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) sv[q][jj] = sm.f[s][q][t + jj];
+      } else {  // a tap beyond a row end: the periodic rule, from global memory
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+          const long long col = wrap_x(i - 2 + jj, a.nx) + kHs;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) sv[q][jj] = __ldg(&MW_SF(a, q * a.plane + row + col));
+        }
+      }
+      float F[4];
+      flux_x_f32(sv, rc, a.hv_f, F);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) sm.sF[fb][q][t] = F[q];
+    }
+    if (w_ok && halo && x0 == 0 && t < 4) {  // this row's periodic halo of the forcing array (ics/bcs.py:35-39)
+      const int dst = t < 2 ? t : a.nx + t;  // columns 0, 1, nx+2, nx+3
+      const int src = t < 2 ? a.nx + t : t;  // columns nx, nx+1, 2, 3
+#pragma unroll
+      for (int q = 0; q < 4; ++q) MW_SF(a, q * a.plane + row + dst) = MW_SF(a, q * a.plane + row + src);
+    }
+    ok = __syncthreads_and(w_ok);  // fluxes visible; every thread is done with chunk b - 1
+    if (!ok) break;
+    if (t == 0 && b >= 1 && issued < n) issue(issued++);  // refill chunk b - 1's slot
+    if (t < kBXCells && i < a.nx) {
+      float inc[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) inc[q] = (sm.sF[fb][q][t] - sm.sF[fb][q][t + 1]) * c;
+      if (a.srcw) inc[WMOM] += dt * split::d2f(MW_SW(a, (long long)k * a.nx + i));
+      const long long o = row + i + kHs;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) MW_SO(a, q * a.plane + o) = sm.i[s][q][t + 2] + inc[q];
+    }
+  }
+  if (!ok && t == 0) {  // a copy never completed: count it, and let none land after the CTA exits
+    atomicAdd(&g_bulk_timeouts, 1ULL);
+    for (int b = waited; b < issued; ++b) mbar_wait_bounded(&sm.full[b % kBXStages], (b / kBXStages) & 1);
   }
 }
 
@@ -754,13 +886,13 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 
 // The (4, nz+4, nx+4) FP32 array as a 3-D tensor (columns, rows, variables)
 // read in boxes of 132 columns x kBulkRows rows x 4 variables.
-static int bulk_tensor_map(const float* p, int nx, int nz, CUtensorMap* tm) {
+static int bulk_tensor_map(const float* p, int nx, int nz, int box_cols, int box_rows, CUtensorMap* tm) {
   PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
   if (!enc) return fail(MW_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
   const cuuint64_t pitch = (cuuint64_t)nx + 2 * kHs, rows = (cuuint64_t)nz + 2 * kHs;
   const cuuint64_t dims[3] = {pitch, rows, 4};
   const cuuint64_t strides[2] = {pitch * sizeof(float), pitch * rows * sizeof(float)};
-  const cuuint32_t box[3] = {(cuuint32_t)kBulkCols, (cuuint32_t)kBulkRows, 4};
+  const cuuint32_t box[3] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows, 4};
   const cuuint32_t estr[3] = {1, 1, 1};
   const CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)p, dims, strides, box, estr,
                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -780,6 +912,23 @@ static int bulk_z_setup() {
                                              (int)sizeof(SmemZBulk));
   if (e != cudaSuccess) return fail(MW_ERR_CUDA, "bulk z kernel shared memory: %s", cudaGetErrorString(e));
   if (dev >= 0 && dev < 64) done[dev].store(1, std::memory_order_relaxed);
+  return MW_OK;
+}
+
+// Resident CTAs of the FP32 x bulk kernel on the current device, cached per device.
+static int bulk_x_resident(int* out) {
+  static std::atomic<int> cache[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return fail(MW_ERR_CUDA, "cudaGetDevice failed");
+  const bool cached = dev >= 0 && dev < 64;
+  if (cached && (*out = cache[dev].load(std::memory_order_relaxed)) > 0) return MW_OK;
+  int per_sm = 0, sms = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage_x_f32_bulk, kXThreads,
+                                                                sizeof(SmemXBulk));
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return fail(MW_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
+  *out = std::max(1, per_sm) * sms;
+  if (cached) cache[dev].store(*out, std::memory_order_relaxed);
   return MW_OK;
 }
 
@@ -845,21 +994,36 @@ static int launch_stage(int nx, int nz, double dx, double dz, double dt_full, co
   a.chunks_per_block = (nchunks + kXBlocksPerRow - 1) / kXBlocksPerRow;
   a.z_tile = z_tile_rows(nx, nz, kZThreads, kZTile);
   set_f32_constants(a, direction);
+  // FP32: tiles staged by tensor copies, which start at 16-byte boundaries of
+  // 4-float-aligned rows
+  const bool bulk = MODE == MODE_F32 && MW_F32_BULK && nx % 4 == 0 && nx >= kZThreads &&
+                    ((uintptr_t)init % 16) == 0 && ((uintptr_t)forcing % 16) == 0;
   if (direction == MW_DIR_X) {
+    if constexpr (MODE == MODE_F32) {
+      if (bulk) {
+        // one wave of CTAs, each an equal range of the row-major chunk list
+        CUtensorMap tmf, tmi;
+        int resident = 0, st = bulk_x_resident(&resident);
+        if (!st) st = bulk_tensor_map((const float*)forcing, nx, nz, kBXCols, 1, &tmf);
+        if (!st) st = bulk_tensor_map((const float*)init, nx, nz, kBXCols, 1, &tmi);
+        if (st) return st;
+        const int cpr = (nx + kBXCells - 1) / kBXCells;
+        const long long total = (long long)cpr * nz;
+        const long long grid = std::min<long long>(total, resident);
+        k_stage_x_f32_bulk<<<(unsigned)grid, kXThreads, sizeof(SmemXBulk), stream>>>(a, total, cpr, tmf, tmi);
+        return check_launch("x direction-stage launch");
+      }
+    }
     dim3 grid((nchunks + a.chunks_per_block - 1) / a.chunks_per_block, (unsigned)min(nz, 65535));
     k_stage_x<T, MODE><<<grid, kXThreads, 0, stream>>>(a);
   } else {
     const int ntiles = (nz + a.z_tile - 1) / a.z_tile;
-    bool bulk = false;
     CUtensorMap tmf, tmi;
     if constexpr (MODE == MODE_F32) {
-      // the bulk copies start at 16-byte boundaries of 4-float-aligned rows
-      bulk = MW_F32_BULK && nx % 4 == 0 && nx >= kZThreads && ((uintptr_t)init % 16) == 0 &&
-             ((uintptr_t)forcing % 16) == 0;
       if (bulk) {
         int st = bulk_z_setup();
-        if (!st) st = bulk_tensor_map((const float*)forcing, nx, nz, &tmf);
-        if (!st) st = bulk_tensor_map((const float*)init, nx, nz, &tmi);
+        if (!st) st = bulk_tensor_map((const float*)forcing, nx, nz, kBulkCols, kBulkRows, &tmf);
+        if (!st) st = bulk_tensor_map((const float*)init, nx, nz, kBulkCols, kBulkRows, &tmi);
         if (st) return st;
       }
     }

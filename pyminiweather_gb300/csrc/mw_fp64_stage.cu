@@ -545,13 +545,17 @@ int launch_stage_ieee(int nx, int nz, double dx, double dz, double dt_full, cons
   a.r1 = r1;
   const int rows = r1 - r0;
   if (direction == MW_DIR_Z) {
-    // rows per z CTA: at most kZTileMax, fewer when the launch would otherwise
-    // leave resident CTA slots empty (the bands of the host-buffer step), at
-    // least 8 (each tile re-reads 4 window rows)
+    // rows per z CTA: at most kZTileMax and at least 8 (each tile re-reads 4
+    // window rows), chosen so that the launch is a whole number of resident
+    // waves or just under (CTAs cost about the same, so a partly filled last
+    // wave would idle SMs; one wave for the bands of the host-buffer step)
     int resident = 0, st = resident_ctas(1, &resident);
     if (st) return st;
     const long long ncb = (nx + kZT - 1) / kZT;
-    a.z_tile = (int)std::max(8LL, std::min<long long>(kZTileMax, (long long)rows * ncb / resident));
+    const long long waves = std::max(1LL, ((long long)rows * ncb + (long long)kZTileMax * resident - 1) /
+                                              ((long long)kZTileMax * resident));
+    const long long tiles = std::max(1LL, waves * resident / ncb);
+    a.z_tile = (int)std::max(8LL, std::min<long long>(kZTileMax, (rows + tiles - 1) / tiles));
   } else {
     a.z_tile = kZTileMax;
   }

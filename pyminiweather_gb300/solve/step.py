@@ -118,11 +118,12 @@ def evolve(params: Dict, fields, mesh=None, dt: float = 1e-4, nsteps: int = 1) -
 
 
 # Row bands of the host-buffer step (GB300, 8192 x 4096 collision, measured):
-# the split form is bound by the copies and hides its compute best in 32
-# bands (9.3 ms per step); the IEEE-FP64 form is bound by its compute, which
-# loses efficiency in small launches, and is fastest in 8 (24.2 ms against
-# 26.2 ms in 32 and 30.1 ms unbanded).
-HOST_STEP_BANDS = {"split": 32, "fp64": 8}
+# the x stages of a band run on a second stream beside the z stages of the
+# others, so the short banded launches fill each other's tails, and both forms
+# do best with 32 bands: the split form is bound by the copies (9.3 ms per
+# step), the IEEE-FP64 form by its compute (20.4 ms against 19.4 ms for the
+# step alone; 22.0 ms in 8 bands, 29.9 ms unbanded).
+HOST_STEP_BANDS = {"split": 32, "fp64": 32}
 
 
 def evolve_host(params: Dict, fields, h_in: torch.Tensor, h_out: torch.Tensor, dt: float = 1e-4,

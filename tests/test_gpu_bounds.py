@@ -4,7 +4,8 @@ outside its array.  A child process loads that library, checks that the
 counter sees a planted out-of-range index (the self-test), then runs on
 ragged grids: the three FP64 forms (IEEE "fp64", "split", "native") and FP32
 through the steps, single stages, host-banded steps and the pair-format
-stages; the ensembles of every form; the stage adjoints of every mode; the
+stages, the FP32 passes fed by tensor copies; the ensembles of every form;
+the stage adjoints of every mode; the
 initial condition, gravity source, stats, solution variables, non-finite
 count and every unfused piece; and the z launches split at 65535 row tiles
 (grid.y's limit) on a two-column grid over four million rows.  It asserts
@@ -46,7 +47,8 @@ DRIVER = textwrap.dedent("""
     for nx, nz, ic in [(2, 1, "collision"), (3, 2, "thermal"), (37, 13, "collision"), (31, 5, "gravity"),
                        (62, 17, "density-current"), (130, 70, "collision"), (257, 129, "gravity"),
                        (96, 320, "thermal"),  # 16 host-step bands, the end ones half as tall
-                       (256, 40, "collision")]:  # the FP32 z pass fed by tensor copies (nx % 4 == 0, nx >= 128)
+                       (256, 40, "collision"), (260, 9, "gravity"), (132, 7, "thermal")]:  # FP32 passes fed by
+        # tensor copies (nx % 4 == 0, nx >= 128): rows of one and of two chunks
         p = make_params(nx, nz, ic)
         hb = None
         for mode in ("fp64", "split", "native"):

@@ -237,6 +237,45 @@ def test_fp32_form_error_and_mass():
     assert n.value == 0
 
 
+@pytest.mark.parametrize("nx,nz,ic", [(256, 40, "collision"), (260, 9, "gravity"), (132, 7, "thermal"),
+                                      (1024, 130, "collision")])
+def test_fp32_tensor_copy_kernels_match_plain_loads(nx, nz, ic):
+    """The FP32 stages whose tiles are staged by tensor copies (arrays 16-byte
+    aligned, nx % 4 == 0, nx >= 128) against the plain-load kernels, which the
+    library uses for the same arrays offset by one float: identical results,
+    halo writes included, in both directions (rows of one and of several
+    chunks, the periodic taps at both row ends, the gravity forcing)."""
+    import ctypes
+    p, f = setup(ic, nx, nz, dtype=torch.float32)
+    evolve(p, f, None, dt=p["dt"], nsteps=3)
+    forcing = f.state + 1e-3 * torch.randn(f.state.shape, generator=torch.Generator().manual_seed(5)).to(f.state)
+    hb = [_native.ptr(a) for a in f.backgrounds()]
+    src = _native.ptr(f.src_w) if ic == "gravity" else None
+
+    def run(offset, direction, flags):
+        def place(t):
+            buf = torch.zeros(t.numel() + offset, dtype=t.dtype, device=t.device)
+            v = buf[offset:].view(t.shape)
+            v.copy_(t)
+            return v
+        ini, frc, out = place(f.state), place(forcing), place(torch.zeros_like(f.state))
+        _native.call("mw_dirstage_f32", nx, nz, p["dx"], p["dz"], p["dt"], *hb, src, _native.ptr(ini),
+                     _native.ptr(frc), _native.ptr(out), p["dt"] / 2, direction, flags, _native.stream_handle())
+        torch.cuda.synchronize()
+        return out.clone(), frc.clone()
+
+    n = ctypes.c_ulonglong(1)
+    _native.call("mw_debug_wait_timeouts", ctypes.byref(n), 1)
+    for direction in (0, 1):
+        for flags in (0, 1):
+            bulk_out, bulk_frc = run(0, direction, flags)
+            plain_out, plain_frc = run(1, direction, flags)
+            assert torch.equal(bulk_out[:, 2:-2, 2:-2], plain_out[:, 2:-2, 2:-2]), (direction, flags)
+            assert torch.equal(bulk_frc, plain_frc), (direction, flags)
+    _native.call("mw_debug_wait_timeouts", ctypes.byref(n), 0)
+    assert n.value == 0
+
+
 def test_fullsize_200_steps_vs_oracle():
     """The benchmark's stated criteria at 8192 x 4096 (collision), against the
     oracle (pinned to the reference at small sizes):
