@@ -333,6 +333,34 @@ def roofline(per, cells, bytes_per_value, peak, peak_kind, names, table, sm_mhz=
     return rl
 
 
+def fp64_probe(torch, native, dev, repeats=5):
+    """FP64 pipe throughput of this GPU, measured: mw_fp64_throughput (8
+    independent FMA chains per thread, 4 CTAs of 256 threads per SM), the
+    median of `repeats` runs of ~75 ms each with the SM clock sampled meanwhile.
+    The denominator of fp64_pipe.frac_of_measured."""
+    import ctypes
+    out = ctypes.c_double(0.0)
+    clocks = ClockSampler(device_id_for_smi(torch, dev))
+    clocks.start()
+    vals = []
+    for _ in range(repeats):
+        native.call("mw_fp64_throughput", 4, 2000, ctypes.byref(out), native.stream_handle())
+        vals.append(out.value / 1e9)
+    clk = clocks.stop()
+    return {"gops": round(statistics.median(vals), 1), "runs": [round(v, 1) for v in vals], "clocks": clk,
+            "kernel": "mw_fp64_throughput: 4 x 152 CTAs x 256 threads, 8 independent FP64 FMA chains per thread"}
+
+
+def with_measured_fp64(rl, probe):
+    """Adds the fraction of the measured FP64 pipe throughput to every
+    fp64_pipe block of a roofline dict."""
+    for blk in (rl.get("fp64_pipe"), rl.get("other_kernel", {}).get("fp64_pipe")):
+        if blk and probe and probe.get("gops"):
+            blk["peak_measured_gops"] = probe["gops"]
+            blk["frac_of_measured"] = round(blk["achieved_gops"] / probe["gops"], 4)
+    return rl
+
+
 def e2e_run(torch, p, f, steps, warmup, dist=None):
     """Public API with host buffers: per step, evolve_host() copies the state in
     from pinned host memory, advances it and copies it back out (the FP64 forms
@@ -384,9 +412,11 @@ def form_leg(torch, native, args, mode, dtype, peak, peak_kind, table, sm_mhz, s
     return out
 
 
-def ensemble_run(torch, steps, warmup, dtype, mode, peak):
+def ensemble_run(torch, steps, warmup, dtype, mode, peak, ops_per_cell_stage=None, probe=None):
     """The batching form: 256 thermal members of uneven sizes (nx log-uniform in
-    [64, 1024]), autotuned, two steps per CUDA-graph replay."""
+    [64, 1024]), autotuned, two steps per CUDA-graph replay.  For the IEEE-FP64
+    form also the FP64-pipe rate, from the single-grid kernels' operation
+    counts per cell-stage (the ensemble kernels run the same arithmetic)."""
     from pyminiweather_gb300.ensemble import Ensemble, thermal_ensemble
     ens = Ensemble(thermal_ensemble(256, seed=0), dtype=dtype, f64_mode=mode)
     tuned = ens.autotune(steps=1)
@@ -413,6 +443,12 @@ def ensemble_run(torch, steps, warmup, dtype, mode, peak):
            "roofline": {"bound": "hbm", "bytes_per_cell_step": bpc, "achieved": round(value * bpc / 1e9, 1),
                         "peak": peak, "unit": "GB/s", "frac": round(value * bpc / 1e9 / peak, 4)},
            "tuning": {k: tuned[k] for k in ("z_tile", "grid_x", "grid_z")}}
+    if ops_per_cell_stage:
+        gops = value * 6 * ops_per_cell_stage / 1e9
+        out["roofline"]["fp64_pipe"] = {"achieved_gops": round(gops, 1), "ops_per_cell_stage": ops_per_cell_stage}
+        if probe and probe.get("gops"):
+            out["roofline"]["fp64_pipe"].update(peak_measured_gops=probe["gops"],
+                                                frac_of_measured=round(gops / probe["gops"], 4))
     del ens
     torch.cuda.empty_cache()
     return out
@@ -646,6 +682,8 @@ def run_gb300(args):
     rl["public_step"] = {"achieved": round(step_gbs, 1), "frac": round(step_gbs / peak, 4),
                          "note": "%d algorithmic B per cell-step over the public step's time"
                                  % (STATE_VALUES_PER_CELL_STEP * vbytes)}
+    probe = fp64_probe(torch, _native, dev) if rl.get("fp64_pipe") or not args.no_extras else None
+    with_measured_fp64(rl, probe)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": DTYPES[args.mode],
@@ -653,9 +691,13 @@ def run_gb300(args):
             "config": config_dict(args), "f64_mode": args.mode,
             "roofline": rl, "clocks": clk, "gpu_launches": 6 * args.steps,
             "mass_drift": (m1 - m0) / m0, "bytes_per_cell_step": STATE_VALUES_PER_CELL_STEP * vbytes}
+    if probe:
+        line["fp64_peak_measured"] = probe
     if rl.get("fp64_pipe"):
-        line["limiter"] = "FP64 pipe (%.0f %% of its peak in the dominant kernel; HBM %.0f %%)" % (
-            100 * rl["fp64_pipe"]["frac"], 100 * rl["frac"])
+        line["limiter"] = ("FP64 pipe (dominant kernel at %.0f %% of its nominal peak, %.0f %% of the measured FMA "
+                           "throughput; HBM %.0f %%)" % (100 * rl["fp64_pipe"]["frac"],
+                                                        100 * rl["fp64_pipe"].get("frac_of_measured", 0),
+                                                        100 * rl["frac"]))
     if not args.no_extras:
         line["e2e"] = e2e_line
 
@@ -671,12 +713,16 @@ def run_gb300(args):
                 continue
             line[key] = form_leg(torch, _native, args, mode, dtype, peak, peak_kind, table, sm_mhz, ks,
                                  1 if ks < 3 else args.warmup)
+            with_measured_fp64(line[key]["roofline"], probe)
         line["fp32"]["speedup_vs_fp64"] = line["fp32"]["value"] / (value if args.mode == "fp64"
                                                                    else line["fp64"]["value"])
         if "fp64_dw" in line:
             line["fp32"]["speedup_vs_fp64_dw"] = line["fp32"]["value"] / line["fp64_dw"]["value"]
         # the batching form (ensemble of uneven grids)
-        line["ensemble"] = {"fp64": ensemble_run(torch, args.steps, args.warmup, torch.float64, "fp64", peak),
+        ieee_ops = [table.get(KERNELS["fp64"][d], {}).get("fp64_ops_per_cell") for d in (0, 1)]
+        ieee_ops = round(sum(ieee_ops) / 2, 2) if all(ieee_ops) else None
+        line["ensemble"] = {"fp64": ensemble_run(torch, args.steps, args.warmup, torch.float64, "fp64", peak,
+                                                 ieee_ops, probe),
                             "fp64_dw": ensemble_run(torch, args.steps, args.warmup, torch.float64, "split", peak),
                             "fp32": ensemble_run(torch, args.steps, args.warmup, torch.float32, "fp64", peak)}
         # the differentiation form: adjoint / forward cost

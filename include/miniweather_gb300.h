@@ -295,8 +295,8 @@ int mw_gravity_source_f64(int nx, int nz, double xlen, double zlen, const double
  * mw_stats_workspace_bytes(nx, nz) bytes.
  * ------------------------------------------------------------------------- */
 /* Bounds-checked build (compiled with MW_CHECK=1, python -m pyminiweather_gb300.build
- * --check): the split-form stage, ensemble and adjoint kernels count every array
- * index outside its array instead of accessing it.  mw_debug_oob_count adds up
+ * --check): every kernel of the library counts each array index outside its
+ * array instead of accessing it.  mw_debug_oob_count adds up
  * that count (and resets it if asked); mw_debug_oob_selftest launches one
  * deliberately out-of-range access that the check diverts (the count goes up by
  * one).  Both fail with MW_ERR_INVALID_ARG in the normal build. */
@@ -304,10 +304,18 @@ int mw_debug_oob_count(unsigned long long* count, int reset);
 int mw_debug_oob_selftest(void* stream);
 
 /* Bounded waits: the kernels that wait on an mbarrier for asynchronous copies
- * (the FP32 z pass) give up after a bounded number of rounds instead of
+ * (the FP32 x and z passes) give up after a bounded number of rounds instead of
  * hanging, abandon their tile and count it here; *count receives the count
  * (reset to 0 if asked).  Zero unless a copy failed to arrive. */
 int mw_debug_wait_timeouts(unsigned long long* count, int reset);
+
+/* FP64 pipe throughput of the current device (no counterpart in the
+ * reference; the denominator of the FP64-pipe roofline of the IEEE-FP64
+ * form): blocks_per_sm x SMs CTAs of 256 threads, each thread 8 independent
+ * FMA chains of iters x 16 steps, timed with CUDA events on `stream`; blocks
+ * until done.  *ops_per_second receives FP64 operations per second (an FMA
+ * counts as one operation, as in the kernels' operation counts). */
+int mw_fp64_throughput(int blocks_per_sm, int iters, double* ops_per_second, void* stream);
 
 /* Count the non-finite (NaN, +-Inf) interior values of a (4, nz+4, nx+4)
  * state into *count (a device counter, added to, not reset); no host sync. */

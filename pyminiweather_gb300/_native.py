@@ -62,6 +62,7 @@ _SIGNATURES = {
     "mw_debug_oob_count": [_P, _i],
     "mw_debug_oob_selftest": [_P],
     "mw_debug_wait_timeouts": [_P, _i],
+    "mw_fp64_throughput": [_i, _i, _P, _P],
     "mw_count_nonfinite_f32": [_i, _i, _P, _P, _P],
     "mw_savetxt_f64": [_P, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_char_p, _i, _i],
     "mw_set_bc_f64": [_i, _i, _P, _P, _i, _P],

@@ -98,3 +98,66 @@ extern "C" int mw_debug_oob_selftest(void* stream) {
 #endif
 }
 
+
+// ---------------------------------------------------------------------------
+// FP64 pipe throughput: the denominator of the FP64-pipe roofline, measured on
+// the device at hand.  Every thread runs 8 independent chains of FP64 FMAs
+// (a <- a m + p), so each warp always has an FP64 instruction ready.
+namespace mw {
+namespace {
+constexpr int kProbeThreads = 256;
+constexpr int kProbeChains = 8;
+constexpr int kProbeUnroll = 16;
+__device__ double g_probe_sink;
+__global__ void __launch_bounds__(kProbeThreads) k_fp64_throughput(int iters) {
+  double a[kProbeChains];
+#pragma unroll
+  for (int c = 0; c < kProbeChains; ++c) a[c] = 1.0 + 1e-3 * (threadIdx.x + c);
+  const double m = 0.999999, p = 1e-9;
+  for (int it = 0; it < iters; ++it)
+#pragma unroll
+    for (int r = 0; r < kProbeUnroll; ++r)
+#pragma unroll
+      for (int c = 0; c < kProbeChains; ++c) a[c] = fma(a[c], m, p);
+  double s = 0.0;
+#pragma unroll
+  for (int c = 0; c < kProbeChains; ++c) s += a[c];
+  if (s == -1.0) g_probe_sink = s;  // never true (s > 0): keeps the chains live without a store per thread
+}
+}  // namespace
+}  // namespace mw
+
+extern "C" int mw_fp64_throughput(int blocks_per_sm, int iters, double* ops_per_second, void* stream) {
+  using namespace mw;
+  MW_REQUIRE(ops_per_second != nullptr, MW_ERR_INVALID_ARG, "ops_per_second must not be NULL");
+  MW_REQUIRE(blocks_per_sm >= 1 && blocks_per_sm <= 8, MW_ERR_INVALID_ARG, "blocks_per_sm must be in [1, 8]");
+  MW_REQUIRE(iters >= 1 && iters <= (1 << 16), MW_ERR_INVALID_ARG, "iters must be in [1, 65536]");
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return fail(MW_ERR_CUDA, "device query: %s", cudaGetErrorString(e));
+  cudaStream_t s = (cudaStream_t)stream;
+  const int blocks = blocks_per_sm * sms;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  if (e == cudaSuccess) {
+    k_fp64_throughput<<<blocks, kProbeThreads, 0, s>>>(iters / 8 + 1);  // warm-up
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(e0, s);
+  if (e == cudaSuccess) {
+    k_fp64_throughput<<<blocks, kProbeThreads, 0, s>>>(iters);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  float ms = 0.0f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (e != cudaSuccess) return fail(MW_ERR_CUDA, "FP64 throughput probe: %s", cudaGetErrorString(e));
+  const double ops = (double)blocks * kProbeThreads * (double)iters * kProbeUnroll * kProbeChains;
+  *ops_per_second = ms > 0.0f ? ops / (ms * 1e-3) : 0.0;
+  return MW_OK;
+}

@@ -447,8 +447,13 @@ __global__ void __launch_bounds__(kZThreads) k_stage_z(StageArgs<T> a, int tile0
 // thread 0 refills its slot with the block kBulkStages further on.  Forcing
 // rows outside [0, nz) are never copied: the wall rule builds them from the
 // register window.
-constexpr int kBulkRows = 4;
-constexpr int kBulkStages = 4;
+#ifndef MW_BZ_STAGES
+#define MW_BZ_STAGES 3
+#endif
+constexpr int kBulkRows = 4;  // >= 4: the window's next row (4 rows ahead) then lies in block b + 1
+constexpr int kBulkStages = MW_BZ_STAGES;  // ring slots (3: 51.7 KB of shared memory, 4 CTAs per SM;
+                                           // 4 slots, 3 CTAs per SM, measured 5 % slower)
+static_assert(kBulkStages >= 3, "the march waits for block b + 1 before refilling block b - 1's slot");
 constexpr int kBulkCols = kZThreads + 4;  // 132 floats = 528 bytes, a multiple of 16
 constexpr long long kBulkSpin = 1LL << 20;  // try_wait rounds before a wait gives up
 constexpr unsigned kBulkBoxBytes = 4u * kBulkRows * kBulkCols * 4;  // one array's box: 4 variables x rows x columns
@@ -618,32 +623,41 @@ __global__ void __launch_bounds__(kZThreads) k_stage_z_f32_bulk(StageArgs<float>
 }
 
 // FP32 x pass fed by the tensor memory accelerator.  The row-major list of
-// kBXCells-cell chunks is split into equal ranges, one per CTA; per chunk one
-// 3-D tensor copy per array of kBXCols columns x 1 row x 4 variables
-// (halo-indexed columns [x0, x0 + kBXCols): cells x0 - 2 .. x0 + kBXCells + 1,
-// starting at a 16-byte boundary since x0 is a multiple of 4) lands in a ring of
-// kBXStages slots.  Thread t evaluates the flux at interface x0 + t from the
-// slot (taps outside [0, nx), at the two ends of a row, are read from global
-// memory with the periodic rule: the halo columns are never trusted) into a
-// double-buffered flux array; after one CTA barrier per chunk, thread t
-// updates cell x0 + t, and thread 0 refills the slot of the previous chunk.
-// Waits are bounded as in the z pass.
+// kBXCells-cell chunks is split into equal ranges, one per CTA of kBXThreads
+// threads; per chunk one 3-D tensor copy per array of kBXCols columns x 1 row
+// x 4 variables (halo-indexed columns [x0, x0 + kBXCols): cells x0 - 2 ..
+// x0 + kBXCells + 1, starting at a 16-byte boundary since x0 is a multiple of
+// 4) lands in a ring of kBXStages slots.  Thread t owns cells x0 + 4t ..
+// x0 + 4t + 3: it reads their taps (cells x0 + 4t - 2 .. x0 + 4t + 5) as two
+// 16-byte words per variable, evaluates the fluxes at its five interfaces
+// x0 + 4t .. x0 + 4t + 4 (the last one again by thread t + 1: no flux
+// exchange, no flux array) and updates its four cells.  Taps beyond a row end
+// come from global memory with the periodic rule (halo columns are never
+// trusted).  One CTA barrier per chunk, after which thread 0 refills the
+// previous chunk's slot; waits are bounded as in the z pass.
 constexpr int kBXCells = 252;
-constexpr int kBXCols = kBXCells + 4;  // 256 floats = 1 KB per variable
-constexpr int kBXStages = 4;
+constexpr int kBXCols = kBXCells + 4;    // 256 floats = 1 KB per variable
+constexpr int kBXThreads = 64;           // 63 own four cells each; the last is idle
+#ifndef MW_BX_STAGES
+#define MW_BX_STAGES 2
+#endif
+constexpr int kBXStages = MW_BX_STAGES;  // ring slots (2: 16.4 KB of shared memory per CTA; 3 or 4
+                                         // slots, fewer CTAs per SM, measured 3-6 % slower; at most 5,
+                                         // within the 48 KB a launch gets without an attribute)
+static_assert(kBXStages >= 2, "chunk b's copies are issued before chunk b - 1's slot is refilled");
+static_assert(kBXStages <= 5, "the x kernel's shared memory must stay within the default 48 KB");
 constexpr unsigned kBXBoxBytes = 4u * kBXCols * 4;  // one array's box: 4 variables x 256 floats
-static_assert(kBXCells % 4 == 0 && kBXCells + 1 <= kXThreads, "x chunk layout");
+static_assert(kBXCells % 4 == 0 && kBXCells / 4 <= kBXThreads, "x chunk layout");
 
 struct SmemXBulk {
-  float f[kBXStages][4][kBXCols];  // forcing
-  float i[kBXStages][4][kBXCols];  // init
-  float sF[2][4][kXThreads];       // interface fluxes, by chunk parity
+  float4 f[kBXStages][4][kBXCols / 4];  // forcing
+  float4 i[kBXStages][4][kBXCols / 4];  // init
   unsigned long long full[kBXStages];
 };
 
-__global__ void __launch_bounds__(kXThreads) k_stage_x_f32_bulk(StageArgs<float> a, long long total, int cpr,
-                                                                 const __grid_constant__ CUtensorMap tmf,
-                                                                 const __grid_constant__ CUtensorMap tmi) {
+__global__ void __launch_bounds__(kBXThreads) k_stage_x_f32_bulk(StageArgs<float> a, long long total, int cpr,
+                                                                  const __grid_constant__ CUtensorMap tmf,
+                                                                  const __grid_constant__ CUtensorMap tmi) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   SmemXBulk& sm = *reinterpret_cast<SmemXBulk*>(smem_raw);
   const int t = threadIdx.x;
@@ -695,7 +709,7 @@ __global__ void __launch_bounds__(kXThreads) k_stage_x_f32_bulk(StageArgs<float>
       ++k;
     }
     const int x0 = cc * kBXCells;
-    const int s = b % kBXStages, fb = b & 1;
+    const int s = b % kBXStages;
     const long long row = (long long)(k + kHs) * a.pitch;
     if (k != rk) {
       rk = k;
@@ -703,44 +717,66 @@ __global__ void __launch_bounds__(kXThreads) k_stage_x_f32_bulk(StageArgs<float>
     }
     const bool w_ok = mbar_wait_bounded(&sm.full[s], (b / kBXStages) & 1);
     if (w_ok) waited = b + 1;
-    const int i = x0 + t;  // interface between cells i - 1 and i
-    if (w_ok && t <= kBXCells && i <= a.nx) {
-      float sv[4][4];
-      if (i >= 2 && i + 1 < a.nx) {
-#pragma unroll
-        for (int jj = 0; jj < 4; ++jj)
-#pragma unroll
-          for (int q = 0; q < 4; ++q) sv[q][jj] = sm.f[s][q][t + jj];
-      } else {  // a tap beyond a row end: the periodic rule, from global memory
-#pragma unroll
-        for (int jj = 0; jj < 4; ++jj) {
-          const long long col = wrap_x(i - 2 + jj, a.nx) + kHs;
-#pragma unroll
-          for (int q = 0; q < 4; ++q) sv[q][jj] = __ldg(&MW_SF(a, q * a.plane + row + col));
-        }
-      }
-      float F[4];
-      flux_x_f32(sv, rc, a.hv_f, F);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) sm.sF[fb][q][t] = F[q];
-    }
-    if (w_ok && halo && x0 == 0 && t < 4) {  // this row's periodic halo of the forcing array (ics/bcs.py:35-39)
+    ok = __syncthreads_and(w_ok);  // every thread is done with chunk b - 1
+    if (!ok) break;
+    if (t == 0 && b >= 1 && issued < n) issue(issued++);  // refill chunk b - 1's slot
+    if (halo && x0 == 0 && t < 4) {  // this row's periodic halo of the forcing array (ics/bcs.py:35-39)
       const int dst = t < 2 ? t : a.nx + t;  // columns 0, 1, nx+2, nx+3
       const int src = t < 2 ? a.nx + t : t;  // columns nx, nx+1, 2, 3
 #pragma unroll
       for (int q = 0; q < 4; ++q) MW_SF(a, q * a.plane + row + dst) = MW_SF(a, q * a.plane + row + src);
     }
-    ok = __syncthreads_and(w_ok);  // fluxes visible; every thread is done with chunk b - 1
-    if (!ok) break;
-    if (t == 0 && b >= 1 && issued < n) issue(issued++);  // refill chunk b - 1's slot
-    if (t < kBXCells && i < a.nx) {
-      float inc[4];
+    const int c0 = x0 + 4 * t;  // first cell of this thread (nx and x0 are multiples of 4: all four or none)
+    if (t < kBXCells / 4 && c0 < a.nx) {
+      float tap[4][8];  // cells c0 - 2 .. c0 + 5
+      if (c0 >= 2 && c0 + 5 < a.nx) {
 #pragma unroll
-      for (int q = 0; q < 4; ++q) inc[q] = (sm.sF[fb][q][t] - sm.sF[fb][q][t + 1]) * c;
-      if (a.srcw) inc[WMOM] += dt * split::d2f(MW_SW(a, (long long)k * a.nx + i));
-      const long long o = row + i + kHs;
+        for (int q = 0; q < 4; ++q) {
+          const float4 lo = sm.f[s][q][t], hi = sm.f[s][q][t + 1];
+          tap[q][0] = lo.x, tap[q][1] = lo.y, tap[q][2] = lo.z, tap[q][3] = lo.w;
+          tap[q][4] = hi.x, tap[q][5] = hi.y, tap[q][6] = hi.z, tap[q][7] = hi.w;
+        }
+      } else {  // a tap beyond a row end: the periodic rule, from global memory
 #pragma unroll
-      for (int q = 0; q < 4; ++q) MW_SO(a, q * a.plane + o) = sm.i[s][q][t + 2] + inc[q];
+        for (int jj = 0; jj < 8; ++jj) {
+          const long long col = wrap_x(c0 - 2 + jj, a.nx) + kHs;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) tap[q][jj] = __ldg(&MW_SF(a, q * a.plane + row + col));
+        }
+      }
+      float F[5][4];  // fluxes at interfaces c0 .. c0 + 4
+#pragma unroll
+      for (int f = 0; f < 5; ++f) {
+        float sv[4][4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+          for (int jj = 0; jj < 4; ++jj) sv[q][jj] = tap[q][f + jj];
+        flux_x_f32(sv, rc, a.hv_f, F[f]);
+      }
+      float iv[4][4];  // init of cells c0 .. c0 + 3 (halo-indexed columns 4t + 2 .. 4t + 5 of the box)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float4 lo = sm.i[s][q][t], hi = sm.i[s][q][t + 1];
+        iv[q][0] = lo.z, iv[q][1] = lo.w, iv[q][2] = hi.x, iv[q][3] = hi.y;
+      }
+      const long long o = row + c0 + kHs;  // 8-byte aligned: two floats per store
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        float inc[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) inc[q] = (F[m][q] - F[m + 1][q]) * c;
+        if (a.srcw) inc[WMOM] += dt * split::d2f(MW_SW(a, (long long)k * a.nx + c0 + m));
+#pragma unroll
+        for (int q = 0; q < 4; ++q) iv[q][m] = iv[q][m] + inc[q];
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        float2* dst = reinterpret_cast<float2*>(&MW_SO(a, q * a.plane + o));
+        float2* dst2 = reinterpret_cast<float2*>(&MW_SO(a, q * a.plane + o + 2));
+        *dst = make_float2(iv[q][0], iv[q][1]);
+        *dst2 = make_float2(iv[q][2], iv[q][3]);
+      }
     }
   }
   if (!ok && t == 0) {  // a copy never completed: count it, and let none land after the CTA exits
@@ -923,7 +959,7 @@ static int bulk_x_resident(int* out) {
   const bool cached = dev >= 0 && dev < 64;
   if (cached && (*out = cache[dev].load(std::memory_order_relaxed)) > 0) return MW_OK;
   int per_sm = 0, sms = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage_x_f32_bulk, kXThreads,
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage_x_f32_bulk, kBXThreads,
                                                                 sizeof(SmemXBulk));
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return fail(MW_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
@@ -995,9 +1031,9 @@ static int launch_stage(int nx, int nz, double dx, double dz, double dt_full, co
   a.z_tile = z_tile_rows(nx, nz, kZThreads, kZTile);
   set_f32_constants(a, direction);
   // FP32: tiles staged by tensor copies, which start at 16-byte boundaries of
-  // 4-float-aligned rows
+  // 4-float-aligned rows (the x pass also stores pairs of floats)
   const bool bulk = MODE == MODE_F32 && MW_F32_BULK && nx % 4 == 0 && nx >= kZThreads &&
-                    ((uintptr_t)init % 16) == 0 && ((uintptr_t)forcing % 16) == 0;
+                    ((uintptr_t)init % 16) == 0 && ((uintptr_t)forcing % 16) == 0 && ((uintptr_t)out % 16) == 0;
   if (direction == MW_DIR_X) {
     if constexpr (MODE == MODE_F32) {
       if (bulk) {
@@ -1010,7 +1046,7 @@ static int launch_stage(int nx, int nz, double dx, double dz, double dt_full, co
         const int cpr = (nx + kBXCells - 1) / kBXCells;
         const long long total = (long long)cpr * nz;
         const long long grid = std::min<long long>(total, resident);
-        k_stage_x_f32_bulk<<<(unsigned)grid, kXThreads, sizeof(SmemXBulk), stream>>>(a, total, cpr, tmf, tmi);
+        k_stage_x_f32_bulk<<<(unsigned)grid, kBXThreads, sizeof(SmemXBulk), stream>>>(a, total, cpr, tmf, tmi);
         return check_launch("x direction-stage launch");
       }
     }

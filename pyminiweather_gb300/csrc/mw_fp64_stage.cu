@@ -10,7 +10,7 @@
 // integer work (conversions, index arithmetic, table look-ups) is nearly free.
 // Against the reference's formulas (one pow, three divides and ~50 operations
 // per interface, interpolate.py:82-186) each interface costs ~37 + n FP64
-// operations and each cell update 8 (ncu: 49.7 per cell-stage in x, 50.7 in
+// operations and each cell update 8 (ncu: 48.7 per cell-stage in x, 49.7 in
 // z on the collision case):
 //   - quantities are carried scaled by 12, so the 4-point interpolation is
 //     A = 7 (s1 + s2) - (s0 + s3) and needs no division; the third
@@ -194,7 +194,6 @@ constexpr int kXWarps = kXT / 32;
 constexpr int kXRowsMax = 64;       // rows of one CTA's range
 struct SmemXW {
   double sS[kXWarps][4][kWI + 4];   // [warp][variable][cell x0-2 .. x0+64]
-  RowD row[kXRowsMax];
 };
 
 // Walks the segments [g0, g1) of the row-major list of kWCells-cell segments
@@ -206,9 +205,8 @@ template <typename RowAt, typename Prologue>
 __device__ __forceinline__ void x_warp_walk(const Args& a, int nseg, long long g0, long long g1, RowAt row_at,
                                             bool halo, double (*sS)[kWI + 4], Prologue prologue) {
   const int lane = threadIdx.x & 31;
-  // values of segment g: cells x0-2+lane, x0+30+lane and (lanes 0..2) x0+62+lane
-  auto load = [&](long long g, double v[3][4]) {
-    const int k = (int)(g / nseg), x0 = (int)(g - (long long)k * nseg) * kWCells;
+  // values of the segment in row k at x0: cells x0-2+lane, x0+30+lane and (lanes 0..2) x0+62+lane
+  auto load = [&](int k, int x0, double v[3][4]) {
     const long long row = (long long)(k + kHs) * a.pitch;
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
@@ -220,11 +218,15 @@ __device__ __forceinline__ void x_warp_walk(const Args& a, int nseg, long long g
       }
     }
   };
+  // (row, segment in row) of the current segment, advanced incrementally (one
+  // 64-bit division per walk, not per segment)
+  int k = (int)(g0 / nseg), sg = (int)(g0 - (long long)k * nseg);
   double v[3][4] = {};
-  if (g0 < g1) load(g0, v);
+  if (g0 < g1) load(k, sg * kWCells, v);
   prologue();
   for (long long g = g0; g < g1; ++g) {
-    const int k = (int)(g / nseg), sg = (int)(g - (long long)k * nseg), x0 = sg * kWCells;
+    const int x0 = sg * kWCells;
+    const int kn = sg + 1 == nseg ? k + 1 : k, sgn = sg + 1 == nseg ? 0 : sg + 1;  // the next segment
     const long long row = (long long)(k + kHs) * a.pitch;
     __syncwarp();  // the previous segment's taps are read
 #pragma unroll
@@ -237,7 +239,7 @@ __device__ __forceinline__ void x_warp_walk(const Args& a, int nseg, long long g
 #pragma unroll
       for (int q = 0; q < 4; ++q) MW_F(a, q * a.plane + row + dst) = MW_F(a, q * a.plane + row + src);
     }
-    if (g + 1 < g1) load(g + 1, v);
+    if (g + 1 < g1) load(kn, sgn * kWCells, v);
     const int ia = x0 + lane, ib = x0 + 32 + lane;  // interfaces (and cells) of this lane
     const bool ua = ia < a.nx, ub = lane < 31 && ib < a.nx;
     double iva[4], ivb[4];
@@ -247,7 +249,7 @@ __device__ __forceinline__ void x_warp_walk(const Args& a, int nseg, long long g
       if (ub) ivb[q] = MW_AT(a.init, q * a.plane + row + ib + kHs, 4 * a.plane);
     }
     __syncwarp();
-    const RowD rc = row_at(k);
+    const auto& rc = row_at(k);
     double Fa[4] = {0, 0, 0, 0}, Fb[4] = {0, 0, 0, 0};
     const unsigned ma = __ballot_sync(0xffffffffu, ia <= a.nx), mb = __ballot_sync(0xffffffffu, ib <= a.nx);
     if (ia <= a.nx) {
@@ -289,6 +291,8 @@ __device__ __forceinline__ void x_warp_walk(const Args& a, int nseg, long long g
 #pragma unroll
       for (int q = 0; q < 4; ++q) MW_AT(a.out, q * a.plane + row + ib + kHs, 4 * a.plane) = o[q];
     }
+    k = kn;
+    sg = sgn;
   }
 }
 
@@ -301,16 +305,18 @@ __device__ __forceinline__ void x_warp_walk(const Args& a, int nseg, long long g
 __global__ void __launch_bounds__(kXT, MW_IEEE_X_MIN_BLOCKS) k_stage_x_ieee_w(Args a, int nseg, long long total,
                                                                                long long gbase) {
   __shared__ SmemXW sm;
+  __shared__ RowD rows[kXRowsMax];
   const long long g0 = gbase + total * blockIdx.x / gridDim.x, g1 = gbase + total * (blockIdx.x + 1) / gridDim.x;
   if (g0 >= g1) return;
   const int row0 = (int)(g0 / nseg), nrows = (int)((g1 - 1) / nseg) - row0 + 1;  // nrows <= kXRowsMax (host)
   const int w = threadIdx.x >> 5;
   const long long n = g1 - g0;
-  x_warp_walk(a, nseg, g0 + n * w / kXWarps, g0 + n * (w + 1) / kXWarps, [&](int k) { return sm.row[k - row0]; },
+  x_warp_walk(a, nseg, g0 + n * w / kXWarps, g0 + n * (w + 1) / kXWarps,
+              [&](int k) -> const RowD& { return rows[k - row0]; },
               a.flags & MW_FLAG_WRITE_HALO, sm.sS[w], [&]() {
                 for (int r = threadIdx.x; r < nrows; r += kXT) {
                   const double rt = MW_AT(a.hytc, row0 + r + kHs, a.nz + 2 * kHs);
-                  sm.row[r] = row_consts(MW_AT(a.hyc, row0 + r + kHs, a.nz + 2 * kHs), rt, kC0 * pow(rt, kGamma));
+                  rows[r] = row_consts(MW_AT(a.hyc, row0 + r + kHs, a.nz + 2 * kHs), rt, kC0 * pow(rt, kGamma));
                 }
                 __syncthreads();
               });
@@ -446,7 +452,8 @@ __global__ void __launch_bounds__(kXT, MW_IEEE_X_MIN_BLOCKS) k_ens_x_ieee(EnsSta
     const int nseg = (a.nx + kWCells - 1) / kWCells;
     const RowD r = MW_AT(reinterpret_cast<const RowD*>(es.xrows),
                          MW_AT(es.members, item.x, es.n_members).cell_off + item.y + kHs, es.n_xrows);
-    x_warp_walk(a, nseg, (long long)item.y * nseg, (long long)(item.y + 1) * nseg, [&](int) { return r; },
+    x_warp_walk(a, nseg, (long long)item.y * nseg, (long long)(item.y + 1) * nseg,
+                [&](int) -> const RowD& { return r; },
                 a.flags & MW_FLAG_WRITE_HALO, sm.sS[w], []() {});
   }
 }

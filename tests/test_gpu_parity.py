@@ -242,15 +242,20 @@ def test_fp32_form_error_and_mass():
 def test_fp32_tensor_copy_kernels_match_plain_loads(nx, nz, ic):
     """The FP32 stages whose tiles are staged by tensor copies (arrays 16-byte
     aligned, nx % 4 == 0, nx >= 128) against the plain-load kernels, which the
-    library uses for the same arrays offset by one float: identical results,
-    halo writes included, in both directions (rows of one and of several
-    chunks, the periodic taps at both row ends, the gravity forcing)."""
+    library uses for the same arrays offset by one float, in both directions
+    (rows of one and of several chunks, the periodic taps at both row ends, the
+    gravity forcing).  The x pass evaluates its fluxes in another code shape, so
+    the compiler's FMA contraction may differ: both FP32 results are held
+    against the IEEE-FP64 stage on the same inputs, the tensor-copy one within
+    twice the plain one's error (plus 1e-6 of the variable's range); the halo
+    writes are identical bit for bit."""
     import ctypes
     p, f = setup(ic, nx, nz, dtype=torch.float32)
     evolve(p, f, None, dt=p["dt"], nsteps=3)
     forcing = f.state + 1e-3 * torch.randn(f.state.shape, generator=torch.Generator().manual_seed(5)).to(f.state)
     hb = [_native.ptr(a) for a in f.backgrounds()]
     src = _native.ptr(f.src_w) if ic == "gravity" else None
+    S = _native.stream_handle()
 
     def run(offset, direction, flags):
         def place(t):
@@ -260,17 +265,30 @@ def test_fp32_tensor_copy_kernels_match_plain_loads(nx, nz, ic):
             return v
         ini, frc, out = place(f.state), place(forcing), place(torch.zeros_like(f.state))
         _native.call("mw_dirstage_f32", nx, nz, p["dx"], p["dz"], p["dt"], *hb, src, _native.ptr(ini),
-                     _native.ptr(frc), _native.ptr(out), p["dt"] / 2, direction, flags, _native.stream_handle())
+                     _native.ptr(frc), _native.ptr(out), p["dt"] / 2, direction, flags, S)
         torch.cuda.synchronize()
         return out.clone(), frc.clone()
+
+    def ref64(direction):
+        ini, frc = f.state.double(), forcing.double()
+        out = torch.zeros_like(ini)
+        _native.call("mw_dirstage_f64", nx, nz, p["dx"], p["dz"], p["dt"], *hb, src, _native.ptr(ini),
+                     _native.ptr(frc), _native.ptr(out), p["dt"] / 2, direction, _native.F64_MODES["fp64"], 0, S)
+        torch.cuda.synchronize()
+        return host(out)
 
     n = ctypes.c_ulonglong(1)
     _native.call("mw_debug_wait_timeouts", ctypes.byref(n), 1)
     for direction in (0, 1):
+        r = ref64(direction)
         for flags in (0, 1):
             bulk_out, bulk_frc = run(0, direction, flags)
             plain_out, plain_frc = run(1, direction, flags)
-            assert torch.equal(bulk_out[:, 2:-2, 2:-2], plain_out[:, 2:-2, 2:-2]), (direction, flags)
+            eb, ep = normwise(host(bulk_out), r), normwise(host(plain_out), r)
+            print("%dx%d %s direction %d flags %d: vs IEEE FP64 tensor-copy %s plain-load %s identical %s"
+                  % (nx, nz, ic, direction, flags, ["%.1e" % e for e in eb], ["%.1e" % e for e in ep],
+                     bool(torch.equal(bulk_out, plain_out))))
+            assert all(b <= 2 * q + 1e-6 for b, q in zip(eb, ep)), (direction, flags, eb, ep)
             assert torch.equal(bulk_frc, plain_frc), (direction, flags)
     _native.call("mw_debug_wait_timeouts", ctypes.byref(n), 0)
     assert n.value == 0
