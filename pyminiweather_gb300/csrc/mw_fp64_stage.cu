@@ -10,8 +10,8 @@
 // integer work (conversions, index arithmetic, table look-ups) is nearly free.
 // Against the reference's formulas (one pow, three divides and ~50 operations
 // per interface, interpolate.py:82-186) each interface costs ~37 + n FP64
-// operations and each cell update 8 (ncu: 48.7 per cell-stage in x, 49.7 in
-// z on the collision case):
+// operations and each cell update 8 (ncu: 47.8 per cell-stage in x on the
+// collision case):
 //   - quantities are carried scaled by 12, so the 4-point interpolation is
 //     A = 7 (s1 + s2) - (s0 + s3) and needs no division; the third
 //     difference is D = (s3 - s0) + 3 (s1 - s2): 6 operations per variable;
@@ -24,7 +24,9 @@
 //     series summed by Horner's rule to the degree n that the warp's largest
 //     |delta| needs for a truncation below 2^-54 relative (one FMA in a
 //     region at rest, up to 15 terms for |delta| < 1/8), and
-//     expm1(gamma log1p(delta)) beyond;
+//     expm1(gamma log1p(delta)) beyond; the single-grid kernels evaluate it
+//     as a polynomial in 12 (rho theta)' with per-row coefficients (RowP), n
+//     operations in all;
 //   - the stage update is out = init + c (F(i) - F(i+1)), c = dt / (12 d):
 //     2 operations per value.
 //
@@ -86,6 +88,50 @@ __device__ __forceinline__ double pressure(double AT, const RowD& r, double add,
   return fma(r.P12, f, add);
 }
 
+// Row constants with the pressure series as a polynomial in the interpolated
+// 12 (rho theta)' itself: b[n] = P12 C(gamma, n) IRT12^n, so that
+// P12 ((1 + d)^gamma - 1) = sum_n b[n] AT^n (d = AT IRT12) is Horner's rule in
+// AT with no multiplication by IRT12 before it and none by P12 after it: two
+// FP64 operations fewer per interface wherever the degree exceeds one.
+struct RowP {
+  RowD d;
+  double b[kMaxDeg + 1];  // b[0] unused
+  int eI;                 // biased exponent of IRT12; 4096 where the b[n] would leave the normal range
+};
+__device__ __forceinline__ RowP row_consts_p(double r, double rt, double P) {
+  RowP o;
+  o.d = row_consts(r, rt, P);
+  double pw = o.d.IRT12;
+  o.b[0] = 0.0;
+#pragma unroll
+  for (int n = 1; n <= kMaxDeg; ++n) {
+    o.b[n] = o.d.P12 * c_pow_g.c[n] * pw;
+    pw *= o.d.IRT12;
+  }
+  const double lo = fabs(o.b[kMaxDeg]), hi = fabs(o.b[1]);
+  const bool normal = lo >= 0x1p-1000 && hi <= 0x1p1000 && pw >= 0x1p-1000;
+  o.eI = normal ? (int)((unsigned long long)__double_as_longlong(o.d.IRT12) >> 52 & 0x7ffu) : 4096;
+  return o;
+}
+
+// The same as pressure(AT, r.d, add, mask), evaluated in AT: the degree comes
+// from a bound on the exponent of d = AT IRT12 (the sum of the exponents of AT
+// and IRT12, plus one), never below the degree d itself needs; warps where the
+// bound reaches 1/8 (and Inf, NaN, rows with eI = 4096) take the series in d.
+__device__ __forceinline__ double pressure(double AT, const RowP& r, double add, unsigned mask) {
+  const int exA = (int)((unsigned long long)__double_as_longlong(AT) >> 52 & 0x7ffu);
+  const int eu = exA == 0 ? 0 : exA + r.eI - 1022;  // biased exponent of d is at most eu
+  if (__any_sync(mask, eu >= 1020)) return pressure(AT, r.d, add, mask);
+  const int exm = (int)__reduce_max_sync(mask, (unsigned)max(eu, 0));
+  const int n = c_pow_g.deg[min(1022 - exm, 64)];
+  double g = r.b[n];
+  for (int k = n - 1; k >= 1; --k) g = fma(g, AT, r.b[k]);
+  return fma(g, AT, add);
+}
+
+__device__ __forceinline__ const RowD& rowd(const RowD& r) { return r; }
+__device__ __forceinline__ const RowD& rowd(const RowP& r) { return r.d; }
+
 // 12 x the 4-point interpolation and the third difference of one variable
 // (the stencils of interpolate.py:33-43 and 69-79).
 __device__ __forceinline__ void interp(double s0, double s1, double s2, double s3, double& A, double& D) {
@@ -95,20 +141,22 @@ __device__ __forceinline__ void interp(double s0, double s1, double s2, double s
 
 // x flux times 12 (interpolate.py:82-129): with u = (rho u)' / rho,
 // F = ((rho u)', u (rho u)' + p', u (rho w)', u (rho theta)) - hv d3, HV = -12 hv.
-__device__ __forceinline__ void flux_x(const double s[4][4], const RowD& r, double HV, unsigned mask, double F[4]) {
+template <typename Row>
+__device__ __forceinline__ void flux_x(const double s[4][4], const Row& r, double HV, unsigned mask, double F[4]) {
   double A[4], D[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) interp(s[q][0], s[q][1], s[q][2], s[q][3], A[q], D[q]);
-  const double ri = rcp(A[DENS] + r.R12, mask);
+  const double ri = rcp(A[DENS] + rowd(r).R12, mask);
   const double u = A[UMOM] * ri;
   F[0] = fma(HV, D[DENS], A[UMOM]);
   F[1] = fma(A[UMOM], u, pressure(A[RHOT], r, HV * D[UMOM], mask));
   F[2] = fma(u, A[WMOM], HV * D[WMOM]);
-  F[3] = fma(u, A[RHOT] + r.RT12, HV * D[RHOT]);
+  F[3] = fma(u, A[RHOT] + rowd(r).RT12, HV * D[RHOT]);
 }
 
 // z flux times 12 (interpolate.py:132-186); w and d3[DENS] vanish at the walls.
-__device__ __forceinline__ void flux_z(const double s[4][4], const RowD& r, double HV, bool wall, unsigned mask,
+template <typename Row>
+__device__ __forceinline__ void flux_z(const double s[4][4], const Row& r, double HV, bool wall, unsigned mask,
                                        double F[4]) {
   double A[4], D[4];
 #pragma unroll
@@ -118,12 +166,12 @@ __device__ __forceinline__ void flux_z(const double s[4][4], const RowD& r, doub
     AW = 0.0;
     D[DENS] = 0.0;
   }
-  const double ri = rcp(A[DENS] + r.R12, mask);
+  const double ri = rcp(A[DENS] + rowd(r).R12, mask);
   const double w = AW * ri;
   F[0] = fma(HV, D[DENS], AW);
   F[1] = fma(w, A[UMOM], HV * D[UMOM]);
   F[2] = fma(AW, w, pressure(A[RHOT], r, HV * D[WMOM], mask));
-  F[3] = fma(w, A[RHOT] + r.RT12, HV * D[RHOT]);
+  F[3] = fma(w, A[RHOT] + rowd(r).RT12, HV * D[RHOT]);
 }
 
 // ---- arguments -------------------------------------------------------------
@@ -305,18 +353,18 @@ __device__ __forceinline__ void x_warp_walk(const Args& a, int nseg, long long g
 __global__ void __launch_bounds__(kXT, MW_IEEE_X_MIN_BLOCKS) k_stage_x_ieee_w(Args a, int nseg, long long total,
                                                                                long long gbase) {
   __shared__ SmemXW sm;
-  __shared__ RowD rows[kXRowsMax];
+  __shared__ RowP rows[kXRowsMax];
   const long long g0 = gbase + total * blockIdx.x / gridDim.x, g1 = gbase + total * (blockIdx.x + 1) / gridDim.x;
   if (g0 >= g1) return;
   const int row0 = (int)(g0 / nseg), nrows = (int)((g1 - 1) / nseg) - row0 + 1;  // nrows <= kXRowsMax (host)
   const int w = threadIdx.x >> 5;
   const long long n = g1 - g0;
   x_warp_walk(a, nseg, g0 + n * w / kXWarps, g0 + n * (w + 1) / kXWarps,
-              [&](int k) -> const RowD& { return rows[k - row0]; },
+              [&](int k) -> const RowP& { return rows[k - row0]; },
               a.flags & MW_FLAG_WRITE_HALO, sm.sS[w], [&]() {
                 for (int r = threadIdx.x; r < nrows; r += kXT) {
                   const double rt = MW_AT(a.hytc, row0 + r + kHs, a.nz + 2 * kHs);
-                  rows[r] = row_consts(MW_AT(a.hyc, row0 + r + kHs, a.nz + 2 * kHs), rt, kC0 * pow(rt, kGamma));
+                  rows[r] = row_consts_p(MW_AT(a.hyc, row0 + r + kHs, a.nz + 2 * kHs), rt, kC0 * pow(rt, kGamma));
                 }
                 __syncthreads();
               });
@@ -324,7 +372,7 @@ __global__ void __launch_bounds__(kXT, MW_IEEE_X_MIN_BLOCKS) k_stage_x_ieee_w(Ar
 
 // ---- z ---------------------------------------------------------------------
 struct SmemZ {
-  RowD row[kZTileMax + 1];
+  RowP row[kZTileMax + 1];
 };
 
 // Columns [cb*NC, cb*NC+NC), rows [z0, z1), z1 - z0 <= kZTileMax; every
@@ -334,7 +382,7 @@ template <int NC>
 __device__ __forceinline__ void z_tile(const Args& a, int cb, int z0, int z1, bool hbot, bool htop, SmemZ& sm) {
   for (int rr = threadIdx.x; rr <= z1 - z0; rr += NC) {
     const int k = z0 + rr;
-    sm.row[rr] = row_consts(MW_AT(a.hyi, k, a.nz + 1), MW_AT(a.hyti, k, a.nz + 1), MW_AT(a.hypi, k, a.nz + 1));
+    sm.row[rr] = row_consts_p(MW_AT(a.hyi, k, a.nz + 1), MW_AT(a.hyti, k, a.nz + 1), MW_AT(a.hypi, k, a.nz + 1));
   }
   __syncthreads();
   const int c = cb * NC + threadIdx.x;  // interior column
