@@ -10,8 +10,8 @@
 // integer work (conversions, index arithmetic, table look-ups) is nearly free.
 // Against the reference's formulas (one pow, three divides and ~50 operations
 // per interface, interpolate.py:82-186) each interface costs ~37 + n FP64
-// operations and each cell update 8 (ncu: 47.8 per cell-stage in x on the
-// collision case):
+// operations and each cell update 8 (ncu: 47.6 per cell-stage in x, 49.3 in
+// z on the collision case):
 //   - quantities are carried scaled by 12, so the 4-point interpolation is
 //     A = 7 (s1 + s2) - (s0 + s3) and needs no division; the third
 //     difference is D = (s3 - s0) + 3 (s1 - s2): 6 operations per variable;
@@ -97,6 +97,7 @@ struct RowP {
   RowD d;
   double b[kMaxDeg + 1];  // b[0] unused
   int eI;                 // biased exponent of IRT12; 4096 where the b[n] would leave the normal range
+  unsigned mI;            // an upper bound of 2^16 x IRT12's significand (in [1, 2)): top 16 fraction bits + 1
 };
 __device__ __forceinline__ RowP row_consts_p(double r, double rt, double P) {
   RowP o;
@@ -110,17 +111,24 @@ __device__ __forceinline__ RowP row_consts_p(double r, double rt, double P) {
   }
   const double lo = fabs(o.b[kMaxDeg]), hi = fabs(o.b[1]);
   const bool normal = lo >= 0x1p-1000 && hi <= 0x1p1000 && pw >= 0x1p-1000;
-  o.eI = normal ? (int)((unsigned long long)__double_as_longlong(o.d.IRT12) >> 52 & 0x7ffu) : 4096;
+  const unsigned long long bI = (unsigned long long)__double_as_longlong(o.d.IRT12);
+  o.eI = normal ? (int)(bI >> 52 & 0x7ffu) : 4096;
+  o.mI = (unsigned)(bI >> 36 & 0xffffu) + 0x10001u;
   return o;
 }
 
 // The same as pressure(AT, r.d, add, mask), evaluated in AT: the degree comes
-// from a bound on the exponent of d = AT IRT12 (the sum of the exponents of AT
-// and IRT12, plus one), never below the degree d itself needs; warps where the
-// bound reaches 1/8 (and Inf, NaN, rows with eI = 4096) take the series in d.
+// from an upper bound on the exponent of d = AT IRT12 (the sum of the exponents
+// of AT and IRT12, plus one where the product of upper bounds of their leading
+// 17 significand bits reaches 2), found by integer operations and never below
+// the degree d itself needs; warps where the bound reaches 1/8 (and Inf, NaN,
+// rows with eI = 4096) take the series in d.
 __device__ __forceinline__ double pressure(double AT, const RowP& r, double add, unsigned mask) {
-  const int exA = (int)((unsigned long long)__double_as_longlong(AT) >> 52 & 0x7ffu);
-  const int eu = exA == 0 ? 0 : exA + r.eI - 1022;  // biased exponent of d is at most eu
+  const unsigned long long bA = (unsigned long long)__double_as_longlong(AT);
+  const int exA = (int)(bA >> 52 & 0x7ffu);
+  const unsigned mA = (unsigned)(bA >> 36 & 0xffffu) + 0x10001u;
+  const int carry = (unsigned long long)mA * r.mI >= (1ull << 33) ? 1 : 0;
+  const int eu = exA == 0 ? 0 : exA + r.eI - 1023 + carry;  // biased exponent of d is at most eu
   if (__any_sync(mask, eu >= 1020)) return pressure(AT, r.d, add, mask);
   const int exm = (int)__reduce_max_sync(mask, (unsigned)max(eu, 0));
   const int n = c_pow_g.deg[min(1022 - exm, 64)];
