@@ -385,7 +385,25 @@ def e2e_run(torch, p, f, steps, warmup, dist=None):
     e1.synchronize()
     ms = e0.elapsed_time(e1)
     nbytes = f.state.numel() * f.state.element_size()
-    return ms, nbytes
+    return ms, nbytes, host_link(torch, f.state, h_in, h_out)
+
+
+def host_link(torch, dev, h_in, h_out, reps=3):
+    """Pinned host <-> device copy rates of one state array (GB/s, best of
+    `reps`, each direction alone): the floor under the host-buffer step, which
+    differs between boxes."""
+    out = {}
+    for name, dst, src in (("h2d", dev, h_in), ("d2h", h_out, dev)):
+        best = 0.0
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dst.copy_(src, non_blocking=True)
+            e1.record()
+            e1.synchronize()
+            best = max(best, src.numel() * src.element_size() / (e0.elapsed_time(e1) * 1e-3) / 1e9)
+        out[name] = round(best, 1)
+    return out
 
 
 def form_leg(torch, native, args, mode, dtype, peak, peak_kind, table, sm_mhz, steps, warmup):
@@ -664,13 +682,15 @@ def run_gb300(args):
         init(f, p)
         clocks_e = ClockSampler(device_id_for_smi(torch, dev))
         clocks_e.start()
-        ms_e, nbytes = e2e_run(torch, p, f, args.steps, 1, dist)
+        ms_e, nbytes, link = e2e_run(torch, p, f, args.steps, args.warmup, dist)
         clk_e = clocks_e.stop()
         ms_e = replica_max(torch, ms_e, dist, "cuda")
         e2e_line = {"value": job_value(world, cells, args.steps, ms_e), "unit": UNIT,
                     "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                     "ms_per_step": ms_e / args.steps, "api": "pyminiweather_gb300.solve.evolve_host",
-                    "f64_mode": args.mode, "clocks": clk_e}
+                    "f64_mode": args.mode, "clocks": clk_e, "host_link_gbs": link,
+                    "copies_back_to_back_ms": round(nbytes / (link["h2d"] * 1e6) + nbytes / (link["d2h"] * 1e6), 3)
+                    if link["h2d"] and link["d2h"] else None}
     # per-kernel durations: the step's six launches issued one by one through
     # the C ABI (same kernels, same arrays, same storage formats), an event after each
     init(f, p)

@@ -238,7 +238,7 @@ def test_fp32_form_error_and_mass():
 
 
 @pytest.mark.parametrize("nx,nz,ic", [(256, 40, "collision"), (260, 9, "gravity"), (132, 7, "thermal"),
-                                      (1024, 130, "collision")])
+                                      (252, 5, "collision"), (508, 6, "thermal"), (1024, 130, "collision")])
 def test_fp32_tensor_copy_kernels_match_plain_loads(nx, nz, ic):
     """The FP32 stages whose tiles are staged by tensor copies (arrays 16-byte
     aligned, nx % 4 == 0, nx >= 128) against the plain-load kernels, which the
