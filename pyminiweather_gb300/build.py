@@ -4,8 +4,8 @@
 
 With --check (or MW_LIBRARY_VARIANT=check in the environment of the process
 that loads the package) the bounds-checked debug library
-libminiweather_gb300_check.so is built (MW_CHECK=1: the split-form kernels
-count out-of-range indices instead of accessing memory there) and loaded.
+libminiweather_gb300_check.so is built (MW_CHECK=1: every kernel counts
+out-of-range indices instead of accessing memory there) and loaded.
 
 Each translation unit is compiled by nvcc in parallel and linked into
 pyminiweather_gb300/_lib/libminiweather_gb300.so (static CUDA runtime).  The
