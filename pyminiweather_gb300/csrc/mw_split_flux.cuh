@@ -55,9 +55,26 @@ struct RowS {
 // expm1(e log1p(d)) in FP64.  Each coefficient exceeds the Horner term added
 // to it (|C(e, n+1) d| < |C(e, n)| for these |d|), so the additions use
 // FastTwoSum.
+//
+// Where the largest |d| of the warp's active lanes is small, fewer terms are
+// evaluated (a warp-uniform choice, so no lane diverges): below 2^-49 the
+// first-order term C(e, 1) d alone (the next is under 2^-48 of it), below
+// 2^-24 degree 2, below 2^-16 degree 3, all in double-FP32.
 __device__ __forceinline__ dw pow_m1(const PowTab& T, double e, dw d) {
   const float ad = fabsf(d.h);
   const float df = d.h;
+  {
+    const unsigned am = __activemask();
+    // |d| as unsigned bits orders like the value (NaN above every finite |d|)
+    const float mx = __uint_as_float(__reduce_max_sync(am, __float_as_uint(ad)));
+    if (mx < 0x1p-16f) {
+      const dw c1{T.h[1], T.l[1]};
+      if (mx < 0x1p-49f) return mul(c1, d);
+      if (mx < 0x1p-24f) return mul(add_big(c1, mulf(d, T.f[2])), d);
+      const dw y = add_big(dw{T.h[2], T.l[2]}, mulf(d, T.f[3]));
+      return mul(add_big(c1, mul(y, d)), d);
+    }
+  }
   // degree 8, computed for every cell so that it schedules with the
   // surrounding flux work; the rare larger |d| redo it below
   float t = fmaf(T.f[8], df, T.f[7]);
