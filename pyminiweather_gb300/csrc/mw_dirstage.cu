@@ -6,15 +6,20 @@
 // update.  Halo cells are never read: the periodic (x) and wall (z) rules of
 // ics/bcs.py are applied to the indices / values as they are loaded.
 //
-// x pass: a CTA walks a run of 255-cell chunks of one row.  Thread t
-// evaluates the flux at interface x0+t into shared memory; after one barrier
-// thread t updates cell x0+t from interfaces t and t+1.  Interface loads are
-// coalesced rows; the four taps hit L1.  Row constants are formed once per
-// CTA and row.
-// z pass: one thread per column marching down a tile of kZTile rows with a
-// rolling 4-row register window, so every forcing value is loaded once per
-// tile and every interface flux is evaluated once; rows are coalesced across
-// the warp.
+// Native FP64 and FP32 forms (the IEEE-FP64 form with the fewest operations
+// is in mw_fp64_stage.cu, the split form in mw_split_stage.cu); this file
+// also holds the stage and step entry points of every form.
+// x pass (plain loads): a CTA walks a run of 255-cell chunks of one row.
+// Thread t evaluates the flux at interface x0+t into shared memory; after one
+// barrier thread t updates cell x0+t from interfaces t and t+1.  Interface
+// loads are coalesced rows; the four taps hit L1.  Row constants are formed
+// once per CTA and row.
+// z pass (plain loads): one thread per column marching down a tile of kZTile
+// rows with a rolling 4-row register window, so every forcing value is loaded
+// once per tile and every interface flux is evaluated once; rows are
+// coalesced across the warp.
+// FP32 on 16-byte-aligned rows (nx % 4 == 0, nx >= 128): both passes are fed
+// by tensor copies instead (k_stage_x_f32_bulk, k_stage_z_f32_bulk below).
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -903,7 +908,7 @@ int ens_f32_occupancy(int direction, int* blocks_per_sm) {
 // ---------------------------------------------------------------------------
 // host side
 #ifndef MW_F32_BULK
-#define MW_F32_BULK 1  // FP32 z pass: rows staged by bulk copies where the layout allows (0: plain loads)
+#define MW_F32_BULK 1  // FP32 passes: tiles staged by tensor copies where the layout allows (0: plain loads)
 #endif
 
 // cuTensorMapEncodeTiled, from the driver through the runtime (no link-time
