@@ -7,8 +7,10 @@
 // so that no multiply-add is contracted and results round exactly as NumPy's
 // do, pow and cos aside.
 #include <algorithm>
+#include <cmath>
 
 #include "mw_common.cuh"
+#include "mw_fp64_math.cuh"
 #include "mw_split.cuh"
 
 namespace mw {
@@ -188,30 +190,54 @@ __device__ __forceinline__ void block_sum2(double& a, double& b, double* wa, dou
 __device__ __forceinline__ double load_state(const double* p) { return *p; }
 __device__ __forceinline__ double load_state(const float* p) { return split::f2d(*p); }
 
+// Per cell the reference forms p = C0 (rho th)^gamma and t = th / (p0 / p)^(Rd/Cp),
+// two powers; since gamma Rd / Cp = Rd / Cv = gamma - 1, the internal energy
+// rho Cv t is Cv K (rho theta)^gamma with K = (C0 / p0)^(Rd/Cp), and with
+// rho theta = (rho theta)_bg (1 + d) it is Pr (1 + ((1 + d)^gamma - 1)),
+// Pr = Cv K (rho theta)_bg^gamma formed once per row (ck = Cv K from the
+// host), the bracket by the binomial series of the stage kernels (degree per
+// warp, expm1 / log1p for |d| >= 1/8).  ke = ((rho u)^2 + (rho w)^2) / rho
+// with one reciprocal.  The same quantities as the reference's up to a few
+// roundings per cell (the sums agree to ~1e-16 relative).
+__constant__ ieee::Series c_stats_pow_g = ieee::make_series(kGamma);
+
 template <typename T>
-__global__ void __launch_bounds__(kStatThreads) k_stats_partial(int nx, int nz, int rpb, double dx, double dz,
-                                                                const double* hyc, const double* hytc, const T* state,
-                                                                double* part) {
+__global__ void __launch_bounds__(kStatThreads) k_stats_partial(int nx, int nz, int rpb, double ck, const double* hyc,
+                                                                const double* hytc, const T* state, double* part) {
   __shared__ double sm[kStatThreads / 32], se[kStatThreads / 32];
   const int NX = nx + 2 * kHs;
   const long long plane = (long long)NX * (nz + 2 * kHs);
+  const int lane = threadIdx.x & 31;
   double m = 0.0, e = 0.0;
   const int k0 = blockIdx.x * rpb, k1 = min(k0 + rpb, nz);
   for (int k = k0; k < k1; ++k) {
     const int kk = k + kHs;
     const double hr = MW_AT(hyc, kk, nz + 2 * kHs), hrt = MW_AT(hytc, kk, nz + 2 * kHs);
-    for (int i = threadIdx.x; i < nx; i += kStatThreads) {
-      const long long o = (long long)kk * NX + i + kHs;
-      const double rho = add_(load_state(&MW_AT(state, o, 4 * plane)), hr);
-      const double u = div_(load_state(&MW_AT(state, plane + o, 4 * plane)), rho);
-      const double w = div_(load_state(&MW_AT(state, 2 * plane + o, 4 * plane)), rho);
-      const double th = div_(add_(load_state(&MW_AT(state, 3 * plane + o, 4 * plane)), hrt), rho);
-      const double p = mul_(kC0, pow(mul_(rho, th), kGamma));
-      const double t = div_(th, pow(div_(kP0, p), kRd / kCp));
-      const double ke = mul_(rho, add_(mul_(u, u), mul_(w, w)));
-      const double ie = mul_(mul_(rho, kCv), t);
-      m = add_(m, rho);
-      e = add_(e, add_(ke, ie));
+    double pr = 0.0;
+    if (lane == 0) pr = ck * pow(hrt, kGamma);  // one power per warp and row
+    pr = __shfl_sync(0xffffffffu, pr, 0);
+    const double irt = 1.0 / hrt;
+    for (int base = 0; base < nx; base += kStatThreads) {
+      const int i = base + threadIdx.x;
+      const bool act = i < nx;
+      const unsigned mask = __ballot_sync(0xffffffffu, act);  // the lanes of this row step
+      if (act) {
+        const long long o = (long long)kk * NX + i + kHs;
+        const double rho = load_state(&MW_AT(state, o, 4 * plane)) + hr;
+        const double ri = ieee::rcp(rho, mask);
+        const double ru = load_state(&MW_AT(state, plane + o, 4 * plane));
+        const double rw = load_state(&MW_AT(state, 2 * plane + o, 4 * plane));
+        const double ke = fma(ru, ru, rw * rw) * ri;
+        const double d = load_state(&MW_AT(state, 3 * plane + o, 4 * plane)) * irt;
+        bool big;
+        const int n = ieee::series_degree(d, mask, c_stats_pow_g, big);
+        double f = d * ieee::series_g(d, n, c_stats_pow_g);  // (1 + d)^gamma - 1
+        if (__any_sync(mask, big)) {
+          if (big) f = expm1(kGamma * log1p(d));
+        }
+        m += rho;
+        e += ke + fma(pr, f, pr);
+      }
     }
   }
   block_sum2<kStatThreads>(m, e, sm, se);
@@ -254,7 +280,8 @@ int run_stats(int nx, int nz, double dx, double dz, const double* hyc, const dou
              workspace_bytes);
   int rpb;
   const int nb = stats_blocks(nz, &rpb);
-  k_stats_partial<T><<<nb, kStatThreads, 0, stream>>>(nx, nz, rpb, dx, dz, hyc, hytc, state, (double*)workspace);
+  const double ck = kCv * std::pow(kC0 / kP0, kRd / kCp);  // Cv (C0 / p0)^(Rd/Cp)
+  k_stats_partial<T><<<nb, kStatThreads, 0, stream>>>(nx, nz, rpb, ck, hyc, hytc, state, (double*)workspace);
   st = check_launch("stats partial launch");
   if (st) return st;
   k_stats_final<<<1, kStatMaxBlocks, 0, stream>>>(nb, dx, dz, (const double*)workspace, out2);
