@@ -474,3 +474,18 @@ def test_nonfinite_detection(dtype):
         with pytest.raises(_native.MiniWeatherError) as ei:
             evolve_host(dict(q, check_finite=True), g, h, h, dt=q["dt"], nbands=3)
         assert ei.value.status == 7
+
+
+def test_fp64_throughput_probe_is_plausible():
+    """mw_fp64_throughput (the measured FP64 peak the bench divides by): a
+    positive rate no higher than the nominal 2 operations per clock per SM at
+    the GPU's highest SM clock, and argument checks."""
+    import ctypes
+    props = torch.cuda.get_device_properties(0)
+    out = ctypes.c_double(0.0)
+    _native.call("mw_fp64_throughput", 2, 200, ctypes.byref(out), _native.stream_handle())
+    nominal = 2.0 * props.multi_processor_count * 2.2e9  # above any GB300 SM clock
+    assert 50e9 < out.value <= nominal, out.value
+    for bad in ((0, 200), (2, 0), (9, 200)):  # blocks_per_sm / iters out of range
+        with pytest.raises(_native.MiniWeatherError):
+            _native.call("mw_fp64_throughput", bad[0], bad[1], ctypes.byref(out), _native.stream_handle())
