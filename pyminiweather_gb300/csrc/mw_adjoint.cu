@@ -24,6 +24,8 @@
 // operations (MW_F64_IEEE: values scaled by 12, 1/rho by a Newton step,
 // dp/d(rho theta) = gamma P_row (1 + delta)^(gamma-1) / (rho theta)_bg by its
 // binomial series, per-row constants from a table in the workspace).
+#include <algorithm>
+
 #include "mw_common.cuh"
 #include "mw_fp64_math.cuh"
 
@@ -143,58 +145,94 @@ __global__ void k_vjp_iface(VjpArgs a) {
 }
 
 // Cell gather: gdst = base_a + base_b + add_gout * gout + sbar (interior); halo cells of gdst = 0.
+// The adjoint of interior cell (k, i) gathered from the interface adjoints
+// of its taps by the general rule: periodic wrap in x, the wall rule's halo
+// taps in z (any cell).
 template <int DIR>
-__global__ void k_vjp_gather(VjpArgs a) {
-  const long long ncell = (long long)a.plane;
+__device__ __forceinline__ void gather_general(const VjpArgs& a, int k, int i, double acc[4]) {
   const long long n = a.nif;
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < ncell;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const int kk = (int)(idx / a.pitch), ii = (int)(idx % a.pitch);
-    const int k = kk - kHs, i = ii - kHs;
+  if (DIR == MW_DIR_X) {
+    for (int j = 0; j < 4; ++j)
+      for (int m = -1; m <= 1; ++m) {
+        const int f = i + 2 - j + m * a.nx;  // interface whose tap j is cell i
+        if (f < 0 || f > a.nx) continue;
+        const long long o = (long long)k * (a.nx + 1) + f;
+        for (int q = 0; q < 4; ++q) acc[q] += kC[j] * MW_WS(a, q * n + o) + kE[j] * MW_WS(a, (4 + q) * n + o);
+      }
+  } else {
+    // taps t = f - 2 + j of interface f in [0, nz]; t maps to row k directly,
+    // or through the wall rule from halo rows -2,-1 (-> 0) and nz, nz+1 (-> nz-1)
+    for (int f = k - 1; f <= k + 2; ++f) {  // interfaces with an interior tap at row k
+      if (f < 0 || f > a.nz) continue;
+      const int j = k - f + 2;
+      const long long o = (long long)f * a.nx + i;
+      for (int q = 0; q < 4; ++q) acc[q] += kC[j] * MW_WS(a, q * n + o) + kE[j] * MW_WS(a, (4 + q) * n + o);
+    }
+    auto halo_taps = [&](int t, double wq[4]) {  // weight of halo row t on row k
+      const int src = t < 0 ? 0 : a.nz - 1;
+      wq[DENS] = wq[RHOT] = (k == src) ? 1.0 : 0.0;
+      wq[WMOM] = 0.0;
+      wq[UMOM] = (k == src) ? MW_VC(a, hyc, t + kHs) / MW_VC(a, hyc, src + kHs) : 0.0;
+    };
+    const int halo_rows[4] = {-2, -1, a.nz, a.nz + 1};
+    for (int h = 0; h < 4; ++h) {
+      const int t = halo_rows[h];
+      double wq[4];
+      halo_taps(t, wq);
+      if (wq[DENS] == 0.0 && wq[UMOM] == 0.0) continue;
+      for (int j = 0; j < 4; ++j) {
+        const int f = t + 2 - j;
+        if (f < 0 || f > a.nz) continue;
+        const long long o = (long long)f * a.nx + i;
+        for (int q = 0; q < 4; ++q)
+          acc[q] += wq[q] * (kC[j] * MW_WS(a, q * n + o) + kE[j] * MW_WS(a, (4 + q) * n + o));
+      }
+    }
+  }
+}
+
+// One thread per cell of a row (grid.y strides over the rows): halo cells get
+// zero; an interior cell whose four interfaces are all interior and none of
+// whose taps wrap or come through the wall rule (x: 2 <= i <= nx - 3, z:
+// 1 <= k <= nz - 2) reads them as a row (x) or column (z) of four, A0 .. A3
+// and D0 .. D3 at interfaces i - 1 .. i + 2, and sums the transposed taps in
+// the symmetric forms (7 (A1 + A2) - (A0 + A3)) / 12 and (D0 - D3) + 3 (D2 - D1);
+// the others take the general rule.  In z the gravity term follows.
+template <int DIR>
+__global__ void __launch_bounds__(128) k_vjp_gather(VjpArgs a) {
+  const long long n = a.nif;
+  const int ii = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ii >= a.pitch) return;
+  const int i = ii - kHs;
+  for (int kk = blockIdx.y; kk < a.nz + 2 * kHs; kk += gridDim.y) {
+    const long long idx = (long long)kk * a.pitch + ii;
+    const int k = kk - kHs;
     if (k < 0 || k >= a.nz || i < 0 || i >= a.nx) {
       for (int q = 0; q < 4; ++q) MW_AT(a.gdst, q * a.plane + idx, 4 * a.plane) = 0.0;
       continue;
     }
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
-    if (DIR == MW_DIR_X) {
-      for (int j = 0; j < 4; ++j)
-        for (int m = -1; m <= 1; ++m) {
-          const int f = i + 2 - j + m * a.nx;  // interface whose tap j is cell i
-          if (f < 0 || f > a.nx) continue;
-          const long long o = (long long)k * (a.nx + 1) + f;
-          for (int q = 0; q < 4; ++q) acc[q] += kC[j] * MW_WS(a, q * n + o) + kE[j] * MW_WS(a, (4 + q) * n + o);
-        }
+    const bool fast = DIR == MW_DIR_X ? (i >= 2 && i + 3 <= a.nx) : (k >= 1 && k + 2 <= a.nz);
+    if (fast) {
+      // interfaces i - 1 .. i + 2 (x: row k of nx + 1; z: rows k - 1 .. k + 2 of column i)
+      const long long o0 = DIR == MW_DIR_X ? (long long)k * (a.nx + 1) + (i - 1) : (long long)(k - 1) * a.nx + i;
+      const long long st = DIR == MW_DIR_X ? 1 : a.nx;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const double A0 = MW_WS(a, q * n + o0), A1 = MW_WS(a, q * n + o0 + st);
+        const double A2 = MW_WS(a, q * n + o0 + 2 * st), A3 = MW_WS(a, q * n + o0 + 3 * st);
+        const double D0 = MW_WS(a, (4 + q) * n + o0), D1 = MW_WS(a, (4 + q) * n + o0 + st);
+        const double D2 = MW_WS(a, (4 + q) * n + o0 + 2 * st), D3 = MW_WS(a, (4 + q) * n + o0 + 3 * st);
+        // cell i is tap j of interface f = i + 2 - j, so kC = (-1, 7, 7, -1) / 12 and
+        // kE = (-1, 3, -3, 1) act on the interfaces i + 2, i + 1, i, i - 1 = (A3, A2, A1, A0)
+        const double ca = fma(7.0, A1 + A2, -(A0 + A3)) * (1.0 / 12.0);
+        const double ce = fma(3.0, D2 - D1, D0 - D3);
+        acc[q] = ca + ce;
+      }
     } else {
-      // taps t = f - 2 + j of interface f in [0, nz]; t maps to row k directly,
-      // or through the wall rule from halo rows -2,-1 (-> 0) and nz, nz+1 (-> nz-1)
-      for (int f = k - 1; f <= k + 2; ++f) {  // interfaces with an interior tap at row k
-        if (f < 0 || f > a.nz) continue;
-        const int j = k - f + 2;
-        const long long o = (long long)f * a.nx + i;
-        for (int q = 0; q < 4; ++q) acc[q] += kC[j] * MW_WS(a, q * n + o) + kE[j] * MW_WS(a, (4 + q) * n + o);
-      }
-      auto halo_taps = [&](int t, double wq[4]) {  // weight of halo row t on row k
-        const int src = t < 0 ? 0 : a.nz - 1;
-        wq[DENS] = wq[RHOT] = (k == src) ? 1.0 : 0.0;
-        wq[WMOM] = 0.0;
-        wq[UMOM] = (k == src) ? MW_VC(a, hyc, t + kHs) / MW_VC(a, hyc, src + kHs) : 0.0;
-      };
-      const int halo_rows[4] = {-2, -1, a.nz, a.nz + 1};
-      for (int h = 0; h < 4; ++h) {
-        const int t = halo_rows[h];
-        double wq[4];
-        halo_taps(t, wq);
-        if (wq[DENS] == 0.0 && wq[UMOM] == 0.0) continue;
-        for (int j = 0; j < 4; ++j) {
-          const int f = t + 2 - j;
-          if (f < 0 || f > a.nz) continue;
-          const long long o = (long long)f * a.nx + i;
-          for (int q = 0; q < 4; ++q)
-            acc[q] += wq[q] * (kC[j] * MW_WS(a, q * n + o) + kE[j] * MW_WS(a, (4 + q) * n + o));
-        }
-      }
-      acc[DENS] -= a.dt_stage * kGrav * gval(a, WMOM, k, i);
+      gather_general<DIR>(a, k, i, acc);
     }
+    if (DIR == MW_DIR_Z) acc[DENS] -= a.dt_stage * kGrav * gval(a, WMOM, k, i);
     for (int q = 0; q < 4; ++q) {
       const long long o = q * a.plane + idx;
       double v = acc[q];
@@ -328,6 +366,11 @@ __global__ void k_vjp_iface_ieee(VjpArgs a, const RowV* rows) {
   }
 }
 
+// k_vjp_gather: 128 columns per CTA, the rows strided over grid.y.
+inline dim3 gather_grid(const Geom& g) {
+  return dim3((unsigned)((g.pitch + 127) / 128), (unsigned)std::min<long long>(g.plane / g.pitch, 65535));
+}
+
 inline unsigned grid_for(long long n, int threads) {
   long long b = (n + threads - 1) / threads;
   if (b < 1) b = 1;
@@ -436,14 +479,14 @@ static int vjp_stage(int nx, int nz, double dx, double dz, double dt_full, const
     else
       k_vjp_iface<MW_DIR_X><<<grid_for(a.nif, 128), 128, 0, s>>>(a);
     if ((st = check_launch("vjp interface launch"))) return st;
-    k_vjp_gather<MW_DIR_X><<<grid_for(g.plane, 256), 256, 0, s>>>(a);
+    k_vjp_gather<MW_DIR_X><<<gather_grid(g), 128, 0, s>>>(a);
   } else {
     if (f64_mode == MW_F64_IEEE)
       k_vjp_iface_ieee<MW_DIR_Z><<<grid_for(a.nif, 128), 128, 0, s>>>(a, rows);
     else
       k_vjp_iface<MW_DIR_Z><<<grid_for(a.nif, 128), 128, 0, s>>>(a);
     if ((st = check_launch("vjp interface launch"))) return st;
-    k_vjp_gather<MW_DIR_Z><<<grid_for(g.plane, 256), 256, 0, s>>>(a);
+    k_vjp_gather<MW_DIR_Z><<<gather_grid(g), 128, 0, s>>>(a);
   }
   return check_launch("vjp gather launch");
 }
