@@ -207,7 +207,10 @@ typedef struct mw_ens_plan_info {
  * work items of z_tile rows (1..64). */
 int mw_ensemble_plan_info(int n_members, const mw_ens_member* members, int z_tile, mw_ens_plan_info* info);
 /* Write the plan into plan_device (info.bytes bytes, 16-byte aligned); the
- * copy to the device is synchronous. */
+ * copy to the device is synchronous.  The plan's work lists are sorted by
+ * decreasing cost and handed out by a cursor kept in the plan (the persistent
+ * warps and CTAs take the next item as they become free), so a plan serves one
+ * step call at a time: calls that use one plan must be ordered (one stream). */
 int mw_ensemble_plan(int n_members, const mw_ens_member* members, int z_tile, void* plan_device, size_t plan_bytes,
                      mw_ens_plan_info* info, void* stream);
 /* nsteps time steps of every member: 6 persistent launches per step, grid_x

@@ -868,17 +868,20 @@ __device__ __forceinline__ void x_row_warp_f32(const StageArgs<float>& a, int k,
 }
 
 __global__ void __launch_bounds__(kXThreads) k_ens_x_f32(EnsStageT<float> es) {
-  const int nw = gridDim.x * (kXThreads / 32);
-  for (int it = blockIdx.x * (kXThreads / 32) + (threadIdx.x >> 5); it < es.n_items; it += nw) {
+  for (unsigned it = ens_take_warp(es.cursor); it < (unsigned)es.n_items; it = ens_take_warp(es.cursor)) {
     const int2 item = MW_AT(es.items, it, es.n_items);  // (member, row)
     const StageArgs<float> a = member_args_f32(es, item.x);
     x_row_warp_f32(a, item.y, a.flags & MW_FLAG_WRITE_HALO);
   }
+  ens_finish(es.cursor);
 }
 
 __global__ void __launch_bounds__(kEnsZCols) k_ens_z_f32(EnsStageT<float> es) {
   __shared__ SmemZT sm;
-  for (int it = blockIdx.x; it < es.n_items; it += gridDim.x) {
+  __shared__ unsigned slot[2];
+  int parity = 0;
+  for (unsigned it = ens_take_cta(es.cursor, slot, parity); it < (unsigned)es.n_items;
+       it = ens_take_cta(es.cursor, slot, parity)) {
     const int2 item = MW_AT(es.items, it, es.n_items);
     const StageArgs<float> a = member_args_f32(es, item.x);
     const int ncb = (a.nx + kEnsZCols - 1) / kEnsZCols;
@@ -886,6 +889,7 @@ __global__ void __launch_bounds__(kEnsZCols) k_ens_z_f32(EnsStageT<float> es) {
     z_tile_t<float, MODE_F32, kEnsZCols>(a, cb, tile * es.z_tile, es.z_tile,
                                          (a.flags & MW_FLAG_WRITE_HALO) && tile == 0, sm);
   }
+  ens_finish(es.cursor);
 }
 
 int launch_ens_f32(const EnsStageT<float>& es, int grid) {

@@ -5,11 +5,14 @@
 // The plan lives in caller-provided device memory:
 //   [members: n x mw_ens_member][x items: int2 (member, row)]
 //   [z items: int2 (member, column block + ncb * z tile)]
-//   [row constants: n_xrows x 32 B, written by each split-form step call]
+//   [row constants: n_xrows x 40 B, written by each FP64 step call]
 //   [stage constants: n x 6 x EnsMemberConsts, written with the plan]
+//   [work cursor: EnsCursor, zero between launches]
 // x work items are member rows (one warp walks the segments of the row); z items
-// are kEnsZCols-column x z_tile-row tiles.  A persistent CTA takes items
-// blockIdx.x, blockIdx.x + gridDim.x, ...
+// are kEnsZCols-column x z_tile-row tiles.  Each list is sorted by decreasing
+// cost (x: row length; z: tile rows, then used columns), members in order
+// within a cost, and the persistent warps (x) / CTAs (z) take items from the
+// cursor as they become free.
 #include <algorithm>
 #include <type_traits>
 #include <cstring>
@@ -72,7 +75,7 @@ int layout(int n, const mw_ens_member* m, int z_tile, mw_ens_plan_info* info) {
   info->z_items_off = align16(info->x_items_off + sizeof(int2) * (size_t)nxi);
   info->xrows_off = align16(info->z_items_off + sizeof(int2) * (size_t)nzi);
   info->n_xrows = nrows;
-  info->bytes = align16(ens_consts_off(*info) + sizeof(EnsMemberConsts) * kEnsConstsPerMember * (size_t)n);
+  info->bytes = ens_cursor_off(*info) + sizeof(EnsCursor);
   return MW_OK;
 }
 
@@ -116,6 +119,7 @@ int ens_step(void* plan, const mw_ens_plan_info* info, const double* hyc, const 
   }
   EnsStageT<T> es;
   es.members = (const mw_ens_member*)((const char*)plan + info->members_off);
+  es.cursor = (EnsCursor*)((char*)plan + ens_cursor_off(*info));
   es.z_tile = info->z_tile;
   es.flags = flags;
   es.hyc = hyc;
@@ -217,6 +221,16 @@ extern "C" int mw_ensemble_plan(int n_members, const mw_ens_member* members, int
     for (int t = 0; t < ntile; ++t)
       for (int cb = 0; cb < ncb; ++cb) zi[b++] = make_int2(e, cb + ncb * t);
   }
+  // decreasing cost, stable: an x row costs its length; a z tile its rows (a
+  // CTA marches them whatever its used columns), then its used columns
+  std::stable_sort(xi, xi + a, [&](int2 p, int2 q) { return members[p.x].nx > members[q.x].nx; });
+  auto tile_cost = [&](int2 it) {
+    const mw_ens_member& m = members[it.x];
+    const int ncb = (m.nx + kEnsZCols - 1) / kEnsZCols;
+    const int cb = it.y % ncb, z0 = (it.y / ncb) * z_tile;
+    return std::make_pair(std::min(z_tile, m.nz - z0), std::min(kEnsZCols, m.nx - cb * kEnsZCols));
+  };
+  std::stable_sort(zi, zi + b, [&](int2 p, int2 q) { return tile_cost(p) > tile_cost(q); });
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e = cudaMemcpyAsync(plan_device, host.data(), info->bytes, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);

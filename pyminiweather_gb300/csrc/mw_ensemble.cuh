@@ -23,11 +23,22 @@ struct EnsMemberConsts {
 };
 static_assert(sizeof(EnsMemberConsts) == 88, "EnsMemberConsts layout");
 
+// Work cursor of the persistent launches, in the plan.  The work lists are
+// sorted by decreasing cost, and a warp (x) or CTA (z) that is free takes the
+// next item, so a launch ends on its cheapest items.  `next` hands out list
+// positions; `done` counts the CTAs that found the list empty, and the last of
+// them resets both for the next launch on the plan (the launches of a step
+// call are ordered by its stream).
+struct EnsCursor {
+  unsigned next, done, pad[2];
+};
+
 // Arguments of one ensemble direction-stage launch (T = state storage type).
 template <typename T>
 struct EnsStageT {
   const mw_ens_member* members;  // device
   const int2* items;             // device work list of this direction
+  EnsCursor* cursor;             // device, in the plan
   int n_items;
   int z_tile;      // rows per z item
   int direction;   // MW_DIR_X / MW_DIR_Z
@@ -73,6 +84,41 @@ constexpr int kEnsConstsPerMember = 6;
 inline size_t ens_consts_off(const mw_ens_plan_info& info) {
   return (info.xrows_off + kEnsRowBytes * (size_t)info.n_xrows + 15) & ~(size_t)15;
 }
+
+inline size_t ens_cursor_off(const mw_ens_plan_info& info) {
+  return (ens_consts_off(info) + sizeof(EnsMemberConsts) * kEnsConstsPerMember * (size_t)info.n_members + 15) &
+         ~(size_t)15;
+}
+
+#ifdef __CUDACC__
+// The next list position for the calling warp (all 32 lanes call it).
+__device__ __forceinline__ unsigned ens_take_warp(EnsCursor* c) {
+  unsigned v = 0;
+  if ((threadIdx.x & 31) == 0) v = atomicAdd(&c->next, 1u);
+  return __shfl_sync(0xffffffffu, v, 0);
+}
+// The next list position for the calling CTA (every thread calls it): thread
+// 0 takes it into one of two shared slots, alternated so that a slot is not
+// rewritten before every thread has read it.
+__device__ __forceinline__ unsigned ens_take_cta(EnsCursor* c, unsigned* slot, int& parity) {
+  if (threadIdx.x == 0) slot[parity] = atomicAdd(&c->next, 1u);
+  __syncthreads();
+  const unsigned v = slot[parity];
+  parity ^= 1;
+  return v;
+}
+// Every thread of the CTA, once it has stopped taking items.
+__device__ __forceinline__ void ens_finish(EnsCursor* c) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&c->done, 1u) == gridDim.x - 1) {  // every other CTA has stopped taking
+      atomicExch(&c->next, 0u);
+      atomicExch(&c->done, 0u);
+    }
+  }
+}
+#endif
 
 // Row-constant tables of the split / IEEE-FP64 ensemble x kernels: entry j from hyc[j], hytc[j].
 int launch_ens_split_rowtable(const double* hyc, const double* hytc, long long n, void* table, cudaStream_t stream);

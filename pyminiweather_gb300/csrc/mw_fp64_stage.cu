@@ -501,8 +501,7 @@ __global__ void k_ens_row_table_ieee(const double* hyc, const double* hytc, long
 __global__ void __launch_bounds__(kXT, MW_IEEE_X_MIN_BLOCKS) k_ens_x_ieee(EnsStage es) {
   __shared__ SmemXW sm;
   const int w = threadIdx.x >> 5;
-  const int nw = gridDim.x * kXWarps;
-  for (int it = blockIdx.x * kXWarps + w; it < es.n_items; it += nw) {
+  for (unsigned it = ens_take_warp(es.cursor); it < (unsigned)es.n_items; it = ens_take_warp(es.cursor)) {
     const int2 item = MW_AT(es.items, it, es.n_items);  // (member, row)
     const Args a = member_args(es, item.x);
     const int nseg = (a.nx + kWCells - 1) / kWCells;
@@ -512,11 +511,15 @@ __global__ void __launch_bounds__(kXT, MW_IEEE_X_MIN_BLOCKS) k_ens_x_ieee(EnsSta
                 [&](int) -> const RowD& { return r; },
                 a.flags & MW_FLAG_WRITE_HALO, sm.sS[w], []() {});
   }
+  ens_finish(es.cursor);
 }
 
 __global__ void __launch_bounds__(kEnsZCols) k_ens_z_ieee(EnsStage es) {
   __shared__ SmemZ sm;
-  for (int it = blockIdx.x; it < es.n_items; it += gridDim.x) {
+  __shared__ unsigned slot[2];
+  int parity = 0;
+  for (unsigned it = ens_take_cta(es.cursor, slot, parity); it < (unsigned)es.n_items;
+       it = ens_take_cta(es.cursor, slot, parity)) {
     const int2 item = MW_AT(es.items, it, es.n_items);  // (member, column block + ncb * tile)
     const Args a = member_args(es, item.x);
     const int ncb = (a.nx + kEnsZCols - 1) / kEnsZCols;
@@ -525,6 +528,7 @@ __global__ void __launch_bounds__(kEnsZCols) k_ens_z_ieee(EnsStage es) {
     const bool halo = a.flags & MW_FLAG_WRITE_HALO;
     z_tile<kEnsZCols>(a, cb, z0, z1, halo && z0 == 0, halo && z1 == a.nz, sm);
   }
+  ens_finish(es.cursor);
 }
 
 // CTAs of k_stage_x_ieee_w (which 0) / k_stage_z_ieee (which 1) resident on

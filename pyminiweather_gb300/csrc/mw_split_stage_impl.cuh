@@ -419,8 +419,7 @@ __device__ SplitArgs member_args(const EnsStage& es, int e) {
 template <int FMT>
 __global__ void __launch_bounds__(kXThreads, MW_XSPLIT_MIN_BLOCKS) k_ens_x_split(EnsStage es) {
   __shared__ SmemXW sm;
-  const int nw = gridDim.x * kXWarps;
-  for (int it = blockIdx.x * kXWarps + (threadIdx.x >> 5); it < es.n_items; it += nw) {
+  for (unsigned it = ens_take_warp(es.cursor); it < (unsigned)es.n_items; it = ens_take_warp(es.cursor)) {
     const int2 item = MW_AT(es.items, it, es.n_items);  // (member, row)
     const SplitArgs a = member_args(es, item.x);
     const int nseg = (a.nx + kWCells - 1) / kWCells;
@@ -429,6 +428,7 @@ __global__ void __launch_bounds__(kXThreads, MW_XSPLIT_MIN_BLOCKS) k_ens_x_split
     x_warp_segments<FMT>(a, nseg, (long long)item.y * nseg, (long long)(item.y + 1) * nseg,
                     [&](int) { return r; }, a.flags & MW_FLAG_WRITE_HALO, sm, []() {});
   }
+  ens_finish(es.cursor);
 }
 
 template <int FMT>
@@ -436,7 +436,10 @@ __global__ void __launch_bounds__(kEnsZCols,
                                   (kZThreads / kEnsZCols) * (FMT == kFromPair ? MW_ZSPLIT_MIN_BLOCKS - 1 : MW_ZSPLIT_MIN_BLOCKS))
     k_ens_z_split(EnsStage es) {
   __shared__ SmemZ sm;
-  for (int it = blockIdx.x; it < es.n_items; it += gridDim.x) {
+  __shared__ unsigned slot[2];
+  int parity = 0;
+  for (unsigned it = ens_take_cta(es.cursor, slot, parity); it < (unsigned)es.n_items;
+       it = ens_take_cta(es.cursor, slot, parity)) {
     const int2 item = MW_AT(es.items, it, es.n_items);  // (member, column block + ncb * tile)
     const SplitArgs a = member_args(es, item.x);
     const int ncb = (a.nx + kEnsZCols - 1) / kEnsZCols;
@@ -445,6 +448,7 @@ __global__ void __launch_bounds__(kEnsZCols,
     const bool halo = a.flags & MW_FLAG_WRITE_HALO;
     z_march<FMT, kEnsZCols>(a, cb, k0, kend, halo && k0 == 0, halo && kend == a.nz, sm);
   }
+  ens_finish(es.cursor);
 }
 
 }  // namespace
@@ -466,8 +470,8 @@ int launch_ens_split(const EnsStage& es, int grid) {
   if (es.n_items == 0) return MW_OK;
   MW_REQUIRE(es.fmt == kF64 || es.fmt == kToPair || es.fmt == kFromPair, MW_ERR_INVALID_ARG, "bad stage format");
   // The grid is sized for the FP64-storage z kernel; the pair-reading one fits
-  // fewer CTAs per SM, so its persistent grid shrinks in proportion (its items
-  // are strided statically over the CTAs, which must all be resident at once).
+  // fewer CTAs per SM, so its persistent grid shrinks in proportion (one wave of
+  // resident CTAs: a CTA beyond it would start only as the list runs out).
   if (es.direction == MW_DIR_Z && es.fmt == kFromPair) {
     const int b0 = ens_z_per_sm<kF64>(), b1 = ens_z_per_sm<kFromPair>();
     if (b1 < b0) grid = std::max(1, (int)((long long)grid * b1 / b0));

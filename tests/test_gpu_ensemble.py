@@ -81,6 +81,27 @@ def test_graph_replay_equals_eager_steps(mode):
     assert a.reverse == b.reverse == 0
 
 
+@pytest.mark.parametrize("dtype,mode", [(torch.float64, "fp64"), (torch.float64, "split"), (torch.float32, "fp64")])
+def test_results_do_not_depend_on_the_grid(dtype, mode):
+    """The persistent warps / CTAs take work items from the plan's cursor as
+    they become free: any grid (one CTA, a few, one wave, several waves) gives
+    the same bits, and the cursor starts every one of the 18 launches of three
+    steps from the head of its list."""
+    mem = small_members(seed=5)
+    ref = None
+    for grids in ((0, 0), (1, 1), (3, 5), (-4, -4)):
+        ens = Ensemble(mem, dtype=dtype, f64_mode=mode)
+        bx, bz = ens.default_grids()
+        ens.grid_x = grids[0] if grids[0] >= 0 else -grids[0] * bx
+        ens.grid_z = grids[1] if grids[1] >= 0 else -grids[1] * bz
+        ens.step(3)
+        torch.cuda.synchronize()
+        if ref is None:
+            ref = (ens.state.clone(), ens.state_tmp.clone())
+        else:
+            assert torch.equal(ens.state, ref[0]) and torch.equal(ens.state_tmp, ref[1]), grids
+
+
 def test_autotune_does_not_change_results():
     mem = small_members(seed=4)
     a, b = Ensemble(mem), Ensemble(mem)
