@@ -102,6 +102,47 @@ def test_results_do_not_depend_on_the_grid(dtype, mode):
             assert torch.equal(ens.state, ref[0]) and torch.equal(ens.state_tmp, ref[1]), grids
 
 
+def test_fp32_members_at_any_float_offset():
+    """Member blocks that start at any float offset (not 8- or 16-byte aligned,
+    as a C caller may lay them out) and rows of any length mod 4: the results
+    equal those of the packed layout bit for bit."""
+    import ctypes
+
+    from pyminiweather_gb300 import _native
+    mem = small_members(seed=6)
+    ref = Ensemble(mem, dtype=torch.float32)
+    n = ref.n_members()
+    specs = (_native.EnsMember * n)()
+    blocks, so = [], 0
+    for e in range(n):
+        s = ref.specs[e]
+        so += 1 + e % 3  # gaps of 1..3 floats between the blocks
+        size = 4 * (s.nx + 4) * (s.nz + 4)
+        specs[e] = _native.EnsMember(s.nx, s.nz, s.dx, s.dz, s.dt, so, s.cell_off, s.int_off)
+        blocks.append((so, size))
+        so += size
+    bufs = [torch.zeros(so + 8, dtype=torch.float32, device="cuda") for _ in range(3)]
+    for e, (o, size) in enumerate(blocks):
+        bufs[0][o:o + size] = ref.member_state(e).reshape(-1)
+        bufs[1][o:o + size] = ref.member_state_tmp(e).reshape(-1)
+    stream = _native.stream_handle()
+    info = _native.EnsPlanInfo()
+    _native.call("mw_ensemble_plan_info", n, specs, ref.z_tile, ctypes.byref(info))
+    plan = torch.empty((info.bytes + 15) // 16 * 2, dtype=torch.float64, device="cuda")
+    _native.call("mw_ensemble_plan", n, specs, ref.z_tile, _native.ptr(plan), plan.numel() * 8, ctypes.byref(info),
+                 stream)
+    rv = ctypes.c_int(0)
+    _native.call("mw_ensemble_step_f32", _native.ptr(plan), ctypes.byref(info),
+                 *[_native.ptr(a) for a in ref.backgrounds()], *[_native.ptr(b) for b in bufs], 3, ctypes.byref(rv),
+                 _native.MW_FLAG_WRITE_HALO, 0, 0, stream)
+    ref.step(3)
+    torch.cuda.synchronize()
+    assert rv.value == ref.reverse
+    for e, (o, size) in enumerate(blocks):
+        assert torch.equal(bufs[0][o:o + size], ref.member_state(e).reshape(-1)), e
+        assert torch.equal(bufs[1][o:o + size], ref.member_state_tmp(e).reshape(-1)), e
+
+
 def test_autotune_does_not_change_results():
     mem = small_members(seed=4)
     a, b = Ensemble(mem), Ensemble(mem)
