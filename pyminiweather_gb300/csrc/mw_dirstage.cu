@@ -339,6 +339,21 @@ __device__ __forceinline__ void x_rowrun_t(const StageArgs<T>& a, int k, int cbe
 // thread per column marching the rows with a rolling 4-row window, the next
 // row loaded one step ahead.  halo: write the wall halo rows of these columns
 // (cb == 0 also does the four x-halo columns).
+// The plain-load FP32 passes wait on memory (one row or segment of loads in
+// flight per thread, no registers to spare for more): prefetch instructions
+// bring later rows / segments into L2 without holding registers.  Measured on
+// the 256-member thermal ensemble (ms per step): none 1.474, z 2 rows ahead
+// 1.410 (1, 3, 4, 8: 1.40-1.44 with x), x 1 segment 1.453, both (x 2, z 2) 1.393.
+#ifndef MW_F32_PF_Z
+#define MW_F32_PF_Z 2  // FP32 z march: L2 prefetch of the rows this many steps ahead (0: none)
+#endif
+#ifndef MW_F32_PF_X
+#define MW_F32_PF_X 2  // FP32 ensemble x rows: L2 prefetch of the segment this many ahead (0: none)
+#endif
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 template <typename T, int MODE, int NC = kZThreads>
 __device__ __forceinline__ void z_tile_t(const StageArgs<T>& a, int cb, int z0, int zt, bool halo, SmemZT& sm) {
   const int z1 = min(z0 + zt, a.nz);
@@ -391,6 +406,14 @@ __device__ __forceinline__ void z_tile_t(const StageArgs<T>& a, int cb, int z0, 
       if (k + 1 < z1) {  // load the row needed by the next iteration now
 #pragma unroll
         for (int q = 0; q < 4; ++q) nxt[q] = zval(a, q, k + 3, col);
+      }
+      if constexpr (MODE == MODE_F32 && MW_F32_PF_Z > 0) {  // rows MW_F32_PF_Z steps ahead into L2
+        const int kf = k + 3 + MW_F32_PF_Z, ki = k + MW_F32_PF_Z;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          if (kf < a.nz) prefetch_l2(&MW_SF(a, q * a.plane + (long long)(kf + kHs) * a.pitch + col));
+          if (ki < z1) prefetch_l2(&MW_SI(a, q * a.plane + (long long)(ki + kHs) * a.pitch + col));
+        }
       }
       T Fn[4];
       flux_at(k + 1, Fn);
@@ -838,6 +861,12 @@ __device__ __forceinline__ void x_row_warp_f32(const StageArgs<float>& a, int k,
     for (int q = 0; q < 4; ++q) MW_SF(a, q * a.plane + row + dst) = MW_SF(a, q * a.plane + row + src);
   }
   for (int x0 = 0; x0 < a.nx; x0 += kF32WCells) {
+    if (MW_F32_PF_X && x0 + MW_F32_PF_X * kF32WCells < a.nx && lane < 16) {  // a later segment's lines into L2
+      const int q = lane & 3;
+      const float* base = (lane & 4) ? a.init : a.forcing;
+      const int col = min(x0 + MW_F32_PF_X * kF32WCells + (lane >> 3) * 32, a.nx + 2 * kHs - 1);
+      prefetch_l2(base + q * a.plane + row + col);
+    }
     const int i = x0 + lane;
     const bool upd = lane < kF32WCells && i < a.nx;
     const long long o = row + i + kHs;
