@@ -102,6 +102,41 @@ def test_results_do_not_depend_on_the_grid(dtype, mode):
             assert torch.equal(ens.state, ref[0]) and torch.equal(ens.state_tmp, ref[1]), grids
 
 
+@pytest.mark.parametrize("dtype,mode", [(torch.float64, "fp64"), (torch.float32, "fp64")])
+def test_plan_lists_sorted_and_cursor_reset(dtype, mode):
+    """The plan's work lists hold every item once, sorted by decreasing cost
+    (x: row length; z: tile rows, then used columns; member order within a
+    cost), and the work cursor at the plan's end is zero again after a step
+    call (the last CTA of every launch resets it)."""
+    mem = small_members(seed=7)
+    ens = Ensemble(mem, dtype=dtype, f64_mode=mode)
+    ens.step(2)
+    torch.cuda.synchronize()
+    raw = ens.plan.view(torch.uint8).cpu().numpy()
+    info = ens.info
+    xi = raw[info.x_items_off:info.x_items_off + 8 * info.n_x_items].view(np.int32).reshape(-1, 2)
+    zi = raw[info.z_items_off:info.z_items_off + 8 * info.n_z_items].view(np.int32).reshape(-1, 2)
+    nxs = [p["nx"] for p, _ in mem]
+    nzs = [p["nz"] for p, _ in mem]
+    assert sorted(map(tuple, xi)) == sorted((e, k) for e in range(len(mem)) for k in range(nzs[e]))
+    keys = [(-nxs[e], e, k) for e, k in xi]
+    assert keys == sorted(keys)
+    zt, cols = ens.z_tile, 64
+
+    def tile(e, y):
+        ncb = (nxs[e] + cols - 1) // cols
+        cb, t = y % ncb, y // ncb
+        return (-min(zt, nzs[e] - t * zt), -min(cols, nxs[e] - cb * cols))
+    expect = sorted(((e, cb + ((nxs[e] + cols - 1) // cols) * t)
+                     for e in range(len(mem)) for t in range((nzs[e] + zt - 1) // zt)
+                     for cb in range((nxs[e] + cols - 1) // cols)))
+    assert sorted(map(tuple, zi)) == expect
+    zkeys = [tile(e, y) for e, y in zi]
+    assert zkeys == sorted(zkeys)
+    cursor = raw[info.bytes - 16:info.bytes].view(np.uint32)
+    assert cursor[0] == 0 and cursor[1] == 0
+
+
 def test_fp32_members_at_any_float_offset():
     """Member blocks that start at any float offset (not 8- or 16-byte aligned,
     as a C caller may lay them out) and rows of any length mod 4: the results
