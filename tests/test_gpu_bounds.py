@@ -44,7 +44,8 @@ DRIVER = textwrap.dedent("""
     torch.cuda.synchronize()
     _native.call("mw_debug_oob_count", ctypes.byref(n), 1)
     assert n.value == 1, n.value  # the planted index was caught (and diverted)
-    for nx, nz, ic in [(2, 1, "collision"), (3, 2, "thermal"), (37, 13, "collision"), (31, 5, "gravity"),
+    for nx, nz, ic in [(2, 1, "collision"), (3, 2, "thermal"), (5, 3, "thermal"), (7, 1, "collision"),
+                       (4, 4, "thermal"), (66, 2, "thermal"), (37, 13, "collision"), (31, 5, "gravity"),
                        (62, 17, "density-current"), (130, 70, "collision"), (257, 129, "gravity"),
                        (96, 320, "thermal"),  # 16 host-step bands, the end ones half as tall
                        (256, 40, "collision"), (260, 9, "gravity"), (132, 7, "thermal")]:  # FP32 passes fed by
@@ -102,8 +103,12 @@ DRIVER = textwrap.dedent("""
                              _native.ptr(g), _native.ptr(g), None, 1, _native.ptr(out), p["dt"] / 3, d, mode,
                              _native.ptr(ws), ws.numel() * 8, S)
         print(nx, nz, ic, "OOB so far", count(), flush=True)
+    from pyminiweather_gb300.ensemble import member_params
+    tiny = [(member_params(nx, nz), None) for nx, nz in ((2, 1), (3, 2), (5, 3), (7, 1), (4, 4), (66, 2))]
     for dtype, mode in ((torch.float64, "fp64"), (torch.float64, "split"), (torch.float32, "fp64")):
         ens = Ensemble(thermal_ensemble(5, seed=3), dtype=dtype, f64_mode=mode)
+        ens.step(3)
+        ens = Ensemble(tiny, dtype=dtype, f64_mode=mode)  # members of 2 to 7 columns, 1 to 4 rows
         ens.step(3)
     print("ensembles: OOB so far", count(), flush=True)
     # z launches split at 65535 row tiles: 2 columns, more than 65535 x 64 rows

@@ -54,6 +54,22 @@ def test_members_match_single_grid_runs(dtype, mode):
         assert err <= MEMBER_TOL[dtype]
 
 
+@pytest.mark.parametrize("dtype,mode", [(torch.float64, "fp64"), (torch.float64, "split"), (torch.float32, "fp64")])
+def test_tiny_members_match_single_grid_runs(dtype, mode):
+    """Members of 2 to 7 columns and 1 to 4 rows (and one of 66 x 2) beside each
+    other: each equals its single-grid run."""
+    rng = np.random.default_rng(8)
+    mem = [(member_params(nx, nz), [(rng.uniform(1, 5), rng.uniform(0.3, 0.7) * 2e4, 1000.0, 2000.0, 2000.0)])
+           for nx, nz in ((2, 1), (3, 2), (5, 3), (7, 1), (4, 4), (66, 2))]
+    ens = Ensemble(mem, dtype=dtype, f64_mode=mode)
+    ens.step(5)
+    for e, (p, bub) in enumerate(mem):
+        got = ens.member_state(e).to(torch.float64).cpu().numpy()
+        ref = single_run(p, bub, 5, dtype, mode)
+        err = max(normwise(got, ref, interior=False))
+        assert err <= MEMBER_TOL[dtype], (p["nx"], p["nz"], err)
+
+
 @pytest.mark.parametrize("mode", ["fp64", "split"])
 def test_members_vs_oracle(mode):
     mem = small_members(seed=2)[:3]
