@@ -17,13 +17,15 @@
 // so dp/dA3 = gamma p / (rho theta); at the z walls w and d3[DENS] are held at
 // zero (interpolate.py:167-173), so those paths carry no adjoint.
 //
-// Two kernels per call: one thread per interface writes (Abar, Dbar) to a
-// caller-provided workspace; one thread per cell gathers its taps.  The
-// interface kernel comes in two forms: the reference's formulas (a pow and
-// three divides per interface, f64_mode MW_F64_NATIVE) and the fewest FP64
-// operations (MW_F64_IEEE: values scaled by 12, 1/rho by a Newton step,
-// dp/d(rho theta) = gamma P_row (1 + delta)^(gamma-1) / (rho theta)_bg by its
-// binomial series, per-row constants from a table in the workspace).
+// f64_mode MW_F64_NATIVE (the reference's formulas: a pow and three divides
+// per interface) runs two kernels per call: one thread per interface writes
+// (Abar, Dbar) to a caller-provided workspace; one thread per cell gathers its
+// taps.  MW_F64_IEEE (the fewest FP64 operations: values scaled by 12, 1/rho
+// by a Newton step, dp/d(rho theta) = gamma P_row (1 + delta)^(gamma-1) /
+// (rho theta)_bg by its binomial series, per-row constants from a table in the
+// workspace) runs the same two kernels in z and, in x, one kernel that computes
+// each warp segment's interface adjoints into shared memory and gathers them
+// there.
 #include <algorithm>
 
 #include "mw_common.cuh"
@@ -278,86 +280,188 @@ __global__ void k_vjp_rows_ieee(int nz, const double* hyc, const double* hytc, c
   }
 }
 
-// The interface adjoints of k_vjp_iface (same Jacobian, same workspace
-// layout) in the fewest FP64 operations: ~43 per interface against ~300.
+// J(f)^T of one interface in the fewest FP64 operations (~43 against ~300
+// for k_vjp_iface, the same Jacobian): taps s, G = g(f) - g(f-1), the row
+// constants rv; Ab = J^T (cd G) and Db = hvcd G, with (rho w)' and d3[DENS]
+// held at zero at the z walls.  The lanes in `mask` call it together.
 template <int DIR>
-__global__ void k_vjp_iface_ieee(VjpArgs a, const RowV* rows) {
+__device__ __forceinline__ void jt_ieee(const double s[4][4], const double dg[4], const RowV& rv, double cd,
+                                        double hvcd, bool wall, unsigned mask, double Ab[4], double Db[4]) {
+  double A[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) A[q] = ieee::interp12(s[q][0], s[q][1], s[q][2], s[q][3]);
+  const double ri = ieee::rcp(A[DENS] + rv.R12, mask);
+  const double u = A[UMOM] * ri, w = A[WMOM] * ri, th = (A[RHOT] + rv.RT12) * ri;
+  // dp/dA3 = Q (1 + d)^(gamma - 1), d = (rho theta)' / (rho theta)_bg
+  const double d = A[RHOT] * rv.IRT12;
+  bool big;
+  const int deg = ieee::series_degree(d, mask, c_pow_gm1, big);
+  double dp;
+  if (deg == 1 && !__any_sync(mask, big)) {
+    dp = fma(A[RHOT], rv.QC1, rv.Q);
+  } else {
+    dp = fma(rv.Q * d, ieee::series_g(d, deg, c_pow_gm1), rv.Q);
+    if (__any_sync(mask, big)) {
+      if (big) dp = rv.Q * exp((kGamma - 1.0) * log1p(d));
+    }
+  }
+  double Fb[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    Fb[q] = cd * dg[q];
+    Db[q] = hvcd * dg[q];
+  }
+  if (DIR == MW_DIR_X) {
+    const double y = fma(Fb[1], u, fma(Fb[2], w, Fb[3] * th));  // Fb1 u + Fb2 w + Fb3 th
+    Ab[DENS] = -(u * y);
+    Ab[UMOM] = fma(Fb[1], u, Fb[0]) + y;
+    Ab[WMOM] = Fb[2] * u;
+    Ab[RHOT] = fma(Fb[1], dp, Fb[3] * u);
+  } else if (!wall) {
+    const double y = fma(Fb[1], u, fma(Fb[2], w, Fb[3] * th));
+    Ab[DENS] = -(w * y);
+    Ab[UMOM] = Fb[1] * w;
+    Ab[WMOM] = fma(Fb[2], w, Fb[0]) + y;
+    Ab[RHOT] = fma(Fb[2], dp, Fb[3] * w);
+  } else {
+    Ab[DENS] = 0.0;
+    Ab[UMOM] = 0.0;
+    Ab[WMOM] = 0.0;
+    Ab[RHOT] = Fb[2] * dp;
+    Db[DENS] = 0.0;
+  }
+}
+
+// ---- IEEE-FP64 stage adjoint, x: one kernel ---------------------------------
+// The interface adjoints (jt_ieee) and the gather of their transposed taps in
+// one pass, with no round trip through the workspace: a warp walks 29-cell
+// segments of a row; lane l computes interface f = p0-1+l into shared memory
+// and, for l < 29, gathers cell p0+l from interfaces p0-1+l .. p0+2+l in the
+// symmetric forms of k_vjp_gather.  The row is periodic: interface f takes its
+// taps and G = g(f) - g(f-1) with the periodic rule, so the reference's
+// interfaces 0 and nx, which share their taps, enter as one.
+constexpr int kFVCells = 29;
+constexpr int kFVPos = kFVCells + 6;  // forcing positions p0-3 .. p0+31
+constexpr int kFXThreads = 256;
+constexpr int kFXWarps = kFXThreads / 32;
+
+struct SmemFX {
+  double s[kFXWarps][4][kFVPos];  // forcing at positions p0-3 .. p0+31
+  double g[kFXWarps][4][33];      // g at positions p0-2 .. p0+30
+  double ab[kFXWarps][4][32];     // Ab at interfaces p0-1 .. p0+30
+  double db[kFXWarps][4][32];     // Db
+};
+// g_dst's halo cells: zero (the frame; O(perimeter) work in CTA 0).
+__device__ __forceinline__ void zero_frame(const VjpArgs& a) {
+  const int rows = a.nz + 2 * kHs;
+  const int frame = 2 * kHs * a.pitch + 2 * kHs * a.nz;  // halo rows + halo columns of interior rows
+  for (int e = threadIdx.x; e < frame; e += blockDim.x) {
+    long long o;
+    if (e < 2 * kHs * a.pitch) {
+      const int r = e / a.pitch, c = e % a.pitch;
+      o = (long long)(r < kHs ? r : rows - 2 * kHs + r) * a.pitch + c;
+    } else {
+      const int e2 = e - 2 * kHs * a.pitch;
+      const int k = e2 / (2 * kHs), h = e2 % (2 * kHs);
+      o = (long long)(k + kHs) * a.pitch + (h < kHs ? h : a.nx + h);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) MW_AT(a.gdst, q * a.plane + o, 4 * a.plane) = 0.0;
+  }
+}
+
+// g_dst of one cell from its gathered adjoints acc: + g_out (add_gout), + the bases.
+__device__ __forceinline__ void store_cell(const VjpArgs& a, long long o, const double acc[4]) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const long long oq = q * a.plane + o;
+    double v = acc[q];
+    if (a.add_gout) v += MW_AT(a.gout, oq, 4 * a.plane);
+    if (a.base_a) v += MW_AT(a.base_a, oq, 4 * a.plane);
+    if (a.base_b) v += MW_AT(a.base_b, oq, 4 * a.plane);
+    MW_AT(a.gdst, oq, 4 * a.plane) = v;
+  }
+}
+
+// The transposed taps of interfaces p0-1+l .. p0+2+l (slots l .. l+3) on their cell.
+__device__ __forceinline__ double gather4(const double* ab, const double* db, int l) {
+  const double ca = fma(7.0, ab[l + 1] + ab[l + 2], -(ab[l] + ab[l + 3])) * (1.0 / 12.0);
+  const double ce = fma(3.0, db[l + 2] - db[l + 1], db[l] - db[l + 3]);
+  return ca + ce;
+}
+
+__global__ void __launch_bounds__(kFXThreads) k_vjp_ieee_x(VjpArgs a, const RowV* rows, int nseg, long long total) {
+  __shared__ SmemFX sm;
+  if (blockIdx.x == 0) zero_frame(a);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const long long b0 = total * blockIdx.x / gridDim.x, b1 = total * (blockIdx.x + 1) / gridDim.x;
+  const long long g0 = b0 + (b1 - b0) * w / kFXWarps, g1 = b0 + (b1 - b0) * (w + 1) / kFXWarps;
+  const double cd = a.dt_stage / a.d, hvcd = -a.hv * cd;
+  auto col = [&](int p) { return ((p % a.nx) + a.nx) % a.nx + kHs; };  // periodic
+  for (long long g = g0; g < g1; ++g) {
+    const int k = (int)(g / nseg), p0 = (int)(g - (long long)k * nseg) * kFVCells;
+    const long long row = (long long)(k + kHs) * a.pitch;
+    {
+      const int cA = col(p0 - 3 + lane), cB = col(p0 + 29 + lane), cG = col(p0 - 1 + lane), cH = col(p0 - 2);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        sm.s[w][q][lane] = MW_VF(a, q * a.plane + row + cA);
+        if (lane < 3) sm.s[w][q][32 + lane] = MW_VF(a, q * a.plane + row + cB);
+        sm.g[w][q][lane + 1] = MW_AT(a.gout, q * a.plane + row + cG, 4 * a.plane);
+        if (lane == 0) sm.g[w][q][0] = MW_AT(a.gout, q * a.plane + row + cH, 4 * a.plane);
+      }
+    }
+    __syncwarp();
+    {  // interface f = p0 - 1 + lane
+      double s[4][4], dg[4], Ab[4], Db[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) s[q][j] = sm.s[w][q][lane + j];
+        dg[q] = sm.g[w][q][lane + 1] - sm.g[w][q][lane];
+      }
+      const RowV rv = MW_AT(rows, k + kHs, 2 * a.nz + 5);
+      jt_ieee<MW_DIR_X>(s, dg, rv, cd, hvcd, false, 0xffffffffu, Ab, Db);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        sm.ab[w][q][lane] = Ab[q];
+        sm.db[w][q][lane] = Db[q];
+      }
+    }
+    __syncwarp();
+    const int t = p0 + lane;  // cell
+    if (lane < kFVCells && t < a.nx) {
+      double acc[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[q] = gather4(sm.ab[w][q], sm.db[w][q], lane);
+      store_cell(a, row + t + kHs, acc);
+    }
+    __syncwarp();
+  }
+}
+
+// z: the interface adjoints of k_vjp_iface (same Jacobian, same workspace
+// layout) by jt_ieee, one thread per interface; k_vjp_gather follows.  (A
+// fused z kernel over tiles of 4 columns x 29 rows staged through shared
+// memory was slower at 512 x 256: 39.6 against 18.8 + 17.7 us per call.)
+__global__ void k_vjp_iface_ieee_z(VjpArgs a, const RowV* rows) {
   const long long n = a.nif;
-  const double cd = a.dt_stage / a.d, hvcd = -a.hv * cd;  // Fbar = cd dg, Dbar = -hv Fbar = hvcd dg
+  const double cd = a.dt_stage / a.d, hvcd = -a.hv * cd;
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride) {
     const long long idx = base + threadIdx.x;
     const unsigned mask = __ballot_sync(0xffffffffu, idx < n);  // base is uniform over the block
     if (idx >= n) continue;
-    double s[4][4], dg[4];
-    bool wall = false;
-    RowV rv;
-    if (DIR == MW_DIR_X) {
-      const int k = (int)(idx / (a.nx + 1)), i = (int)(idx % (a.nx + 1));
-      const long long row = (long long)(k + kHs) * a.pitch;
+    const int k = (int)(idx / a.nx), c = (int)(idx % a.nx);
+    double s[4][4], dg[4], Ab[4], Db[4];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const long long col = wrap_x(i - 2 + j, a.nx) + kHs;
+    for (int j = 0; j < 4; ++j)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) s[q][j] = MW_VF(a, q * a.plane + row + col);
-      }
+      for (int q = 0; q < 4; ++q) s[q][j] = zval(a, q, k - 2 + j, c + kHs);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) dg[q] = (i < a.nx ? gval(a, q, k, i) : 0.0) - (i > 0 ? gval(a, q, k, i - 1) : 0.0);
-      rv = MW_AT(rows, k + kHs, 2 * a.nz + 5);
-    } else {
-      const int k = (int)(idx / a.nx), c = (int)(idx % a.nx);
-#pragma unroll
-      for (int j = 0; j < 4; ++j)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) s[q][j] = zval(a, q, k - 2 + j, c + kHs);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) dg[q] = (k < a.nz ? gval(a, q, k, c) : 0.0) - (k > 0 ? gval(a, q, k - 1, c) : 0.0);
-      rv = MW_AT(rows, a.nz + 2 * kHs + k, 2 * a.nz + 5);
-      wall = (k == 0) || (k == a.nz);
-    }
-    double A[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) A[q] = ieee::interp12(s[q][0], s[q][1], s[q][2], s[q][3]);
-    const double ri = ieee::rcp(A[DENS] + rv.R12, mask);
-    const double u = A[UMOM] * ri, w = A[WMOM] * ri, th = (A[RHOT] + rv.RT12) * ri;
-    // dp/dA3 = Q (1 + d)^(gamma - 1), d = (rho theta)' / (rho theta)_bg
-    const double d = A[RHOT] * rv.IRT12;
-    bool big;
-    const int deg = ieee::series_degree(d, mask, c_pow_gm1, big);
-    double dp;
-    if (deg == 1 && !__any_sync(mask, big)) {
-      dp = fma(A[RHOT], rv.QC1, rv.Q);
-    } else {
-      dp = fma(rv.Q * d, ieee::series_g(d, deg, c_pow_gm1), rv.Q);
-      if (__any_sync(mask, big)) {
-        if (big) dp = rv.Q * exp((kGamma - 1.0) * log1p(d));
-      }
-    }
-    double Fb[4], Db[4], Ab[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      Fb[q] = cd * dg[q];
-      Db[q] = hvcd * dg[q];
-    }
-    if (DIR == MW_DIR_X) {
-      const double y = fma(Fb[1], u, fma(Fb[2], w, Fb[3] * th));  // Fb1 u + Fb2 w + Fb3 th
-      Ab[DENS] = -(u * y);
-      Ab[UMOM] = fma(Fb[1], u, Fb[0]) + y;
-      Ab[WMOM] = Fb[2] * u;
-      Ab[RHOT] = fma(Fb[1], dp, Fb[3] * u);
-    } else if (!wall) {
-      const double y = fma(Fb[1], u, fma(Fb[2], w, Fb[3] * th));
-      Ab[DENS] = -(w * y);
-      Ab[UMOM] = Fb[1] * w;
-      Ab[WMOM] = fma(Fb[2], w, Fb[0]) + y;
-      Ab[RHOT] = fma(Fb[2], dp, Fb[3] * w);
-    } else {
-      Ab[DENS] = 0.0;
-      Ab[UMOM] = 0.0;
-      Ab[WMOM] = 0.0;
-      Ab[RHOT] = Fb[2] * dp;
-      Db[DENS] = 0.0;
-    }
+    for (int q = 0; q < 4; ++q) dg[q] = (k < a.nz ? gval(a, q, k, c) : 0.0) - (k > 0 ? gval(a, q, k - 1, c) : 0.0);
+    const RowV rv = MW_AT(rows, a.nz + 2 * kHs + k, 2 * a.nz + 5);
+    jt_ieee<MW_DIR_Z>(s, dg, rv, cd, hvcd, k == 0 || k == a.nz, mask, Ab, Db);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       MW_WS(a, q * n + idx) = Ab[q];
@@ -473,18 +577,31 @@ static int vjp_stage(int nx, int nz, double dx, double dz, double dt_full, const
     k_vjp_rows_ieee<<<grid_for(2 * nz + 5, 128), 128, 0, s>>>(nz, hyc, hytc, hyi, hyti, hypi, rows);
     if ((st = check_launch("vjp row-table launch"))) return st;
   }
+  if (f64_mode == MW_F64_IEEE && direction == MW_DIR_X) {  // one fused launch, a grid of resident CTAs at most
+    int per_sm = 0, sms = 0, dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_vjp_ieee_x, kFXThreads, 0);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return fail(MW_ERR_CUDA, "vjp occupancy query: %s", cudaGetErrorString(e));
+    const long long resident = (long long)std::max(1, per_sm) * sms;
+    const int nseg = (nx + kFVCells - 1) / kFVCells;
+    const long long total = (long long)nseg * nz;
+    const long long grid = std::max(1LL, std::min(resident, (total + kFXWarps - 1) / kFXWarps));
+    k_vjp_ieee_x<<<(unsigned)grid, kFXThreads, 0, s>>>(a, rows, nseg, total);
+    return check_launch("vjp launch");
+  }
+  if (f64_mode == MW_F64_IEEE) {
+    k_vjp_iface_ieee_z<<<grid_for(a.nif, 128), 128, 0, s>>>(a, rows);
+    if ((st = check_launch("vjp interface launch"))) return st;
+    k_vjp_gather<MW_DIR_Z><<<gather_grid(g), 128, 0, s>>>(a);
+    return check_launch("vjp gather launch");
+  }
   if (direction == MW_DIR_X) {
-    if (f64_mode == MW_F64_IEEE)
-      k_vjp_iface_ieee<MW_DIR_X><<<grid_for(a.nif, 128), 128, 0, s>>>(a, rows);
-    else
-      k_vjp_iface<MW_DIR_X><<<grid_for(a.nif, 128), 128, 0, s>>>(a);
+    k_vjp_iface<MW_DIR_X><<<grid_for(a.nif, 128), 128, 0, s>>>(a);
     if ((st = check_launch("vjp interface launch"))) return st;
     k_vjp_gather<MW_DIR_X><<<gather_grid(g), 128, 0, s>>>(a);
   } else {
-    if (f64_mode == MW_F64_IEEE)
-      k_vjp_iface_ieee<MW_DIR_Z><<<grid_for(a.nif, 128), 128, 0, s>>>(a, rows);
-    else
-      k_vjp_iface<MW_DIR_Z><<<grid_for(a.nif, 128), 128, 0, s>>>(a);
+    k_vjp_iface<MW_DIR_Z><<<grid_for(a.nif, 128), 128, 0, s>>>(a);
     if ((st = check_launch("vjp interface launch"))) return st;
     k_vjp_gather<MW_DIR_Z><<<gather_grid(g), 128, 0, s>>>(a);
   }
