@@ -152,10 +152,12 @@ def test_ensemble_plan_validation():
     assert info.n_x_items == 32 + 50
     assert info.n_z_items == 1 * 2 + 2 * 4  # (64-column blocks) x (16-row tiles) per member
     assert info.bytes % 16 == 0 and info.z_items_off >= info.x_items_off + 8 * info.n_x_items
-    # the split form's row-constant table: one 32-byte entry per cell-centre background value used
+    # the FP64 forms' row-constant table: one 40-byte entry per cell-centre background value used
     assert info.n_xrows == max(0 + 32 + 4, 36 + 50 + 4)
     assert info.xrows_off >= info.z_items_off + 8 * info.n_z_items and info.xrows_off % 16 == 0
-    assert info.bytes >= info.xrows_off + 32 * info.n_xrows
+    # then the members' stage constants (6 x 88 bytes each, 16-byte aligned), then the 16-byte work cursor last
+    consts = (info.xrows_off + 40 * info.n_xrows + 15) // 16 * 16
+    assert info.bytes == (consts + 2 * 6 * 88 + 15) // 16 * 16 + 16
     bad = (M * 2)(M(64, 32, 312.5, 312.5, 0.1, 0, 0, 0), M(100, 50, 200.0, 200.0, 0.1, 100, 36, 33))
     assert L.mw_ensemble_plan_info(2, bad, 16, ctypes.byref(info)) == ALIAS
     assert L.mw_ensemble_plan_info(2, mem, 65, ctypes.byref(info)) == INVALID
