@@ -344,7 +344,8 @@ __device__ __forceinline__ void x_rowrun_t(const StageArgs<T>& a, int k, int cbe
 // bring later rows / segments into L2 without holding registers.  Measured on
 // the 256-member thermal ensemble (ms per step): none 1.474, z 2 rows ahead
 // 1.410 (1, 3, 4, 8: 1.40-1.44 with x), x 1 segment 1.453, both (x 2, z 2) 1.393;
-// x 3 segments ahead 1.406, x prefetched into L1 instead of L2 1.391.
+// x 3 segments ahead 1.406, x prefetched into L1 instead of L2 1.391; the next
+// row taken one row early and its first lines prefetched 1.430.
 #ifndef MW_F32_PF_Z
 #define MW_F32_PF_Z 2  // FP32 z march: L2 prefetch of the rows this many steps ahead (0: none)
 #endif
