@@ -351,18 +351,21 @@ struct SmemFX {
   double ab[kFXWarps][4][32];     // Ab at interfaces p0-1 .. p0+30
   double db[kFXWarps][4][32];     // Db
 };
-// g_dst's halo cells: zero (the frame; O(perimeter) work in CTA 0).
+
+// g_dst's halo cells: zero (the frame, strided over every thread of the launch).
 __device__ __forceinline__ void zero_frame(const VjpArgs& a) {
   const int rows = a.nz + 2 * kHs;
-  const int frame = 2 * kHs * a.pitch + 2 * kHs * a.nz;  // halo rows + halo columns of interior rows
-  for (int e = threadIdx.x; e < frame; e += blockDim.x) {
+  const long long hrow = 2LL * kHs * a.pitch;               // the halo rows' cells
+  const long long frame = hrow + 2LL * kHs * a.nz;          // + the halo columns of the interior rows
+  const long long step = (long long)gridDim.x * blockDim.x;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < frame; e += step) {
     long long o;
-    if (e < 2 * kHs * a.pitch) {
-      const int r = e / a.pitch, c = e % a.pitch;
+    if (e < hrow) {
+      const int r = (int)(e / a.pitch), c = (int)(e % a.pitch);
       o = (long long)(r < kHs ? r : rows - 2 * kHs + r) * a.pitch + c;
     } else {
-      const int e2 = e - 2 * kHs * a.pitch;
-      const int k = e2 / (2 * kHs), h = e2 % (2 * kHs);
+      const long long e2 = e - hrow;
+      const int k = (int)(e2 / (2 * kHs)), h = (int)(e2 % (2 * kHs));
       o = (long long)(k + kHs) * a.pitch + (h < kHs ? h : a.nx + h);
     }
 #pragma unroll
@@ -392,7 +395,7 @@ __device__ __forceinline__ double gather4(const double* ab, const double* db, in
 
 __global__ void __launch_bounds__(kFXThreads) k_vjp_ieee_x(VjpArgs a, const RowV* rows, int nseg, long long total) {
   __shared__ SmemFX sm;
-  if (blockIdx.x == 0) zero_frame(a);
+  zero_frame(a);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const long long b0 = total * blockIdx.x / gridDim.x, b1 = total * (blockIdx.x + 1) / gridDim.x;
   const long long g0 = b0 + (b1 - b0) * w / kFXWarps, g1 = b0 + (b1 - b0) * (w + 1) / kFXWarps;

@@ -304,18 +304,20 @@ __device__ __forceinline__ void vjp_segments(const VjpSplitArgs& a, int nseg, lo
   }
 }
 
-// Halo cells of g_dst: zero (the whole frame; O(perimeter) work in CTA 0).
+// g_dst's halo cells: zero (the frame, strided over every thread of the launch).
 __device__ __forceinline__ void zero_frame(const VjpSplitArgs& a) {
   const int rows = a.nz + 2 * kHs;
-  const int frame = 2 * kHs * a.pitch + 2 * kHs * a.nz;  // halo rows + halo columns of interior rows
-  for (int e = threadIdx.x; e < frame; e += blockDim.x) {
+  const long long hrow = 2LL * kHs * a.pitch;               // the halo rows' cells
+  const long long frame = hrow + 2LL * kHs * a.nz;          // + the halo columns of the interior rows
+  const long long step = (long long)gridDim.x * blockDim.x;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < frame; e += step) {
     long long o;
-    if (e < 2 * kHs * a.pitch) {
-      const int r = e / a.pitch, c = e % a.pitch;
+    if (e < hrow) {
+      const int r = (int)(e / a.pitch), c = (int)(e % a.pitch);
       o = (long long)(r < kHs ? r : rows - 2 * kHs + r) * a.pitch + c;
     } else {
-      const int e2 = e - 2 * kHs * a.pitch;
-      const int k = e2 / (2 * kHs), h = e2 % (2 * kHs);
+      const long long e2 = e - hrow;
+      const int k = (int)(e2 / (2 * kHs)), h = (int)(e2 % (2 * kHs));
       o = (long long)(k + kHs) * a.pitch + (h < kHs ? h : a.nx + h);
     }
 #pragma unroll
@@ -329,7 +331,7 @@ __device__ __forceinline__ void zero_frame(const VjpSplitArgs& a) {
 template <int DIR>
 __global__ void __launch_bounds__(kVThreads) k_vjp_split(VjpSplitArgs a, int nseg, long long total) {
   __shared__ SmemV sm;
-  if (blockIdx.x == 0) zero_frame(a);
+  zero_frame(a);
   const long long g0 = total * blockIdx.x / gridDim.x, g1 = total * (blockIdx.x + 1) / gridDim.x;
   const int w = threadIdx.x >> 5;
   const long long n = g1 - g0;
@@ -361,7 +363,7 @@ struct SmemVZ {
 __global__ void __launch_bounds__(kZTThreads) k_vjp_split_zt(VjpSplitArgs a, int nseg, int ncb, long long total) {
   extern __shared__ __align__(16) unsigned char vz_raw[];
   SmemVZ& sm = *reinterpret_cast<SmemVZ*>(vz_raw);
-  if (blockIdx.x == 0) zero_frame(a);
+  zero_frame(a);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const dw hv12 = ld(a.hv12);
   const dw2 hv = splat(hv12);
