@@ -335,10 +335,6 @@ __device__ __forceinline__ void x_rowrun_t(const StageArgs<T>& a, int k, int cbe
   }
 }
 
-// z: columns [cb*NC, cb*NC+NC) (NC threads), rows [z0, z0+zt), zt <= kEnsZTileMax; one
-// thread per column marching the rows with a rolling 4-row window, the next
-// row loaded one step ahead.  halo: write the wall halo rows of these columns
-// (cb == 0 also does the four x-halo columns).
 // The plain-load FP32 passes wait on memory (one row or segment of loads in
 // flight per thread, no registers to spare for more): prefetch instructions
 // bring later rows / segments into L2 without holding registers.  Measured on
@@ -356,6 +352,10 @@ __device__ __forceinline__ void prefetch_l2(const void* p) {
   asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
 }
 
+// z: columns [cb*NC, cb*NC+NC) (NC threads), rows [z0, z0+zt), zt <= kEnsZTileMax; one
+// thread per column marching the rows with a rolling 4-row window, the next
+// row loaded one step ahead.  halo: write the wall halo rows of these columns
+// (cb == 0 also does the four x-halo columns).
 template <typename T, int MODE, int NC = kZThreads>
 __device__ __forceinline__ void z_tile_t(const StageArgs<T>& a, int cb, int z0, int zt, bool halo, SmemZT& sm) {
   const int z1 = min(z0 + zt, a.nz);
