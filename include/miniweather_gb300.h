@@ -241,9 +241,12 @@ int mw_ensemble_step_f32(void* plan_device, const mw_ens_plan_info* info, const 
  * (a halo value's adjoint returns to the cell it was copied or scaled from),
  * the hyperviscosity and the gravity term.  Arrays are (4, nz+4, nx+4) FP64;
  * a base may be g_dst itself (accumulation); g_dst must not overlap g_out or
- * forcing.  f64_mode: MW_F64_NATIVE or MW_F64_IEEE (FP64 arithmetic, two
- * kernels) or MW_F64_SPLIT (double-FP32 interior arithmetic as the split
- * forward, one kernel after a small background-table kernel).
+ * forcing.  f64_mode: MW_F64_NATIVE (FP64 arithmetic, the reference's
+ * formulas: an interface kernel then a gather), MW_F64_IEEE (FP64 arithmetic
+ * with the fewest operations, after a small background-table kernel: one
+ * kernel in x, an interface kernel then the gather in z) or MW_F64_SPLIT
+ * (double-FP32 interior arithmetic as the split forward, one kernel after a
+ * small background-table kernel).
  * workspace: mw_dirstage_vjp_workspace_bytes.
  * ------------------------------------------------------------------------- */
 size_t mw_dirstage_vjp_workspace_bytes(int nx, int nz);

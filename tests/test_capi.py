@@ -178,3 +178,21 @@ def test_thermal_ensemble_generator():
     assert 0.35 < np.mean(np.array(nx) < 256) < 0.65
     cells = sum(m[0]["nx"] * m[0]["nz"] for m in a)
     assert 15e6 < cells < 35e6
+
+
+def test_python_constants_match_the_header():
+    """The flag, enum and limit constants of the Python binding are the header's."""
+    import os
+    import re
+    text = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                             "miniweather_gb300.h")).read()
+    found = {}
+    for name, val in re.findall(r"#define\s+(MW_[A-Z0-9_]+)\s+(\d+)u?\b", text):
+        found[name] = int(val)
+    for name, val in re.findall(r"\b(MW_[A-Z0-9_]+)\s*=\s*(\d+)\s*[,}/]", text):
+        found[name] = int(val)
+    names = [n for n in dir(_native) if n.startswith("MW_") and isinstance(getattr(_native, n), int)]
+    assert len(names) >= 14
+    for n in names:
+        assert n in found, n
+        assert getattr(_native, n) == found[n], n
