@@ -422,6 +422,28 @@ def test_host_step_matches_copy_step_copy(nx, nz, nbands, flags, mode):
         assert torch.equal(got.state, ref.state) and torch.equal(got.state_tmp, ref.state_tmp), step
 
 
+@pytest.mark.parametrize("mode", ["fp64", "split"])
+def test_host_step_pageable_host_arrays(mode):
+    """evolve_host with pageable (not page-locked) host tensors: the copies are
+    staged by the host, the banded step gives the bits of pinned arrays."""
+    from pyminiweather_gb300.solve import evolve_host
+    p = make_params(256, 128, "thermal")
+    p["f64_mode"] = mode
+    outs = []
+    for pinned in (True, False):
+        f = initialize_fields(p)
+        init(f, p, None)
+        h = f.state.cpu()
+        h = h.pin_memory() if pinned else h.clone()
+        assert h.is_pinned() == pinned
+        reset_direction()
+        for _ in range(3):
+            evolve_host(p, f, h, h, dt=p["dt"], nbands=8)
+        torch.cuda.synchronize()
+        outs.append((h.clone(), f.state.clone()))
+    assert torch.equal(outs[0][0], outs[1][0]) and torch.equal(outs[0][1], outs[1][1])
+
+
 def test_host_step_fp32_and_native_forms():
     from pyminiweather_gb300.solve import evolve_host
     for dtype, mode in ((torch.float32, "split"), (torch.float64, "native")):
